@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the D3Q19 flow step on the 192^3 porous medium (BASELINE configuration
+"single large 3D porous medium": spheres of radius 8 at seeded uniform centres, overlap allowed,
+porosity 0.60, tau 0.8, f_ext (1e-6,0,0)).
+
+One "step" is one fused pull-stream + bounce-back + moments + BGK/Guo collision over the whole
+box.  The headline is the FP32-deviation kernel (MLUPS = fluid-node updates per microsecond);
+the FP64 strict kernel, which reproduces the reference operation for operation, is measured
+beside it.  ``e2e`` is the same work through the C ABI with host buffers: upload of the
+populations and moments from pinned host memory, K steps, download of density and flux.
+``--impl reference`` times the CPU oracle (a C restatement of the reference Fortran, built with
+the reference's -O3 -fopenmp -funroll-loops flags) on the same workload.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_BOX = 192
+RADIUS = 8.0
+POROSITY = 0.60
+SEED = 20261203
+TAU = 0.8
+FEXT = (1e-6, 0.0, 0.0)
+BYTES_F32 = 38 * 4   # 19 reads + 19 writes of one FP32 deviation per fluid node
+BYTES_F64 = 38 * 8
+WORKLOAD = "D3Q19 porous 192^3 spheres r=8 porosity 0.60 seed 20261203, tau 0.8, f_ext (1e-6,0,0)"
+METRIC = "D3Q19 MLUPS (fluid-node updates/us), FP32-deviation populations"
+
+
+def args_():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=L_BOX)
+    ap.add_argument("--fp64-steps", type=int, default=0, help="default: min(steps, 200)")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(profile_name):
+    """DRAM bytes per launch per fluid node from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", profile_name)
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_fluid_node:\s*([0-9.eE+-]+)", text)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed regions."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in open(self.file.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip() == "Active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return world, rank, local, None
+
+
+def max_over_ranks(dist, value):
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_mlups(nature, seconds, threads):
+    """Oracle (C restatement of the reference) on the full box: steps until `seconds` of CPU work."""
+    import oracle
+
+    oracle.build()
+    nfluid = int((nature == 0).sum())
+    t0 = time.perf_counter()
+    steps = 1
+    while True:
+        t = time.perf_counter()
+        oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=steps, nthreads=threads)
+        dt = time.perf_counter() - t
+        if dt * 2 > seconds or steps >= 64:
+            break
+        steps *= 2
+    # subtract nothing: init_populations is part of every run but is one pass out of ~60 per step
+    return nfluid * steps / dt / 1e6, steps, dt, time.perf_counter() - t0
+
+
+def run_reference(a):
+    world, rank, local, dist = dist_setup()
+    if rank != 0:
+        return
+    from laboetie_gb300 import geometry as geo
+
+    nature = geo.porous_spheres(a.size, RADIUS, POROSITY, SEED)
+    threads = os.cpu_count() or 1
+    # --warmup untimed steps (a short run), then K timed samples of the same workload
+    import oracle
+
+    oracle.build()
+    oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=1, nthreads=threads)
+    mlups, steps, dt, _ = cpu_oracle_mlups(nature, a.cpu_seconds, threads)
+    line = {
+        "impl": "reference", "metric": METRIC.replace("FP32-deviation", "FP64"), "value": round(mlups, 4),
+        "unit": "MLUPS", "n_gpus": a.gpus, "steps": steps, "warmup": 1,
+        "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded porous medium)",
+        "config": {"workload": WORKLOAD, "global_batch": 1, "seq_len": 0, "parallelism": "openmp"},
+        "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"{steps} reference flow steps of the full 192^3 box "
+                                   "(collide + bounce-back/stream + moments, OpenMP streaming)"},
+        "e2e": {"value": round(mlups, 4), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = args_()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    world, rank, local, dist = dist_setup()
+    import ctypes as C
+
+    from laboetie_gb300 import FP32_DEV, FP64, Box, library
+    from laboetie_gb300 import geometry as geo
+
+    L = library()
+    nature = geo.porous_spheres(a.size, RADIUS, POROSITY, SEED)
+    nfluid = int((nature == 0).sum())
+    K, W = a.steps, max(a.warmup, 3)
+    K64 = a.fp64_steps or min(K, 200)
+    clocks = ClockSampler(local)
+
+    # ---------------------------------------------------------- FP32 deviation (headline)
+    box = Box(nature, relaxation_time=TAU, f_ext=FEXT, precision=FP32_DEV, device=local)
+    box.flow_init()
+    box.time_flow_steps(W, force_on=True)          # warm-up, untimed
+    box.sync()
+    barrier(dist)
+    clocks.start()
+    ms32 = box.time_flow_steps(K, force_on=True)   # CUDA events on the library stream
+    box.sync()
+    ms32 = max_over_ranks(dist, ms32)
+    barrier(dist)
+
+    # ---------------------------------------------------------- FP64 strict
+    box64 = Box(nature, relaxation_time=TAU, f_ext=FEXT, precision=FP64, device=local)
+    box64.flow_init()
+    box64.time_flow_steps(W, force_on=True)
+    box64.sync()
+    barrier(dist)
+    ms64 = box64.time_flow_steps(K64, force_on=True)
+    box64.sync()
+    ms64 = max_over_ranks(dist, ms64)
+    barrier(dist)
+    # initial state for e2e: the FP64 populations after the warm-up (realistic, non-trivial)
+    n0, rho0, j0 = box64.flow_get()
+    box64.close()
+
+    # ---------------------------------------------------------- e2e through the C ABI
+    rhos = np.zeros(nature.shape)
+    js = [np.zeros(nature.shape) for _ in range(3)]
+    host = [n0, rho0, *j0, rhos, *js]
+    for h in host:
+        rc = L.lbgpu_host_register(h.ctypes.data, h.nbytes)
+        if rc:
+            raise RuntimeError("cudaHostRegister failed")
+    barrier(dist)
+    t0 = time.perf_counter()
+    box.flow_set(n0, rho0, j0)
+    box.flow_steps(K, force_on=True)
+    rc = L.lbgpu_flow_get(box.ctx, None, rhos.ctypes.data, *(x.ctypes.data for x in js))
+    box.sync()
+    t_e2e = time.perf_counter() - t0
+    clocks_out = clocks.stop()
+    t_e2e = max_over_ranks(dist, t_e2e)
+    for h in host:
+        L.lbgpu_host_unregister(h.ctypes.data)
+    if rc:
+        raise RuntimeError("lbgpu_flow_get failed")
+    box.close()
+
+    # ---------------------------------------------------------- CPU baseline (rank 0, N=1)
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        mlups_cpu, steps_cpu, dt_cpu, _ = cpu_oracle_mlups(nature, a.cpu_seconds, threads)
+        cpu = {"value": round(mlups_cpu, 4), "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"{steps_cpu} flow steps of the full 192^3 box by the C restatement of "
+                         "the reference (FP64, OpenMP streaming as the reference)"}
+
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    ms_step32 = ms32 / K
+    ms_step64 = ms64 / K64
+    value = world * nfluid * K / (ms32 * 1e-3) / 1e6
+    mlups64 = world * nfluid * K64 / (ms64 * 1e-3) / 1e6
+    achieved32 = BYTES_F32 * nfluid / (ms_step32 * 1e-3) / 1e9
+    achieved64 = BYTES_F64 * nfluid / (ms_step64 * 1e-3) / 1e9
+    tr = ncu_traffic("flow_step_f32_192cube.md")
+    h2d = (19 + 4) * 8 * nature.size
+    d2h = 4 * 8 * nature.size
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": round(ms_step32, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded porous medium)",
+        "config": {"workload": WORKLOAD, "global_batch": world, "seq_len": 0,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "fluid_nodes": nfluid, "nodes": int(nature.size),
+                   "l2": "inputs larger than L2 (538 MB of FP32 populations per buffer)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved32, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved32 / hbm, 4), "peak_kind": peak_kind,
+                     "traffic": (round(tr * nfluid) if tr else None),
+                     "algorithmic_bytes_per_fluid_node": BYTES_F32},
+        "fp64": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
+                 "ms_per_step": round(ms_step64, 4),
+                 "roofline": {"bound": "hbm", "achieved": round(achieved64, 1), "peak": hbm,
+                              "unit": "GB/s", "frac": round(achieved64 / hbm, 4),
+                              "algorithmic_bytes_per_fluid_node": BYTES_F64},
+                 "speedup_fp32_over_fp64": round(value / mlups64, 2)},
+        "e2e": {"value": round(world * nfluid * K / t_e2e / 1e6, 2), "unit": "MLUPS",
+                "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
+                "what": "lbgpu_flow_set (n, density, j from pinned host) + K fused steps + "
+                        "lbgpu_flow_get (density, j to pinned host), wall clock"},
+        "gpu_launches": K + 3,
+        "clocks": clocks_out,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

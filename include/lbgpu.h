@@ -1,0 +1,164 @@
+/*
+ * lbgpu.h -- C ABI of the GB300 (sm_103a) lattice-Boltzmann library for laboetie.
+ *
+ * The Fortran host of laboetie (maxlevesque/laboetie) keeps lb.in parsing, geometry and all
+ * output; through iso_c_binding it calls these entry points in place of its hot loops:
+ *
+ *   collide / bounce-back / streaming / moments   src/module_collision.f90:15,
+ *                                                 src/equilibration.f90:143-491
+ *   tracer moment propagation + VACF              src/drop_tracers.f90:63-123,
+ *                                                 src/module_moment_propagation.f90:30-289
+ *   Poisson solve + Nernst-Planck update          src/sor.f90:7-91, src/just_eq_smolu.f90:6-135,
+ *                                                 src/poisson_nernst_planck.f90:38-48
+ *
+ * Conventions
+ *   - Every host array is a 1-based Fortran array passed by address: column-major, x fastest.
+ *     A field f(lx,ly,lz) has element (i,j,k) at f[(i-1) + lx*((j-1) + ly*(k-1))].
+ *     Flow populations are n(lx,ly,lz,19) (equilibration.f90 layout, velocity slowest).
+ *     Tracer quantities P(3,lx,ly,lz) have the component fastest (module_moment_propagation.f90:138).
+ *   - nature: int8, 0 = fluid, 1 = solid (module_system.f90:32).
+ *   - Velocity index l is the reference's order (module_lbmodel.f90:68-86).
+ *   - Every function returns an int status: 0 = LBGPU_OK, otherwise a bit mask of
+ *     lbgpu_status; lbgpu_last_error() gives the message.  The reference has no error returns
+ *     (it STOPs), so the Fortran shim maps a non-zero status to ERROR STOP.
+ *   - A context owns all device memory and one CUDA stream; it is not thread-safe.  One context
+ *     per host thread.  The library never falls back to the CPU: without a usable GPU,
+ *     lbgpu_create() fails with LBGPU_ERR_CUDA.
+ */
+#ifndef LBGPU_H
+#define LBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBGPU_ABI_VERSION 1
+
+typedef struct lbgpu_ctx lbgpu_ctx;
+
+/* Status bits.  Several may be set at once. */
+enum lbgpu_status {
+    LBGPU_OK = 0,
+    LBGPU_ERR_INVALID = 1 << 0,            /* bad argument or call order */
+    LBGPU_ERR_CUDA = 1 << 1,               /* CUDA runtime error, or no GPU */
+    LBGPU_ERR_NEGATIVE_POPULATION = 1 << 2,/* equilibration.f90:248 "n(x,y,z,vel) < 0" */
+    LBGPU_ERR_NONFINITE = 1 << 3,          /* a population or moment became NaN/Inf */
+    LBGPU_ERR_FRACTION = 1 << 4,           /* module_moment_propagation.f90:249 "restpart is negative" */
+    LBGPU_ERR_STEP_CAP = 1 << 5,           /* step / iteration cap reached without convergence */
+    LBGPU_ERR_OOM = 1 << 6,                /* device memory budget exceeded */
+    LBGPU_ERR_FLUX_SUM = 1 << 7,           /* just_eq_smolu.f90:108-112 "sum of all flux does not add up" */
+    LBGPU_ERR_CHARGE = 1 << 8,             /* charge_test.f90:20-24 "charge is not conserved" */
+    LBGPU_ERR_UNSUPPORTED = 1 << 9,        /* an input the reference has no defined result for */
+    LBGPU_ERR_TIMEOUT = 1 << 10            /* a device-side wait ran out of its iteration limit */
+};
+
+/* Storage / arithmetic of the flow and tracer populations. */
+enum lbgpu_precision {
+    LBGPU_FP64 = 0,      /* plain FP64, the reference's arithmetic operation by operation */
+    LBGPU_FP32_DEV = 1   /* FP32 deviations f - w*rho0 with FP32 collision; FP64 sums */
+};
+
+typedef struct {
+    int lx, ly, lz;              /* lb.in lx, ly, lz (equilibration.f90:40-42) */
+    int precision;               /* enum lbgpu_precision */
+    double relaxation_time;      /* lb.in relaxation_time (module_collision.f90:38), > 0.5 */
+    double target_error;         /* lb.in target_error (equilibration.f90:57), default 1e-10 */
+    double f_ext[3];             /* lb.in f_ext (equilibration.f90:379, drop_tracers.f90:92) */
+    double rho0;                 /* lb.in initialSolventDensity (init_simu.f90:283) */
+    int device;                  /* CUDA device ordinal */
+} lbgpu_params;
+
+/* Fill *p with the reference defaults for a lx*ly*lz box (tau 1, target 1e-10, rho0 1). */
+void lbgpu_default_params(lbgpu_params *p, int lx, int ly, int lz);
+
+/* Create a context for one box: copies the geometry to the device, classifies every node
+ * (fluid/solid, interfacial as supercell_definition.f90:115-147) and allocates the flow state.
+ * Replaces the allocations of equilibration.f90:59-119. */
+int lbgpu_create(const lbgpu_params *p, const int8_t *nature, lbgpu_ctx **out);
+void lbgpu_destroy(lbgpu_ctx *ctx);
+
+/* Copy the message of the last failed call into buf (always NUL-terminated). */
+int lbgpu_last_error(const lbgpu_ctx *ctx, char *buf, size_t len);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* detectInterfacialNodes (supercell_definition.f90:115-147): out[node] = 1 if any of the 18
+ * periodic neighbours has a different nature, else 0. */
+int lbgpu_interfacial(lbgpu_ctx *ctx, uint8_t *out);
+
+/* counts[0..3] = fluid, solid, fluid&interfacial, solid&interfacial node counts. */
+int lbgpu_node_counts(lbgpu_ctx *ctx, long long counts[4]);
+
+/* ---------------------------------------------------------------- flow: state transfer */
+
+/* init_simu.f90:283-291 on the device: density = rho0 on fluid, 0 on solid; n_l = w_l*density;
+ * j = 0 and the force field = 0 (equilibration.f90:75-80,94-96). */
+int lbgpu_flow_init(lbgpu_ctx *ctx);
+
+/* n(lx,ly,lz,19), density, jx, jy, jz: host <-> device copies of the device-resident state.
+ * After lbgpu_flow_steps / lbgpu_equilibration, get returns the populations n after the last
+ * streaming and the moments of that step (the reference's state at loop exit). */
+int lbgpu_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const double *jx,
+                   const double *jy, const double *jz);
+int lbgpu_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double *jy,
+                   double *jz);
+
+/* ---------------------------------------------------------------- flow: reference operators
+ * One call = one reference operator on host arrays (copied in and out on every call).  These
+ * let the Fortran loop of equilibration.f90 stay as it is, statement for statement. */
+
+/* collide(n, density, jx, jy, jz, f_ext_x, f_ext_y, f_ext_z), module_collision.f90:15-108:
+ * n (lx,ly,lz,19) is updated in place on fluid nodes. */
+int lbgpu_collide(lbgpu_ctx *ctx, double *n, const double *density, const double *jx,
+                  const double *jy, const double *jz, const double *f_ext_x,
+                  const double *f_ext_y, const double *f_ext_z);
+
+/* Halfway bounce-back swap + periodic streaming, equilibration.f90:204-243: n in place. */
+int lbgpu_bounce_back_stream(lbgpu_ctx *ctx, double *n);
+
+/* equilibration.f90:248,254,266-268,293-300,339-343: density = SUM(n,4);
+ * j = f_ext/2 + sum_l n_l c_l; *l2err = max|j - j_old| with j_old read from jx/jy/jz on entry.
+ * Returns LBGPU_ERR_NEGATIVE_POPULATION if any n < 0 (results are still written). */
+int lbgpu_moments(lbgpu_ctx *ctx, const double *n, const double *f_ext_x,
+                  const double *f_ext_y, const double *f_ext_z, double *density, double *jx,
+                  double *jy, double *jz, double *l2err);
+
+/* ---------------------------------------------------------------- flow: device-resident loop */
+
+enum lbgpu_flow_mode {
+    LBGPU_FLOW_FIXED = 0,     /* nsteps steps with the current force, no convergence test */
+    LBGPU_FLOW_REFERENCE = 1  /* equilibration.f90:143-491 semantics, see lbgpu_equilibration */
+};
+
+/* Run the flow phase of equilibration.f90:143-491 on the device: fused collide + bounce-back +
+ * stream + moments + l2err each step, the two-phase f_ext state machine (force switched on at
+ * the first convergence, exit at the second) evaluated on the device between steps.
+ * Stops at convergence or after max_steps (LBGPU_ERR_STEP_CAP).  l2err_hist (optional,
+ * capacity hist_cap) receives l2err(t) for t = 1..steps (the output/l2err.dat series).
+ * *steps_out = the exit step t. */
+int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap,
+                        int *steps_out);
+
+/* Fixed-step flow: nsteps fused steps with the force of the given phase (0 = no force,
+ * 1 = f_ext on fluid nodes), no convergence test (the timing mode). */
+int lbgpu_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on);
+
+/* Time nsteps fixed steps with CUDA events on the context's stream (one launch per step,
+ * replayed from a CUDA graph).  *ms = elapsed device time. */
+int lbgpu_time_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms);
+
+/* Wait for all work of the context. */
+int lbgpu_sync(lbgpu_ctx *ctx);
+
+/* Page-lock (pin) an existing host array so that the copies of the calls above run at full
+ * host<->device bandwidth, e.g. the Fortran host's n(:,:,:,:).  Unregister before freeing it. */
+int lbgpu_host_register(void *ptr, size_t bytes);
+int lbgpu_host_unregister(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,94 @@
+// ctx.h -- the library context: device allocations and host-side bookkeeping of one box.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "common.cuh"
+#include "lbgpu.h"
+
+namespace lbg {
+
+// Small device-resident results of the operator kernels.
+struct Scratch {
+    unsigned long long err_bits;
+    unsigned status;
+    unsigned pad;
+    unsigned long long counts[4];
+};
+
+// How the populations in the "previous" buffer relate to the state the host asks for.
+enum PrevKind { PREV_NONE = 0, PREV_RAW = 1, PREV_POST = 2 };
+
+// Operator-mode scratch (lbgpu_collide & co.): populations in/out, moments, force field.
+struct OpBuffers {
+    double *n[2] = {nullptr, nullptr};
+    double *m[4] = {nullptr, nullptr, nullptr, nullptr};  // rho, jx, jy, jz
+    double *F[3] = {nullptr, nullptr, nullptr};
+};
+
+struct MpState;   // tracer moment propagation (mp.cu)
+struct PnpState;  // Poisson-Nernst-Planck (pnp.cu)
+
+}  // namespace lbg
+
+struct lbgpu_ctx {
+    lbgpu_params p{};
+    long long N = 0;
+    unsigned long long counts[4] = {0, 0, 0, 0};
+    std::string last_error;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // geometry
+    int8_t *d_nature = nullptr;
+    uint32_t *d_mask = nullptr;
+
+    // flow state.  FP64: d_f[2] doubles; FP32 deviation: d_g[2] floats.
+    double *d_f[2] = {nullptr, nullptr};
+    float *d_g[2] = {nullptr, nullptr};
+    double *d_j[3] = {nullptr, nullptr, nullptr};
+    double *d_rho = nullptr;
+    lbg::FlowCtl *d_ctl = nullptr;
+    lbg::Scratch *d_scratch = nullptr;
+    lbg::LbConst64 K64{};
+
+    int cur = 0;                 // buffer read by the next step
+    int prev_kind = lbg::PREV_NONE;
+    int prev_force_moment = 0;   // f_ext in the moments of the state held in buffer 1-cur
+    int force_last_collide = 0;  // f_ext in the collision that produced buffer cur
+    bool moments_valid = false;  // d_rho / d_j hold the moments of the state
+
+    // cached CUDA graphs of the step loop
+    cudaGraphExec_t graph_ref = nullptr;
+    int graph_ref_len = 0;
+    cudaGraphExec_t graph_fixed[2] = {nullptr, nullptr};  // [force_on], two steps each
+    int graph_fixed_parity[2] = {-1, -1};
+
+    lbg::OpBuffers *op = nullptr;
+    lbg::MpState *mp = nullptr;
+    lbg::PnpState *pnp = nullptr;
+};
+
+namespace lbg {
+
+int ctx_fail(lbgpu_ctx *ctx, int code, const std::string &msg);
+int ctx_cuda(lbgpu_ctx *ctx, cudaError_t e, const char *what);
+int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature);
+void ctx_release_device(lbgpu_ctx *ctx);
+LbConst64 make_const64(double tau);
+struct FlowArgs64;
+void fill_args64(lbgpu_ctx *ctx, FlowArgs64 &a);
+int force_mask(const double f[3]);
+void mp_release(lbgpu_ctx *ctx);
+void pnp_release(lbgpu_ctx *ctx);
+
+#define LBG_CK(ctx, call)                                                   \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) return ::lbg::ctx_cuda((ctx), e_, #call);   \
+    } while (0)
+
+}  // namespace lbg

@@ -1,0 +1,277 @@
+// flow_f32.cu -- FP32-deviation D3Q19 kernels.
+//
+// Populations are stored as single-precision deviations d_l = f_l - w_l*rho0 from the rest
+// state of density rho0 (lb.in initialSolventDensity).  Since sum_l w_l c_l = 0 and
+// w_l = w_inv(l), the deviations stream and bounce back exactly like f, the momentum is
+// j = F/2 + sum_l d_l c_l, and BGK relaxes d the same way it relaxes f:
+//   d*_l = (1-1/tau) d_l + (1/tau) dneq_l + (1-1/(2 tau)) T_l
+//   dneq_l = w_l (rho - rho0) + a1_l (c.j) + a2_l ((c.j)(c.u) - cs^2 (j.u))
+//   T_l    = a1_l (c.F - u.F) + 2 a2_l (c.u)(c.F)
+// which is module_collision.f90:87-104 with the a2 double sum written as a contraction.
+// Storing deviations keeps the ~7 significant digits of FP32 for the flow signal rather than
+// for the rest density.  Moments handed back to the host are accumulated in FP64.
+#include <cfloat>
+
+#include "common.cuh"
+#include "flow.h"
+#include "lbgpu.h"
+
+namespace lbg {
+namespace {
+
+constexpr int BLOCK = 256;
+
+template <int CX, int CY, int CZ>
+__device__ __forceinline__ float dotf(float x, float y, float z)
+{
+    float s = 0.0f;
+    if constexpr (CX > 0) s += x;
+    if constexpr (CX < 0) s -= x;
+    if constexpr (CY > 0) s += y;
+    if constexpr (CY < 0) s -= y;
+    if constexpr (CZ > 0) s += z;
+    if constexpr (CZ < 0) s -= z;
+    return s;
+}
+
+struct Coords32 {
+    int X[3], Y[3], Z[3];
+};
+
+__device__ __forceinline__ Coords32 coords32(unsigned node, int lx, int ly, int lz)
+{
+    Coords32 k;
+    const int x = (int)(node % (unsigned)lx);
+    const unsigned yz = node / (unsigned)lx;
+    const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
+    const int sy = lx, sz = lx * ly;
+    k.X[0] = wrap_plus(x, lx);       k.X[1] = x;       k.X[2] = wrap_minus(x, lx);
+    k.Y[0] = wrap_plus(y, ly) * sy;  k.Y[1] = y * sy;  k.Y[2] = wrap_minus(y, ly) * sy;
+    k.Z[0] = wrap_plus(z, lz) * sz;  k.Z[1] = z * sz;  k.Z[2] = wrap_minus(z, lz) * sz;
+    return k;
+}
+
+__device__ __forceinline__ void pull19f(float (&g)[Q], const float *__restrict__ src,
+                                        unsigned node, uint32_t m, const Coords32 &k, size_t N)
+{
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        if constexpr (l == 0) {
+            g[0] = __ldg(src + node);
+        } else {
+            const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);
+            g[l] = ((m >> l) & 1u) ? __ldg(src + (size_t)inv(l) * N + node)
+                                   : __ldg(src + (size_t)l * N + s);
+        }
+    });
+}
+
+template <int FMASK>
+__device__ __forceinline__ void collide_dev(float (&g)[Q], const float drho, const float jx,
+                                            const float jy, const float jz, const FlowArgs32 &a,
+                                            const bool force)
+{
+    const float rho = a.rho0 + drho;
+    const float ir = 1.0f / rho;
+    const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
+    const float ju = jx * ux + jy * uy + jz * uz;
+    const float cs2 = 1.0f / 3.0f;
+    float uF = 0.0f;
+    if (FMASK && force) uF = ux * a.F[0] + uy * a.F[1] + uz * a.F[2];
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        constexpr int w = wclass(l);
+        const float cj = dotf<c.x, c.y, c.z>(jx, jy, jz);
+        const float cu = dotf<c.x, c.y, c.z>(ux, uy, uz);
+        const float neq = a.w[w] * drho + a.a1[w] * cj + a.a2[w] * (cj * cu - cs2 * ju);
+        float r = a.c1 * g[l] + a.c2 * neq;
+        if constexpr (FMASK != 0) {
+            if (force) {
+                const float cF = dotf<(FMASK & 1) ? c.x : 0, (FMASK & 2) ? c.y : 0, (FMASK & 4) ? c.z : 0>(
+                    a.F[0], a.F[1], a.F[2]);
+                r += a.c3 * (a.a1[w] * (cF - uF) + a.two_a2[w] * cu * cF);
+            }
+        }
+        g[l] = r;
+    });
+}
+
+// Fused pull-stream + moments + collision, FP32 deviations.
+template <int FMASK>
+__global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
+{
+    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
+    if (node >= (unsigned)a.N) return;
+    const uint32_t m = __ldg(a.mask + node);
+    if (!(m & FLUID_BIT)) return;
+    const float *__restrict__ src = a.parity ? a.g1 : a.g0;
+    float *__restrict__ dst = a.parity ? a.g0 : a.g1;
+    const size_t N = (size_t)a.N;
+    const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
+    float g[Q];
+    pull19f(g, src, node, m, k, N);
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        drho += g[l];
+        if constexpr (c.x > 0) jx += g[l];
+        if constexpr (c.x < 0) jx -= g[l];
+        if constexpr (c.y > 0) jy += g[l];
+        if constexpr (c.y < 0) jy -= g[l];
+        if constexpr (c.z > 0) jz += g[l];
+        if constexpr (c.z < 0) jz -= g[l];
+    });
+    if (FMASK && a.force_moment) {
+        jx += 0.5f * a.F[0];
+        jy += 0.5f * a.F[1];
+        jz += 0.5f * a.F[2];
+    }
+    collide_dev<FMASK>(g, drho, jx, jy, jz, a, a.force_collide != 0);
+#pragma unroll
+    for (int l = 0; l < Q; ++l) __stcs(dst + (size_t)l * N + node, g[l]);
+}
+
+// Zero deviations: the rest state rho = rho0, j = 0 (init_simu.f90:283-291 on fluid nodes).
+__global__ void __launch_bounds__(BLOCK) k_init32(const FlowArgs32 a)
+{
+    const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
+    const size_t total = (size_t)Q * (size_t)a.N;
+    if (i < total) {
+        a.g0[i] = 0.0f;
+        a.g1[i] = 0.0f;
+    }
+}
+
+// Moments in FP64 (and optionally f = d + w rho0) of the populations in buffer `parity`
+// (after streaming when PULL, else as stored); solid nodes report the reference's zeros.
+template <bool PULL>
+__global__ void __launch_bounds__(BLOCK) k_finalize32(const FlowArgs32 a)
+{
+    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
+    if (node >= (unsigned)a.N) return;
+    const uint32_t m = a.mask[node];
+    const size_t N = (size_t)a.N;
+    if (!(m & FLUID_BIT)) {
+        a.rho[node] = 0.0;
+        a.jx[node] = 0.0;
+        a.jy[node] = 0.0;
+        a.jz[node] = 0.0;
+        if (a.nout)
+            for (int l = 0; l < Q; ++l) a.nout[(size_t)l * N + node] = 0.0;
+        return;
+    }
+    const float *__restrict__ src = a.parity ? a.g1 : a.g0;
+    float g[Q];
+    if constexpr (PULL) {
+        const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
+        pull19f(g, src, node, m, k, N);
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[l] = src[(size_t)l * N + node];
+    }
+    double drho = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        const double v = (double)g[l];
+        drho += v;
+        jx += c.x * v;
+        jy += c.y * v;
+        jz += c.z * v;
+        if (a.nout) a.nout[(size_t)l * N + node] = v + a.w64[wclass(l)] * a.rho0d;
+    });
+    if (a.force_moment) {
+        jx += 0.5 * (double)a.F[0];
+        jy += 0.5 * (double)a.F[1];
+        jz += 0.5 * (double)a.F[2];
+    }
+    a.rho[node] = a.rho0d + drho;
+    a.jx[node] = jx;
+    a.jy[node] = jy;
+    a.jz[node] = jz;
+}
+
+// Collision of raw deviations in buffer `parity` with the given FP64 density and flux
+// (a.rho, a.j*), written to the other buffer (the start of a step, module_collision.f90:15).
+template <int FMASK>
+__global__ void __launch_bounds__(BLOCK) k_collide32(const FlowArgs32 a)
+{
+    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
+    if (node >= (unsigned)a.N) return;
+    const size_t N = (size_t)a.N;
+    const float *__restrict__ src = a.parity ? a.g1 : a.g0;
+    float *__restrict__ dst = a.parity ? a.g0 : a.g1;
+    float g[Q];
+#pragma unroll
+    for (int l = 0; l < Q; ++l) g[l] = src[(size_t)l * N + node];
+    if (a.mask[node] & FLUID_BIT) {
+        const float drho = (float)(a.rho[node] - a.rho0d);
+        collide_dev<FMASK>(g, drho, (float)a.jx[node], (float)a.jy[node], (float)a.jz[node], a,
+                           a.force_collide != 0);
+    }
+#pragma unroll
+    for (int l = 0; l < Q; ++l) dst[(size_t)l * N + node] = g[l];
+}
+
+// d_l = n_l - w_l rho0 for every node: FP64 host populations into FP32 deviations.
+__global__ void __launch_bounds__(BLOCK) k_to_dev32(const FlowArgs32 a, const double *__restrict__ n,
+                                                    float *__restrict__ out)
+{
+    const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
+    const size_t N = (size_t)a.N;
+    if (i >= (size_t)Q * N) return;
+    const int l = (int)(i / N);
+    out[i] = (float)(n[i] - a.w64[wclass(l)] * a.rho0d);
+}
+
+}  // namespace
+
+cudaError_t launch_to_dev32(const FlowArgs32 &a, const double *n, float *out, cudaStream_t s)
+{
+    const size_t total = (size_t)Q * (size_t)a.N;
+    k_to_dev32<<<(unsigned)((total + BLOCK - 1) / BLOCK), BLOCK, 0, s>>>(a, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_collide_f32(const FlowArgs32 &a, cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    int fm = (a.F[0] != 0.0f ? 1 : 0) | (a.F[1] != 0.0f ? 2 : 0) | (a.F[2] != 0.0f ? 4 : 0);
+    if (fm) k_collide32<7><<<grid, BLOCK, 0, s>>>(a);
+    else k_collide32<0><<<grid, BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_t s)
+{
+    if (!grid) grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    int fm = (a.F[0] != 0.0f ? 1 : 0) | (a.F[1] != 0.0f ? 2 : 0) | (a.F[2] != 0.0f ? 4 : 0);
+    switch (fm) {
+    case 0: k_step32<0><<<grid, BLOCK, 0, s>>>(a); break;
+    case 1: k_step32<1><<<grid, BLOCK, 0, s>>>(a); break;
+    case 2: k_step32<2><<<grid, BLOCK, 0, s>>>(a); break;
+    case 4: k_step32<4><<<grid, BLOCK, 0, s>>>(a); break;
+    default: k_step32<7><<<grid, BLOCK, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_f32(const FlowArgs32 &a, cudaStream_t s)
+{
+    const size_t total = (size_t)Q * (size_t)a.N;
+    k_init32<<<(unsigned)((total + BLOCK - 1) / BLOCK), BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_f32(const FlowArgs32 &a, bool pull, cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    if (pull) k_finalize32<true><<<grid, BLOCK, 0, s>>>(a);
+    else k_finalize32<false><<<grid, BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace lbg

@@ -1,0 +1,166 @@
+// flow_f32_api.cu -- host side of the FP32-deviation flow path (same C ABI as FP64).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+#include "flow.h"
+#include "lbgpu.h"
+
+namespace lbg {
+
+static void fill_args32(lbgpu_ctx *ctx, FlowArgs32 &a)
+{
+    std::memset(&a, 0, sizeof(a));
+    const LbConst64 &K = ctx->K64;
+    a.mask = ctx->d_mask;
+    a.g0 = ctx->d_g[0];
+    a.g1 = ctx->d_g[1];
+    a.jx = ctx->d_j[0];
+    a.jy = ctx->d_j[1];
+    a.jz = ctx->d_j[2];
+    a.rho = ctx->d_rho;
+    a.N = ctx->N;
+    a.lx = ctx->p.lx;
+    a.ly = ctx->p.ly;
+    a.lz = ctx->p.lz;
+    for (int w = 0; w < 3; ++w) {
+        a.w[w] = (float)K.a0[w];
+        a.a1[w] = (float)K.a1[w];
+        a.a2[w] = (float)K.a2[w];
+        a.two_a2[w] = (float)K.two_a2[w];
+        a.w64[w] = K.a0[w];
+    }
+    a.c1 = (float)K.c1;
+    a.c2 = (float)K.c2;
+    a.c3 = (float)K.c3;
+    a.rho0 = (float)ctx->p.rho0;
+    a.rho0d = ctx->p.rho0;
+    for (int d = 0; d < 3; ++d) a.F[d] = (float)ctx->p.f_ext[d];
+}
+
+int f32_flow_init(lbgpu_ctx *ctx)
+{
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    LBG_CK(ctx, launch_init_f32(a, ctx->stream));
+    ctx->cur = 0;
+    ctx->prev_kind = PREV_RAW;
+    ctx->prev_force_moment = 0;
+    ctx->force_last_collide = 0;
+    LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return LBGPU_OK;
+}
+
+int f32_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const double *jx,
+                 const double *jy, const double *jz)
+{
+    const long long N = ctx->N;
+    cudaStream_t s = ctx->stream;
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    double *tmp = nullptr;
+    LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
+    LBG_CK(ctx, cudaMemcpyAsync(tmp, n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
+    LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->d_g[1], s));
+    LBG_CK(ctx, cudaFreeAsync(tmp, s));
+    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_rho, density, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    const double *j[3] = {jx, jy, jz};
+    for (int q = 0; q < 3; ++q)
+        LBG_CK(ctx, cudaMemcpyAsync(ctx->d_j[q], j[q], sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    a.parity = 1;
+    a.force_collide = ctx->force_last_collide;
+    LBG_CK(ctx, launch_collide_f32(a, s));
+    ctx->cur = 0;
+    ctx->prev_kind = PREV_RAW;
+    ctx->prev_force_moment = ctx->force_last_collide;
+    LBG_CK(ctx, cudaStreamSynchronize(s));
+    return LBGPU_OK;
+}
+
+int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double *jy, double *jz)
+{
+    if (ctx->prev_kind == PREV_NONE)
+        return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_flow_get: no flow state (call lbgpu_flow_init)");
+    const long long N = ctx->N;
+    cudaStream_t s = ctx->stream;
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    a.parity = 1 - ctx->cur;
+    a.force_moment = ctx->prev_force_moment;
+    double *tmp = nullptr;
+    if (n) {
+        LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
+        a.nout = tmp;
+    }
+    LBG_CK(ctx, launch_finalize_f32(a, ctx->prev_kind == PREV_POST, s));
+    if (n) LBG_CK(ctx, cudaMemcpyAsync(n, tmp, sizeof(double) * Q * N, cudaMemcpyDeviceToHost, s));
+    if (density) LBG_CK(ctx, cudaMemcpyAsync(density, ctx->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    double *j[3] = {jx, jy, jz};
+    for (int q = 0; q < 3; ++q)
+        if (j[q]) LBG_CK(ctx, cudaMemcpyAsync(j[q], ctx->d_j[q], sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    if (tmp) LBG_CK(ctx, cudaFreeAsync(tmp, s));
+    LBG_CK(ctx, cudaStreamSynchronize(s));
+    return LBGPU_OK;
+}
+
+int f32_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
+{
+    cudaStream_t s = ctx->stream;
+    force_on = force_on ? 1 : 0;
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    auto one = [&]() -> int {
+        a.parity = ctx->cur;
+        a.force_moment = ctx->force_last_collide;
+        a.force_collide = force_on;
+        LBG_CK(ctx, launch_flow_step_f32(a, 0, s));
+        ctx->prev_force_moment = ctx->force_last_collide;
+        ctx->force_last_collide = force_on;
+        ctx->cur ^= 1;
+        ctx->prev_kind = PREV_POST;
+        return LBGPU_OK;
+    };
+    int rc;
+    if (!ms) {
+        for (int t = 0; t < nsteps; ++t)
+            if ((rc = one())) return rc;
+        return LBGPU_OK;
+    }
+    if (ctx->force_last_collide != force_on)
+        if ((rc = one())) return rc;
+    if (!ctx->graph_fixed[force_on] || ctx->graph_fixed_parity[force_on] != ctx->cur) {
+        if (ctx->graph_fixed[force_on]) cudaGraphExecDestroy(ctx->graph_fixed[force_on]);
+        cudaGraph_t g;
+        LBG_CK(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < 2; ++k) {
+            a.parity = ctx->cur ^ k;
+            a.force_moment = force_on;
+            a.force_collide = force_on;
+            cudaError_t e = launch_flow_step_f32(a, 0, s);
+            if (e != cudaSuccess) {
+                cudaStreamEndCapture(s, &g);
+                return ctx_cuda(ctx, e, "capture");
+            }
+        }
+        LBG_CK(ctx, cudaStreamEndCapture(s, &g));
+        LBG_CK(ctx, cudaGraphInstantiate(&ctx->graph_fixed[force_on], g, 0));
+        cudaGraphDestroy(g);
+        ctx->graph_fixed_parity[force_on] = ctx->cur;
+    }
+    LBG_CK(ctx, cudaEventRecord(ctx->ev0, s));
+    for (int k = 0; k < nsteps / 2; ++k) LBG_CK(ctx, cudaGraphLaunch(ctx->graph_fixed[force_on], s));
+    if (nsteps & 1) {
+        if ((rc = one())) return rc;
+    } else if (nsteps > 0) {
+        ctx->prev_force_moment = force_on;
+        ctx->prev_kind = PREV_POST;
+    }
+    LBG_CK(ctx, cudaEventRecord(ctx->ev1, s));
+    LBG_CK(ctx, cudaEventSynchronize(ctx->ev1));
+    LBG_CK(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    return LBGPU_OK;
+}
+
+}  // namespace lbg

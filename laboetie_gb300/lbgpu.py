@@ -1,0 +1,272 @@
+"""ctypes binding of liblbgpu (include/lbgpu.h) and a Box class mirroring the reference calls.
+
+Arrays use the reference's memory order: a field f(lx,ly,lz) is a numpy array of shape
+(lz, ly, lx) (x fastest), flow populations n(lx,ly,lz,19) are (19, lz, ly, lx) and tracer
+quantities P(3,lx,ly,lz) are (lz, ly, lx, 3).  Every call goes to the GPU library; a non-zero
+status raises LbgpuError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "_build", "liblbgpu.so")
+
+FP64 = 0
+FP32_DEV = 1
+
+STATUS = {
+    1 << 0: "invalid argument", 1 << 1: "CUDA error", 1 << 2: "negative population",
+    1 << 3: "non-finite value", 1 << 4: "remaining fraction below eps", 1 << 5: "step cap",
+    1 << 6: "out of device memory", 1 << 7: "flux sum not zero", 1 << 8: "charge not conserved",
+    1 << 9: "unsupported", 1 << 10: "device wait timed out",
+}
+ERR_NEGATIVE_POPULATION = 1 << 2
+ERR_FRACTION = 1 << 4
+ERR_STEP_CAP = 1 << 5
+ERR_OOM = 1 << 6
+
+
+class LbgpuError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        names = [v for k, v in STATUS.items() if status & k]
+        super().__init__(f"{message} [status {status}: {', '.join(names)}]")
+        self.status = status
+
+
+class Params(C.Structure):
+    """lbgpu_params (include/lbgpu.h)."""
+    _fields_ = [
+        ("lx", C.c_int), ("ly", C.c_int), ("lz", C.c_int), ("precision", C.c_int),
+        ("relaxation_time", C.c_double), ("target_error", C.c_double),
+        ("f_ext", C.c_double * 3), ("rho0", C.c_double), ("device", C.c_int),
+    ]
+
+
+class Tracer(C.Structure):
+    """lbgpu_tracer (include/lbgpu.h): the lb.in tracer tags of drop_tracers.f90 and
+    module_moment_propagation.f90."""
+    _fields_ = [
+        ("Db", C.c_double), ("ka", C.c_double), ("kd", C.c_double), ("Ds", C.c_double),
+        ("z", C.c_double), ("f_ext", C.c_double * 3), ("elec_slope", C.c_double * 3),
+    ]
+
+
+class PnpParams(C.Structure):
+    """lbgpu_pnp_params (include/lbgpu.h)."""
+    _fields_ = [
+        ("bjl", C.c_double), ("sigma", C.c_double), ("lambda_D", C.c_double),
+        ("D_plus", C.c_double), ("D_minus", C.c_double), ("charge_distrib", C.c_int),
+        ("solver", C.c_int), ("omega", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int),
+        ("np_loop_bug", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def library():
+    """Load liblbgpu.so (building it first if it is missing).  Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        from . import build as _build
+
+        _build.build()
+    L = C.CDLL(_LIB_PATH)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    pi = C.POINTER(C.c_int)
+    L.lbgpu_default_params.argtypes = [C.POINTER(Params), i, i, i]
+    L.lbgpu_default_params.restype = None
+    L.lbgpu_create.argtypes = [C.POINTER(Params), vp, C.POINTER(vp)]
+    L.lbgpu_destroy.argtypes = [vp]
+    L.lbgpu_destroy.restype = None
+    L.lbgpu_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.lbgpu_interfacial.argtypes = [vp, vp]
+    L.lbgpu_node_counts.argtypes = [vp, vp]
+    L.lbgpu_flow_init.argtypes = [vp]
+    L.lbgpu_flow_set.argtypes = [vp] * 6
+    L.lbgpu_flow_get.argtypes = [vp] * 6
+    L.lbgpu_collide.argtypes = [vp] * 9
+    L.lbgpu_bounce_back_stream.argtypes = [vp, vp]
+    L.lbgpu_moments.argtypes = [vp] * 10
+    L.lbgpu_equilibration.argtypes = [vp, i, vp, i, pi]
+    L.lbgpu_flow_steps.argtypes = [vp, i, i]
+    L.lbgpu_time_flow_steps.argtypes = [vp, i, i, C.POINTER(C.c_float)]
+    L.lbgpu_sync.argtypes = [vp]
+    L.lbgpu_host_register.argtypes = [vp, C.c_size_t]
+    L.lbgpu_host_unregister.argtypes = [vp]
+    for name, args in (
+        ("lbgpu_mp_init", [vp, C.POINTER(Tracer), vp, vp, vp, vp, vp]),
+        ("lbgpu_mp_propagate", [vp, i, vp, pi, pi]),
+        ("lbgpu_mp_get", [vp, vp, vp]),
+        ("lbgpu_mp_release", [vp]),
+        ("lbgpu_time_mp_steps", [vp, i, C.POINTER(C.c_float)]),
+        ("lbgpu_pnp_init", [vp, C.POINTER(PnpParams), C.POINTER(d)]),
+        ("lbgpu_pnp_set", [vp, vp, vp, vp, d]),
+        ("lbgpu_pnp_get", [vp, vp, vp, vp, C.POINTER(d)]),
+        ("lbgpu_sor", [vp, pi]),
+        ("lbgpu_just_eq_smolu", [vp, pi]),
+        ("lbgpu_poisson_nernst_planck", [vp, i, pi, pi]),
+        ("lbgpu_charge_test", [vp, C.POINTER(d), C.POINTER(d)]),
+    ):
+        if hasattr(L, name):
+            getattr(L, name).argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a, shape):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+class Box:
+    """One simulation box on the GPU (an lbgpu context).
+
+    ``nature`` is an int8 array of shape (lz, ly, lx) with 0 = fluid, 1 = solid.
+    """
+
+    def __init__(self, nature, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0), target_error=1e-10,
+                 rho0=1.0, precision=FP64, device=0):
+        self.L = library()
+        nature = np.ascontiguousarray(nature, dtype=np.int8)
+        if nature.ndim != 3:
+            raise ValueError("nature must be (lz, ly, lx)")
+        self.shape = nature.shape
+        lz, ly, lx = nature.shape
+        self.N = nature.size
+        p = Params()
+        self.L.lbgpu_default_params(C.byref(p), lx, ly, lz)
+        p.relaxation_time = relaxation_time
+        p.target_error = target_error
+        p.f_ext = (C.c_double * 3)(*f_ext)
+        p.rho0 = rho0
+        p.precision = precision
+        p.device = device
+        self.params = p
+        self.ctx = C.c_void_p()
+        rc = self.L.lbgpu_create(C.byref(p), nature.ctypes.data, C.byref(self.ctx))
+        if rc:
+            raise LbgpuError(rc, self._msg(None))
+        self.nature = nature
+
+    # -------------------------------------------------------------- helpers
+    def _msg(self, ctx):
+        buf = C.create_string_buffer(1024)
+        self.L.lbgpu_last_error(ctx, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _chk(self, rc, what=""):
+        if rc:
+            raise LbgpuError(rc, f"{what}: {self._msg(self.ctx)}")
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.lbgpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -------------------------------------------------------------- geometry
+    def interfacial(self):
+        out = np.zeros(self.shape, dtype=np.uint8)
+        self._chk(self.L.lbgpu_interfacial(self.ctx, out.ctypes.data), "interfacial")
+        return out
+
+    def node_counts(self):
+        c = (C.c_longlong * 4)()
+        self._chk(self.L.lbgpu_node_counts(self.ctx, c), "node_counts")
+        return dict(fluid=c[0], solid=c[1], fluid_interfacial=c[2], solid_interfacial=c[3])
+
+    # -------------------------------------------------------------- flow state
+    def flow_init(self):
+        self._chk(self.L.lbgpu_flow_init(self.ctx), "flow_init")
+
+    def flow_set(self, n, rho, j):
+        pshape = (19,) + self.shape
+        n = _f64(n, pshape)
+        rho = _f64(rho, self.shape)
+        jx, jy, jz = (_f64(x, self.shape) for x in j)
+        self._chk(self.L.lbgpu_flow_set(self.ctx, _ptr(n), _ptr(rho), _ptr(jx), _ptr(jy), _ptr(jz)),
+                  "flow_set")
+
+    def flow_get(self, populations=True):
+        n = np.zeros((19,) + self.shape) if populations else None
+        rho = np.zeros(self.shape)
+        j = [np.zeros(self.shape) for _ in range(3)]
+        self._chk(self.L.lbgpu_flow_get(self.ctx, _ptr(n), _ptr(rho), *(_ptr(x) for x in j)),
+                  "flow_get")
+        return n, rho, tuple(j)
+
+    # -------------------------------------------------------------- reference operators
+    def collide(self, n, rho, j, f):
+        """module_collision.f90 collide(n, density, jx, jy, jz, f_ext_x, f_ext_y, f_ext_z)."""
+        n = np.array(n, dtype=np.float64, order="C").reshape((19,) + self.shape)
+        a = [_f64(x, self.shape) for x in (rho, *j, *f)]
+        self._chk(self.L.lbgpu_collide(self.ctx, _ptr(n), *(_ptr(x) for x in a)), "collide")
+        return n
+
+    def bounce_back_stream(self, n):
+        """equilibration.f90:204-243."""
+        n = np.array(n, dtype=np.float64, order="C").reshape((19,) + self.shape)
+        self._chk(self.L.lbgpu_bounce_back_stream(self.ctx, _ptr(n)), "bounce_back_stream")
+        return n
+
+    def moments(self, n, f, j_old):
+        """equilibration.f90:248-343: returns (status, rho, j, l2err)."""
+        n = _f64(n, (19,) + self.shape)
+        f = [_f64(x, self.shape) for x in f]
+        j = [np.array(x, dtype=np.float64, order="C").reshape(self.shape) for x in j_old]
+        rho = np.zeros(self.shape)
+        err = C.c_double(0)
+        rc = self.L.lbgpu_moments(self.ctx, _ptr(n), *(_ptr(x) for x in f), _ptr(rho),
+                                  *(_ptr(x) for x in j), C.byref(err))
+        if rc and rc != ERR_NEGATIVE_POPULATION:
+            self._chk(rc, "moments")
+        return rc, rho, tuple(j), err.value
+
+    # -------------------------------------------------------------- device loop
+    def equilibration(self, max_steps=0, hist_cap=0):
+        """equilibration.f90:143-491 on the device.  Returns (steps, l2err history)."""
+        hist = np.zeros(hist_cap) if hist_cap else None
+        steps = C.c_int(0)
+        rc = self.L.lbgpu_equilibration(self.ctx, max_steps, _ptr(hist), hist_cap, C.byref(steps))
+        self._chk(rc, "equilibration")
+        return steps.value, (hist[: min(steps.value, hist_cap)] if hist is not None else None)
+
+    def flow_steps(self, nsteps, force_on=True):
+        self._chk(self.L.lbgpu_flow_steps(self.ctx, nsteps, int(force_on)), "flow_steps")
+
+    def time_flow_steps(self, nsteps, force_on=True):
+        ms = C.c_float(0)
+        self._chk(self.L.lbgpu_time_flow_steps(self.ctx, nsteps, int(force_on), C.byref(ms)),
+                  "time_flow_steps")
+        return ms.value
+
+    def sync(self):
+        self._chk(self.L.lbgpu_sync(self.ctx), "sync")

@@ -1,0 +1,212 @@
+"""Parity of the GPU flow path (C ABI) with the CPU oracle.
+
+FP64 results must be bit-identical (numpy array_equal; +0 and -0 compare equal): the kernels
+evaluate every operation of the Fortran source in the same order with separate roundings.
+The FP32-deviation path is checked against FP64 with the tolerance stated in each test.
+"""
+import numpy as np
+import pytest
+
+from laboetie_gb300 import FP32_DEV, FP64, Box, LbgpuError
+from laboetie_gb300 import geometry as geo
+
+pytestmark = pytest.mark.gpu
+
+
+def random_nature(shape, solid_frac, seed):
+    rng = np.random.default_rng(seed)
+    nat = (rng.random(shape) < solid_frac).astype(np.int8)
+    nat.flat[0] = 0
+    return nat
+
+
+def random_state(nature, seed, amp=0.02):
+    """A positive population field with its own density and a random flux."""
+    import oracle
+
+    rng = np.random.default_rng(seed)
+
+    c, inv, a0, a1, a2, de = oracle.tables()
+    n = a0[:, None, None, None] * (1.0 + amp * rng.standard_normal((19,) + nature.shape))
+    n[:, nature == 1] = rng.random((19, int((nature == 1).sum()))) * 0.05
+    rho = n.sum(axis=0)
+    j = [(n * c[:, d][:, None, None, None]).sum(axis=0) + amp * rng.standard_normal(nature.shape)
+         for d in range(3)]
+    return n, rho, j
+
+
+GEOMS = [
+    ("slit", lambda: geo.slit(4, 4, 12)),
+    ("cylinder", lambda: geo.cylinder(9, 9, 5)),
+    ("cc", lambda: geo.cc(8, 8, 8)),
+    ("cavity", lambda: geo.spherical_cavity(7, 7, 7)),
+    ("tube", lambda: geo.tube_varying_diameter(10, 9, 9)),
+    ("random", lambda: random_nature((6, 5, 7), 0.3, 1)),
+    ("thin-x", lambda: random_nature((9, 8, 1), 0.25, 2)),
+    ("thin-2", lambda: random_nature((2, 3, 2), 0.3, 3)),
+]
+
+
+@pytest.mark.parametrize("name,make", GEOMS)
+def test_interfacial_and_counts_bit_exact(oracle_mod, name, make):
+    nat = make()
+    with Box(nat) as box:
+        got = box.interfacial()
+        want = oracle_mod.detect_interfacial(nat)
+        assert np.array_equal(got, want)
+        cnt = box.node_counts()
+        assert cnt["fluid"] == int((nat == 0).sum())
+        assert cnt["solid"] == int((nat == 1).sum())
+        assert cnt["fluid_interfacial"] == int(((nat == 0) & (want == 1)).sum())
+        assert cnt["solid_interfacial"] == int(((nat == 1) & (want == 1)).sum())
+
+
+@pytest.mark.parametrize("fkind", ["field", "x-only", "zero"])
+@pytest.mark.parametrize("tau", [1.0, 0.8, 1.7])
+def test_collide_operator_bit_exact(oracle_mod, fkind, tau):
+    nat = random_nature((6, 7, 5), 0.3, 11)
+    n, rho, j = random_state(nat, 5)
+    rng = np.random.default_rng(7)
+    if fkind == "field":
+        f = [1e-3 * rng.standard_normal(nat.shape) * (nat == 0) for _ in range(3)]
+    elif fkind == "x-only":
+        f = [np.where(nat == 0, 1e-5, 0.0), np.zeros(nat.shape), np.zeros(nat.shape)]
+    else:
+        f = [np.zeros(nat.shape) for _ in range(3)]
+    with Box(nat, relaxation_time=tau) as box:
+        got = box.collide(n, rho, j, f)
+    want = oracle_mod.collide(nat, tau, n, rho, j, f)
+    assert np.array_equal(got, want)
+
+
+def test_bounce_back_stream_operator_bit_exact(oracle_mod):
+    for seed, shape in ((1, (5, 6, 7)), (2, (3, 4, 1)), (3, (1, 1, 8)), (4, (2, 2, 2))):
+        nat = random_nature(shape, 0.35, seed)
+        n, _, _ = random_state(nat, seed)
+        with Box(nat) as box:
+            got = box.bounce_back_stream(n)
+        want = oracle_mod.bounce_back_stream(nat, n)
+        assert np.array_equal(got, want), shape
+
+
+def test_moments_operator_bit_exact(oracle_mod):
+    nat = random_nature((6, 5, 4), 0.3, 21)
+    n, _, jold = random_state(nat, 22)
+    rng = np.random.default_rng(23)
+    f = [1e-4 * rng.standard_normal(nat.shape) for _ in range(3)]
+    with Box(nat) as box:
+        st, rho, j, err = box.moments(n, f, jold)
+    st_o, rho_o, j_o, err_o = oracle_mod.moments(nat, n, f, jold)
+    assert st == 0 and st_o == 0
+    assert np.array_equal(rho, rho_o)
+    for d in range(3):
+        assert np.array_equal(j[d], j_o[d])
+    assert err == err_o
+    # a negative population is reported (equilibration.f90:248)
+    n2 = n.copy()
+    n2[3, 1, 2, 1] = -1e-9
+    with Box(nat) as box:
+        st, *_ = box.moments(n2, f, jold)
+    assert st & 4
+
+
+def oracle_fixed_steps(oracle, nat, tau, f_ext, K, svden=1.0):
+    """Reference loop of equilibration.f90 with the force switched on after step 1."""
+    n, rho = oracle.init_populations(nat, svden)
+    j = [np.zeros(nat.shape) for _ in range(3)]
+    zero = [np.zeros(nat.shape) for _ in range(3)]
+    fon = [np.where(nat == 0, f_ext[d], 0.0) for d in range(3)]
+    for t in range(1, K + 1):
+        f = zero if t == 1 else fon
+        n = oracle.collide(nat, tau, n, rho, j, f)
+        n = oracle.bounce_back_stream(nat, n)
+        st, rho, j, _ = oracle.moments(nat, n, f, j)
+        assert st == 0
+    return n, rho, j
+
+
+@pytest.mark.parametrize("f_ext", [(1e-5, 0.0, 0.0), (0.0, 2e-5, 0.0), (1e-5, -3e-6, 2e-6)])
+def test_fused_fixed_steps_bit_exact(oracle_mod, f_ext):
+    nat = geo.porous_spheres(L=10, radius=2.0, porosity=0.7, seed=5)
+    K = 25
+    with Box(nat, relaxation_time=0.8, f_ext=f_ext) as box:
+        box.flow_init()
+        box.flow_steps(K, force_on=True)
+        n, rho, j = box.flow_get()
+    n_o, rho_o, j_o = oracle_fixed_steps(oracle_mod, nat, 0.8, f_ext, K)
+    assert np.array_equal(n, n_o)
+    assert np.array_equal(rho, rho_o)
+    for d in range(3):
+        assert np.array_equal(j[d], j_o[d])
+
+
+def test_equilibration_c1_bit_exact(oracle_mod):
+    """BASELINE configs[0] flow phase: slit 4x4x34, tau 1, f_ext (1e-5,0,0), target 1e-10."""
+    nat = geo.slit(4, 4, 34)
+    ref = oracle_mod.equilibration(nat, tau=1.0, target_error=1e-10, f_ext=(1e-5, 0, 0),
+                                   max_steps=100000)
+    with Box(nat, relaxation_time=1.0, f_ext=(1e-5, 0, 0), target_error=1e-10) as box:
+        box.flow_init()
+        steps, hist = box.equilibration(max_steps=100000, hist_cap=100000)
+        n, rho, j = box.flow_get()
+    assert steps == ref["steps"]
+    assert np.array_equal(hist, ref["l2err"])
+    assert np.array_equal(n, ref["n"])
+    assert np.array_equal(rho, ref["rho"])
+    for d in range(3):
+        assert np.array_equal(j[d], ref["j"][d])
+
+
+def test_equilibration_porous_bit_exact(oracle_mod):
+    nat = geo.porous_spheres(L=12, radius=2.5, porosity=0.65, seed=9)
+    kw = dict(tau=0.8, target_error=1e-9, f_ext=(2e-5, 1e-5, 0.0))
+    ref = oracle_mod.equilibration(nat, max_steps=50000, **kw)
+    with Box(nat, relaxation_time=0.8, f_ext=kw["f_ext"], target_error=1e-9) as box:
+        box.flow_init()
+        steps, hist = box.equilibration(max_steps=50000, hist_cap=50000)
+        n, rho, j = box.flow_get()
+    assert steps == ref["steps"]
+    assert np.array_equal(hist, ref["l2err"])
+    assert np.array_equal(n, ref["n"])
+    for d in range(3):
+        assert np.array_equal(j[d], ref["j"][d])
+
+
+def test_equilibration_without_force_exits_at_step_4(oracle_mod):
+    nat = geo.slit(1, 1, 12)
+    ref = oracle_mod.equilibration(nat, max_steps=100)
+    with Box(nat) as box:
+        box.flow_init()
+        steps, _ = box.equilibration(max_steps=100)
+    assert steps == ref["steps"] == 4
+
+
+def test_equilibration_step_cap_and_negative_population():
+    nat = geo.slit(4, 4, 20)
+    with Box(nat, relaxation_time=1.0, f_ext=(1e-5, 0, 0)) as box:
+        box.flow_init()
+        with pytest.raises(LbgpuError) as e:
+            box.equilibration(max_steps=50)
+        assert e.value.status & (1 << 5)
+    with Box(nat, relaxation_time=3.0, f_ext=(0.5, 0, 0), target_error=1e-300) as box:
+        box.flow_init()
+        with pytest.raises(LbgpuError) as e:
+            box.equilibration(max_steps=5000)
+        assert e.value.status & 4
+
+
+def test_fp32_deviation_tracks_fp64_on_the_slit():
+    """FP32-deviation storage vs FP64 on the C1 slit after 4000 forced steps:
+    the velocity profile agrees to 1e-4 relative to its maximum."""
+    nat = geo.slit(4, 4, 34)
+    out = {}
+    for prec in (FP64, FP32_DEV):
+        with Box(nat, relaxation_time=1.0, f_ext=(1e-5, 0, 0), precision=prec) as box:
+            box.flow_init()
+            box.flow_steps(4000, force_on=True)
+            _, rho, j = box.flow_get(populations=False)
+        out[prec] = (rho, j)
+    jx64, jx32 = out[FP64][1][0], out[FP32_DEV][1][0]
+    rel = np.max(np.abs(jx32 - jx64)) / np.max(np.abs(jx64))
+    assert rel < 1e-4, rel
+    assert np.max(np.abs(out[FP32_DEV][0] - out[FP64][0])) < 1e-5
