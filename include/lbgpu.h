@@ -158,6 +158,44 @@ int lbgpu_sync(lbgpu_ctx *ctx);
 int lbgpu_host_register(void *ptr, size_t bytes);
 int lbgpu_host_unregister(void *ptr);
 
+/* ---------------------------------------------------------------- tracer moment propagation */
+
+/* The lb.in tracer tags (drop_tracers.f90:88-92, module_moment_propagation.f90:41-71). */
+typedef struct {
+    double Db;             /* tracer_Db, bulk diffusion coefficient (> epsilon) */
+    double ka, kd;         /* tracer_ka, tracer_kd adsorption / desorption rates (>= 0) */
+    double Ds;             /* tracer_Ds, must be 0 as in the reference */
+    double z;              /* tracer_z; charged tracers are refused as in the reference */
+    double f_ext[3];       /* lb.in f_ext, added to the flux of the tracer populations */
+    double elec_slope[3];  /* system elec_slope (0 unless the PNP stage read it) */
+} lbgpu_tracer;
+
+/* update_tracer_population + moment_propagation::init (drop_tracers.f90:63-123,
+ * module_moment_propagation.f90:30-160): builds the tracer populations from the flow moments,
+ * the scattering probabilities (fermi = 1/2), P(t=1) and VACF(t=0) (written to vacf0).
+ * density/jx/jy/jz are node%solventDensity/solventFlux as host arrays, or all NULL to use the
+ * moments of the context's own flow state (after lbgpu_equilibration).  Propagation runs in the
+ * context's precision.  A remaining fraction below epsilon is reported by the first
+ * lbgpu_mp_propagate (module_moment_propagation.f90:249,257), as the reference stops there. */
+int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tracer, const double *density,
+                  const double *jx, const double *jy, const double *jz, double vacf0[3]);
+
+/* moment_propagation::propagate (module_moment_propagation.f90:164-289) for steps it = k+1 ...
+ * k+nsteps, stopping early once converged (it > 2 and |VACF| < min(Db/(2 lx ly lz), 1e-12)).
+ * vacf (optional, capacity 3*nsteps) receives VACF(it) for each step run (vacf.dat rows);
+ * *steps_done the number of steps run, *is_converged the convergence flag. */
+int lbgpu_mp_propagate(lbgpu_ctx *ctx, int nsteps, double *vacf, int *steps_done,
+                       int *is_converged);
+
+/* Current P(3,lx,ly,lz) and adsorbed part (zeros when no adsorption); either may be NULL. */
+int lbgpu_mp_get(lbgpu_ctx *ctx, double *P, double *P_ads);
+
+/* deallocate_propagated_quantity (module_moment_propagation.f90:350-353). */
+int lbgpu_mp_release(lbgpu_ctx *ctx);
+
+/* Time nsteps propagation steps (convergence test disabled) with CUDA events. */
+int lbgpu_time_mp_steps(lbgpu_ctx *ctx, int nsteps, float *ms);
+
 #ifdef __cplusplus
 }
 #endif

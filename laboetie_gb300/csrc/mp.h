@@ -1,0 +1,70 @@
+// mp.h -- tracer moment propagation (drop_tracers.f90, module_moment_propagation.f90).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace lbg {
+
+constexpr int MP_BLOCK = 256;
+
+// Device control block of the propagation loop (module_moment_propagation.f90:164-289).
+struct MpCtl {
+    int it;              // next step (1-based)
+    int parity;          // buffer holding P(now)
+    int done;            // converged or step budget used: launches return at once
+    int converged;
+    int last_it;         // last step completed
+    int max_it;          // last step this call may run
+    int it_base;         // first step of this call (history index 0)
+    unsigned status;
+    unsigned blocks_done;
+    double thr1, thr2;   // convergence thresholds (module_moment_propagation.f90:284)
+    double vacf[3];      // VACF of the last step
+};
+
+struct MpArgs64 {
+    const uint32_t *mask;
+    const double *rho, *jx, *jy, *jz;  // node%solventDensity / solventFlux after the flow phase
+    double *coef;                      // 18*N: coef[(l-1)*N + r] = scattprop of r+c_l towards r
+    double *frac;                      // remaining fraction at r (before the adsorption term)
+    double *us[3];                     // u*(r)
+    double *P[2][3];                   // propagated quantity, now/next by parity
+    double *A[2][3];                   // adsorbed part (adsorption only)
+    double *partial;                   // 3 per block
+    MpCtl *ctl;
+    double *hist;                      // 3 per step
+    long long N;
+    int lx, ly, lz;
+    int ads;
+    double lambda, ka, kd, one_minus_kd, bw;
+    double a0[3], a1[3], lwh[3];       // lwh = (lambda*a0)*0.5 (fermi = 1/2 for a neutral tracer)
+    double fext[3], q, D, E[3];        // drop_tracers.f90:88-100
+};
+
+struct MpArgs32 {
+    const uint32_t *mask;
+    const float *V[3];                 // (j + f_ext)/rho at every fluid node
+    float *P[2][3];
+    float *A[2][3];
+    double *partial;
+    MpCtl *ctl;
+    double *hist;
+    long long N;
+    int lx, ly, lz;
+    int ads;
+    float ka, kd, one_minus_kd;
+    float a1[3], lwh[3];
+};
+
+cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
+cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
+cudaError_t launch_mp_reduce_init(double *partial, unsigned nblocks, MpCtl *ctl, cudaStream_t s);
+cudaError_t launch_mp_v32(const MpArgs64 &a64, float *V0, float *V1, float *V2, cudaStream_t s);
+cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, cudaStream_t s);
+cudaError_t launch_mp_init_f32(const MpArgs32 &a, float bw, unsigned grid, cudaStream_t s);
+
+}  // namespace lbg

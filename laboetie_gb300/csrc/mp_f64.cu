@@ -1,0 +1,214 @@
+// mp_f64.cu -- FP64 strict tracer moment propagation (compiled with -fmad=false).
+//
+// The scattering probabilities of a neutral tracer (module_moment_propagation.f90:341-346,
+// fermi = 1/2) depend only on the converged flow, so they are computed once, in the reference's
+// operation order, into a table coef[(l-1)*N + r] = scattprop of node r+c_l towards r.  A step
+// then gathers P_now from the fluid neighbours through that table, in l order, exactly as the
+// reference's sweep does (module_moment_propagation.f90:207-253): the propagated quantities are
+// bit-identical to the reference; only the VACF node sum runs in a different (fixed) order.
+// Storing the table instead of recomputing it matters on GB300, whose FP64 rate is low.
+#include "common.cuh"
+#include "lbgpu.h"
+#include "mp.h"
+#include "reduce.cuh"
+
+namespace lbg {
+namespace {
+
+__device__ __forceinline__ void nb_offsets(long long node, int lx, int ly, int lz, long long (&X)[3],
+                                           long long (&Y)[3], long long (&Z)[3])
+{
+    const unsigned nd = (unsigned)node;
+    const int x = (int)(nd % (unsigned)lx);
+    const unsigned yz = nd / (unsigned)lx;
+    const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
+    const long long sy = lx, sz = (long long)lx * ly;
+    // [c+1] = coordinate of (x + c), periodic
+    X[0] = wrap_minus(x, lx);       X[1] = x;       X[2] = wrap_plus(x, lx);
+    Y[0] = wrap_minus(y, ly) * sy;  Y[1] = y * sy;  Y[2] = wrap_plus(y, ly) * sy;
+    Z[0] = wrap_minus(z, lz) * sz;  Z[1] = z * sz;  Z[2] = wrap_plus(z, lz) * sz;
+}
+
+// tracer population n_l (drop_tracers.f90:97-100, fluid node):
+// a0*rho + a1*sum(c(:)*(J(:) + f_ext(:) - rho*q*D*E(:)))
+template <int L>
+__device__ __forceinline__ double n_tracer(double rho, double Jx, double Jy, double Jz,
+                                           const MpArgs64 &a)
+{
+    constexpr Vel c = vel(L);
+    constexpr int w = wclass(L);
+    double s = 0.0;
+    if constexpr (c.x != 0) {
+        const double t = Jx + a.fext[0] - rho * a.q * a.D * a.E[0];
+        s = c.x > 0 ? s + t : s - t;
+    }
+    if constexpr (c.y != 0) {
+        const double t = Jy + a.fext[1] - rho * a.q * a.D * a.E[1];
+        s = c.y > 0 ? s + t : s - t;
+    }
+    if constexpr (c.z != 0) {
+        const double t = Jz + a.fext[2] - rho * a.q * a.D * a.E[2];
+        s = c.z > 0 ? s + t : s - t;
+    }
+    if constexpr (L == 0) return a.a0[w] * rho;
+    else return a.a0[w] * rho + a.a1[w] * s;
+}
+
+template <int L>
+__device__ __forceinline__ double scattprop(double n, double rho, const MpArgs64 &a)
+{
+    // n/rho - w + lambda*w*fermi with fermi = 1/2   (module_moment_propagation.f90:345)
+    return n / rho - a.a0[wclass(L)] + a.lwh[wclass(L)];
+}
+
+// module_moment_propagation.f90:30-160 (init) for every fluid node: scattering table, remaining
+// fraction, u*, P(t=1) and this block's share of VACF(0).
+__global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
+{
+    __shared__ double sh[MP_BLOCK / 32];
+    const long long N = a.N;
+    const long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    unsigned bad = 0;
+    if (r < N) {
+        const uint32_t m = a.mask[r];
+        if (m & FLUID_BIT) {
+            long long X[3], Y[3], Z[3];
+            nb_offsets(r, a.lx, a.ly, a.lz, X, Y, Z);
+            const double rho = a.rho[r], Jx = a.jx[r], Jy = a.jy[r], Jz = a.jz[r];
+            double frac = 1.0, ux = 0.0, uy = 0.0, uz = 0.0;
+            double P[3] = {0.0, 0.0, 0.0};
+            static_for<1, Q>([&](auto L) {
+                constexpr int l = decltype(L)::value;
+                constexpr int li = inv(l);
+                constexpr Vel c = vel(l);
+                constexpr Vel ci = vel(li);
+                if ((m >> li) & 1u) {   // neighbour r + c_l is solid
+                    a.coef[(long long)(l - 1) * N + r] = 0.0;
+                    return;
+                }
+                const double sp = scattprop<l>(n_tracer<l>(rho, Jx, Jy, Jz, a), rho, a);
+                frac = frac - sp;
+                if constexpr (c.x != 0) ux = c.x > 0 ? ux + sp : ux - sp;
+                if constexpr (c.y != 0) uy = c.y > 0 ? uy + sp : uy - sp;
+                if constexpr (c.z != 0) uz = c.z > 0 ? uz + sp : uz - sp;
+                const double bs = a.bw * sp;
+                if constexpr (c.x != 0) v[0] = v[0] + bs;
+                if constexpr (c.y != 0) v[1] = v[1] + bs;
+                if constexpr (c.z != 0) v[2] = v[2] + bs;
+                const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
+                const double rhop = a.rho[rp];
+                const double spp =
+                    scattprop<li>(n_tracer<li>(rhop, a.jx[rp], a.jy[rp], a.jz[rp], a), rhop, a);
+                a.coef[(long long)(l - 1) * N + r] = spp;
+                // P(r,1) += exp_min_dphi * scattprop_p * c_inv * boltz_weight, exp_min_dphi = 1
+                if constexpr (ci.x != 0) P[0] = P[0] + (ci.x > 0 ? spp : -spp) * a.bw;
+                if constexpr (ci.y != 0) P[1] = P[1] + (ci.y > 0 ? spp : -spp) * a.bw;
+                if constexpr (ci.z != 0) P[2] = P[2] + (ci.z > 0 ? spp : -spp) * a.bw;
+            });
+            a.frac[r] = frac;
+            a.us[0][r] = ux;
+            a.us[1][r] = uy;
+            a.us[2][r] = uz;
+            for (int d = 0; d < 3; ++d) a.P[0][d][r] = P[d];
+            const double fr = (a.ads && (m & INTERFACIAL_BIT)) ? frac - a.ka : frac;
+            if (fr < 2.220446049250313e-16) bad = LBGPU_ERR_FRACTION;
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        const double b = block_sum_fixed(v[d], sh);
+        if (threadIdx.x == 0) a.partial[3 * blockIdx.x + d] = b;
+    }
+    if (bad) atomicOr(&a.ctl->status, bad);
+}
+
+// module_moment_propagation.f90:164-289, one step.
+__global__ void __launch_bounds__(MP_BLOCK) k_mp_step(const MpArgs64 a)
+{
+    const volatile MpCtl *vc = a.ctl;
+    if (vc->done) return;
+    const int par = vc->parity;
+    const long long N = a.N;
+    const long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (r < N) {
+        const uint32_t m = a.mask[r];
+        if (m & FLUID_BIT) {
+            long long X[3], Y[3], Z[3];
+            nb_offsets(r, a.lx, a.ly, a.lz, X, Y, Z);
+            const double *__restrict__ Px = a.P[par][0];
+            const double *__restrict__ Py = a.P[par][1];
+            const double *__restrict__ Pz = a.P[par][2];
+            double n0 = 0.0, n1 = 0.0, n2 = 0.0;
+            static_for<1, Q>([&](auto L) {
+                constexpr int l = decltype(L)::value;
+                constexpr Vel c = vel(l);
+                if ((m >> inv(l)) & 1u) return;
+                const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
+                const double cf = a.coef[(long long)(l - 1) * N + r];
+                n0 = n0 + Px[rp] * cf;
+                n1 = n1 + Py[rp] * cf;
+                n2 = n2 + Pz[rp] * cf;
+            });
+            const double p0 = Px[r], p1 = Py[r], p2 = Pz[r];
+            v[0] = p0 * a.us[0][r];
+            v[1] = p1 * a.us[1][r];
+            v[2] = p2 * a.us[2][r];
+            const double frac = a.frac[r];
+            if (!a.ads || !(m & INTERFACIAL_BIT)) {
+                n0 = n0 + frac * p0;
+                n1 = n1 + frac * p1;
+                n2 = n2 + frac * p2;
+            } else {
+                const double f2 = frac - a.ka;
+                const double q0 = a.A[par][0][r], q1 = a.A[par][1][r], q2 = a.A[par][2][r];
+                n0 = n0 + f2 * p0 + q0 * a.kd;
+                n1 = n1 + f2 * p1 + q1 * a.kd;
+                n2 = n2 + f2 * p2 + q2 * a.kd;
+                a.A[par ^ 1][0][r] = q0 * a.one_minus_kd + p0 * a.ka;
+                a.A[par ^ 1][1][r] = q1 * a.one_minus_kd + p1 * a.ka;
+                a.A[par ^ 1][2][r] = q2 * a.one_minus_kd + p2 * a.ka;
+            }
+            a.P[par ^ 1][0][r] = n0;
+            a.P[par ^ 1][1][r] = n1;
+            a.P[par ^ 1][2][r] = n2;
+        }
+    }
+    grid_sum3(v, a.partial, &a.ctl->blocks_done,
+              [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });
+}
+
+// Sum of the init partials in block order -> ctl->vacf (VACF at t = 0).
+__global__ void __launch_bounds__(MP_BLOCK) k_mp_reduce(const double *partial, unsigned nb, MpCtl *ctl)
+{
+    __shared__ double sh[MP_BLOCK / 32];
+    double t[3] = {0.0, 0.0, 0.0};
+    for (unsigned i = threadIdx.x; i < nb; i += MP_BLOCK)
+        for (int d = 0; d < 3; ++d) t[d] += partial[3 * i + d];
+    for (int d = 0; d < 3; ++d) {
+        const double s = block_sum_fixed(t[d], sh);
+        if (threadIdx.x == 0) ctl->vacf[d] = s;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
+{
+    k_mp_init<<<grid, MP_BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
+{
+    k_mp_step<<<grid, MP_BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mp_reduce_init(double *partial, unsigned nblocks, MpCtl *ctl, cudaStream_t s)
+{
+    k_mp_reduce<<<1, MP_BLOCK, 0, s>>>(partial, nblocks, ctl);
+    return cudaGetLastError();
+}
+
+}  // namespace lbg

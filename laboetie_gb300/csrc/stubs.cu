@@ -1,6 +1,5 @@
 // stubs.cu -- release hooks of subsystems built in other translation units.
 #include "ctx.h"
 namespace lbg {
-void mp_release(lbgpu_ctx *) {}
 void pnp_release(lbgpu_ctx *) {}
 }  // namespace lbg

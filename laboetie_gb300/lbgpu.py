@@ -251,13 +251,17 @@ class Box:
         return rc, rho, tuple(j), err.value
 
     # -------------------------------------------------------------- device loop
-    def equilibration(self, max_steps=0, hist_cap=0):
-        """equilibration.f90:143-491 on the device.  Returns (steps, l2err history)."""
+    def equilibration(self, max_steps=0, hist_cap=0, check=True):
+        """equilibration.f90:143-491 on the device.  Returns (steps, l2err history), or
+        (steps, history, status) when check is False (the state stays readable after an error)."""
         hist = np.zeros(hist_cap) if hist_cap else None
         steps = C.c_int(0)
         rc = self.L.lbgpu_equilibration(self.ctx, max_steps, _ptr(hist), hist_cap, C.byref(steps))
+        h = hist[: min(steps.value, hist_cap)] if hist is not None else None
+        if not check:
+            return steps.value, h, rc
         self._chk(rc, "equilibration")
-        return steps.value, (hist[: min(steps.value, hist_cap)] if hist is not None else None)
+        return steps.value, h
 
     def flow_steps(self, nsteps, force_on=True):
         self._chk(self.L.lbgpu_flow_steps(self.ctx, nsteps, int(force_on)), "flow_steps")
@@ -270,3 +274,56 @@ class Box:
 
     def sync(self):
         self._chk(self.L.lbgpu_sync(self.ctx), "sync")
+
+
+def _tracer(Db=0.01, ka=0.0, kd=0.0, Ds=0.0, z=0.0, f_ext=(0.0, 0.0, 0.0),
+            elec_slope=(0.0, 0.0, 0.0)):
+    t = Tracer()
+    t.Db, t.ka, t.kd, t.Ds, t.z = Db, ka, kd, Ds, z
+    t.f_ext = (C.c_double * 3)(*f_ext)
+    t.elec_slope = (C.c_double * 3)(*elec_slope)
+    return t
+
+
+def _mp_init(self, moments=None, **tracer):
+    """update_tracer_population + moment_propagation::init.  moments = (rho, (jx, jy, jz)) as
+    host arrays, or None for the box's own flow state.  Returns VACF(0)."""
+    t = _tracer(**tracer)
+    v0 = (C.c_double * 3)()
+    if moments is None:
+        rc = self.L.lbgpu_mp_init(self.ctx, C.byref(t), None, None, None, None, v0)
+    else:
+        rho, j = moments
+        arrs = [_f64(rho, self.shape)] + [_f64(x, self.shape) for x in j]
+        rc = self.L.lbgpu_mp_init(self.ctx, C.byref(t), *(_ptr(x) for x in arrs), v0)
+    self._chk(rc, "mp_init")
+    return np.array(list(v0))
+
+
+def _mp_propagate(self, nsteps):
+    """Returns (vacf (steps,3), converged)."""
+    v = np.zeros((max(nsteps, 1), 3))
+    done, conv = C.c_int(0), C.c_int(0)
+    rc = self.L.lbgpu_mp_propagate(self.ctx, nsteps, _ptr(v), C.byref(done), C.byref(conv))
+    self._chk(rc, "mp_propagate")
+    return v[: done.value], bool(conv.value)
+
+
+def _mp_get(self):
+    P = np.zeros(self.shape + (3,))
+    A = np.zeros(self.shape + (3,))
+    self._chk(self.L.lbgpu_mp_get(self.ctx, _ptr(P), _ptr(A)), "mp_get")
+    return P, A
+
+
+def _time_mp_steps(self, nsteps):
+    ms = C.c_float(0)
+    self._chk(self.L.lbgpu_time_mp_steps(self.ctx, nsteps, C.byref(ms)), "time_mp_steps")
+    return ms.value
+
+
+Box.mp_init = _mp_init
+Box.mp_propagate = _mp_propagate
+Box.mp_get = _mp_get
+Box.time_mp_steps = _time_mp_steps
+Box.mp_release = lambda self: self._chk(self.L.lbgpu_mp_release(self.ctx), "mp_release")

@@ -173,10 +173,11 @@ def moments(nature, n, f, j_old):
 
 def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), svden=1.0,
                   max_steps=0, fixed_steps=0, compensate_f_ext=False, particle_diameter=1,
-                  particle_coords=(0, 0, 0), geometry_label=0, nthreads=1, hist_cap=None):
+                  particle_coords=(0, 0, 0), geometry_label=0, nthreads=1, hist_cap=None,
+                  check=True):
     """Full flow phase of equilibration.f90 from the init_simu.f90 initial state.
 
-    Returns dict(n, rho, j, f, steps, l2err)."""
+    Returns dict(n, rho, j, f, steps, l2err, status); raises on a non-zero status if check."""
     nature = np.ascontiguousarray(nature, dtype=np.int8)
     lx, ly, lz = _dims(nature)
     n, rho = init_populations(nature, svden)
@@ -189,9 +190,10 @@ def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), sv
     steps = C.c_int(0)
     rc = lib().orc_equilibration(C.byref(p), nature, n, rho, jx, jy, jz, fx, fy, fz,
                                  hist.ctypes.data, cap, C.byref(steps))
-    _chk(rc, "equilibration")
+    if check:
+        _chk(rc, "equilibration")
     return dict(n=n, rho=rho, j=(jx, jy, jz), f=(fx, fy, fz), steps=steps.value,
-                l2err=hist[: min(steps.value, cap)])
+                l2err=hist[: min(steps.value, cap)], status=rc)
 
 
 def update_tracer_population(nature, rho, j, f_ext, tracer_z=0.0, tracer_D=0.0,

@@ -157,8 +157,9 @@ def test_equilibration_c1_bit_exact(oracle_mod):
         assert np.array_equal(j[d], ref["j"][d])
 
 
-def test_equilibration_porous_bit_exact(oracle_mod):
-    nat = geo.porous_spheres(L=12, radius=2.5, porosity=0.65, seed=9)
+def test_equilibration_cc_bit_exact(oracle_mod):
+    """Touching spheres (geometryLabel 3) 12^3, tau 0.8, oblique force, target 1e-9."""
+    nat = geo.cc(12, 12, 12)
     kw = dict(tau=0.8, target_error=1e-9, f_ext=(2e-5, 1e-5, 0.0))
     ref = oracle_mod.equilibration(nat, max_steps=50000, **kw)
     with Box(nat, relaxation_time=0.8, f_ext=kw["f_ext"], target_error=1e-9) as box:
@@ -168,6 +169,25 @@ def test_equilibration_porous_bit_exact(oracle_mod):
     assert steps == ref["steps"]
     assert np.array_equal(hist, ref["l2err"])
     assert np.array_equal(n, ref["n"])
+    for d in range(3):
+        assert np.array_equal(j[d], ref["j"][d])
+
+
+def test_equilibration_step_cap_state_bit_exact(oracle_mod):
+    """A random porous medium with isolated fluid pockets never meets the target (the reference
+    would loop for ever); at a step cap both stop at the same step in the same state."""
+    nat = geo.porous_spheres(L=12, radius=2.5, porosity=0.65, seed=9)
+    kw = dict(tau=0.8, target_error=1e-9, f_ext=(2e-5, 1e-5, 0.0))
+    ref = oracle_mod.equilibration(nat, max_steps=1500, check=False, **kw)
+    assert ref["status"] == 2 and ref["steps"] == 1500
+    with Box(nat, relaxation_time=0.8, f_ext=kw["f_ext"], target_error=1e-9) as box:
+        box.flow_init()
+        steps, hist, rc = box.equilibration(max_steps=1500, hist_cap=1500, check=False)
+        n, rho, j = box.flow_get()
+    assert rc & (1 << 5) and steps == 1500
+    assert np.array_equal(hist, ref["l2err"])
+    assert np.array_equal(n, ref["n"])
+    assert np.array_equal(rho, ref["rho"])
     for d in range(3):
         assert np.array_equal(j[d], ref["j"][d])
 
