@@ -60,6 +60,10 @@ struct lbgpu_ctx {
     int prev_force_moment = 0;   // f_ext in the moments of the state held in buffer 1-cur
     int force_last_collide = 0;  // f_ext in the collision that produced buffer cur
     bool moments_valid = false;  // d_rho / d_j hold the moments of the state
+    // FP32 deviations: in-place AA streaming (one buffer) unless LBGPU_FP32_STREAMING=ab
+    bool aa = true;
+    int aa_phase = 0;            // parity of the next AA launch (1: buffer holds swapped f*)
+    int aa_minb[2] = {4, 3};     // AA kernel variants for even / odd launches
 
     // cached CUDA graphs of the step loop
     cudaGraphExec_t graph_ref = nullptr;

@@ -47,6 +47,7 @@ struct FlowArgs32 {
     float F[3];
     double rho0d;
     double w64[3];
+    int minb_even, minb_odd;     // AA kernel variants (resident blocks per SM)
 };
 
 // FP64 strict ---------------------------------------------------------------------------
@@ -70,6 +71,8 @@ cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_
 cudaError_t launch_init_f32(const FlowArgs32 &a, cudaStream_t s);
 cudaError_t launch_finalize_f32(const FlowArgs32 &a, bool pull, cudaStream_t s);
 cudaError_t launch_collide_f32(const FlowArgs32 &a, cudaStream_t s);
+cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s);
+cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s);
 cudaError_t launch_to_dev32(const FlowArgs32 &a, const double *n, float *out, cudaStream_t s);
 
 // geometry ------------------------------------------------------------------------------

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -67,7 +69,20 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     if (p.precision == LBGPU_FP64) {
         for (int b = 0; b < 2; ++b) LBG_CK(ctx, dalloc(&ctx->d_f[b], (size_t)Q * N));
     } else {
-        for (int b = 0; b < 2; ++b) LBG_CK(ctx, dalloc(&ctx->d_g[b], (size_t)Q * N));
+        const char *mode = std::getenv("LBGPU_FP32_STREAMING");
+        ctx->aa = !(mode && std::string(mode) == "ab");
+        if (ctx->aa && (unsigned long long)Q * N >= (1ULL << 32))
+            return ctx_fail(ctx, LBGPU_ERR_INVALID,
+                            "FP32 in-place streaming addresses 19*N populations with 32-bit "
+                            "indices: box too large (use LBGPU_FP32_STREAMING=ab)");
+        if (const char *e = std::getenv("LBGPU_AA_MINB")) {  // "<even>,<odd>", e.g. "4,3"
+            int ev = 0, od = 0;
+            if (std::sscanf(e, "%d,%d", &ev, &od) == 2) {
+                ctx->aa_minb[0] = ev;
+                ctx->aa_minb[1] = od;
+            }
+        }
+        for (int b = 0; b < (ctx->aa ? 1 : 2); ++b) LBG_CK(ctx, dalloc(&ctx->d_g[b], (size_t)Q * N));
     }
     for (int d = 0; d < 3; ++d) LBG_CK(ctx, dalloc(&ctx->d_j[d], N));
     LBG_CK(ctx, dalloc(&ctx->d_rho, N));

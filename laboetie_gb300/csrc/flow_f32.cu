@@ -134,6 +134,132 @@ __global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
     for (int l = 0; l < Q; ++l) __stcs(dst + (size_t)l * N + node, g[l]);
 }
 
+// In-place AA-pattern step (one population buffer).  Even launches read the node's own 19
+// slots and write the post-collision populations back into the opposite slots; odd launches
+// read the 19 slots that stream into the node and write the post-collision populations into
+// the slots they stream to.  In both cases a thread writes exactly the slots it read (so the
+// update is race-free and every store lands on a sector that is already in L2), and after an
+// odd launch the buffer holds the streamed populations in natural order again.
+// Halfway bounce-back (equilibration.f90:204-243): a population whose source (or destination)
+// across link l is of the other nature is read from (written to) the node itself.
+template <bool ODD, int FMASK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
+{
+    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
+    if (node >= (unsigned)a.N) return;
+    const uint32_t m = __ldg(a.mask + node);
+    if (!(m & FLUID_BIT)) return;
+    float *g = a.g0;
+    const unsigned N = (unsigned)a.N;  // 19*N < 2^32 is checked when the context is created
+    float f[Q];
+    unsigned off[Q];  // element index of the slot read for direction l (odd launches)
+    if constexpr (ODD) {
+        const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
+        static_for<0, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            if constexpr (l == 0) {
+                off[0] = node;
+            } else {
+                const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);  // node - c_l
+                off[l] = ((m >> l) & 1u) ? (unsigned)l * N + node : (unsigned)inv(l) * N + s;
+            }
+        });
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = g[off[l]];
+    } else {
+        const float *p = g + node;
+#pragma unroll
+        for (int l = 0; l < Q; ++l, p += N) f[l] = *p;
+    }
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        drho += f[l];
+        if constexpr (c.x > 0) jx += f[l];
+        if constexpr (c.x < 0) jx -= f[l];
+        if constexpr (c.y > 0) jy += f[l];
+        if constexpr (c.y < 0) jy -= f[l];
+        if constexpr (c.z > 0) jz += f[l];
+        if constexpr (c.z < 0) jz -= f[l];
+    });
+    if (FMASK && a.force_moment) {
+        jx += 0.5f * a.F[0];
+        jy += 0.5f * a.F[1];
+        jz += 0.5f * a.F[2];
+    }
+    collide_dev<FMASK>(f, drho, jx, jy, jz, a, a.force_collide != 0);
+    if constexpr (ODD) {
+        // the population leaving along l goes to the slot the opposite direction was read from
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
+    } else {
+        float *p = g + node;
+#pragma unroll
+        for (int l = 0; l < Q; ++l, p += N) *p = f[inv(l)];
+    }
+}
+
+// Moments (FP64) of an AA buffer: natural order after an odd launch (SWAPPED = false), or
+// post-collision values in opposite slots after an even launch (SWAPPED = true, gathered as
+// the next odd launch would).
+template <bool SWAPPED>
+__global__ void __launch_bounds__(BLOCK) k_aa_finalize32(const FlowArgs32 a)
+{
+    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
+    if (node >= (unsigned)a.N) return;
+    const uint32_t m = a.mask[node];
+    const size_t N = (size_t)a.N;
+    if (!(m & FLUID_BIT)) {
+        a.rho[node] = 0.0;
+        a.jx[node] = 0.0;
+        a.jy[node] = 0.0;
+        a.jz[node] = 0.0;
+        if (a.nout)
+            for (int l = 0; l < Q; ++l) a.nout[(size_t)l * N + node] = 0.0;
+        return;
+    }
+    const float *g = a.g0;
+    float f[Q];
+    if constexpr (SWAPPED) {
+        const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
+        static_for<0, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            if constexpr (l == 0) {
+                f[0] = g[node];
+            } else {
+                const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);
+                f[l] = ((m >> l) & 1u) ? g[(size_t)l * N + node] : g[(size_t)inv(l) * N + s];
+            }
+        });
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * N + node];
+    }
+    double drho = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        const double v = (double)f[l];
+        drho += v;
+        jx += c.x * v;
+        jy += c.y * v;
+        jz += c.z * v;
+        if (a.nout) a.nout[(size_t)l * N + node] = v + a.w64[wclass(l)] * a.rho0d;
+    });
+    if (a.force_moment) {
+        jx += 0.5 * (double)a.F[0];
+        jy += 0.5 * (double)a.F[1];
+        jz += 0.5 * (double)a.F[2];
+    }
+    a.rho[node] = a.rho0d + drho;
+    a.jx[node] = jx;
+    a.jy[node] = jy;
+    a.jz[node] = jz;
+}
+
 // Zero deviations: the rest state rho = rho0, j = 0 (init_simu.f90:283-291 on fluid nodes).
 __global__ void __launch_bounds__(BLOCK) k_init32(const FlowArgs32 a)
 {
@@ -141,7 +267,7 @@ __global__ void __launch_bounds__(BLOCK) k_init32(const FlowArgs32 a)
     const size_t total = (size_t)Q * (size_t)a.N;
     if (i < total) {
         a.g0[i] = 0.0f;
-        a.g1[i] = 0.0f;
+        if (a.g1) a.g1[i] = 0.0f;
     }
 }
 
@@ -256,6 +382,46 @@ cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_
     case 4: k_step32<4><<<grid, BLOCK, 0, s>>>(a); break;
     default: k_step32<7><<<grid, BLOCK, 0, s>>>(a); break;
     }
+    return cudaGetLastError();
+}
+
+// minb: resident blocks per SM the kernel is compiled for (2, 3 or 4 -> up to 128, 85 or 64
+// registers per thread); picked per device by the tuner in flow_f32_api.cu.
+template <int FM, int MINB>
+static void aa_launch(const FlowArgs32 &a, bool odd, unsigned grid, cudaStream_t s)
+{
+    if (odd) k_aa32<true, FM, MINB><<<grid, BLOCK, 0, s>>>(a);
+    else k_aa32<false, FM, MINB><<<grid, BLOCK, 0, s>>>(a);
+}
+
+template <int FM>
+static void aa_launch_minb(const FlowArgs32 &a, bool odd, int minb, unsigned grid, cudaStream_t s)
+{
+    if (minb <= 2) aa_launch<FM, 2>(a, odd, grid, s);
+    else if (minb == 3) aa_launch<FM, 3>(a, odd, grid, s);
+    else aa_launch<FM, 4>(a, odd, grid, s);
+}
+
+cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    const int fm = (a.F[0] != 0.0f ? 1 : 0) | (a.F[1] != 0.0f ? 2 : 0) | (a.F[2] != 0.0f ? 4 : 0);
+    const int minb = odd ? a.minb_odd : a.minb_even;
+    switch (fm) {
+    case 0: aa_launch_minb<0>(a, odd, minb, grid, s); break;
+    case 1: aa_launch_minb<1>(a, odd, minb, grid, s); break;
+    case 2: aa_launch_minb<2>(a, odd, minb, grid, s); break;
+    case 4: aa_launch_minb<4>(a, odd, minb, grid, s); break;
+    default: aa_launch_minb<7>(a, odd, minb, grid, s); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    if (swapped) k_aa_finalize32<true><<<grid, BLOCK, 0, s>>>(a);
+    else k_aa_finalize32<false><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
 

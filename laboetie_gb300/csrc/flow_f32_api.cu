@@ -38,6 +38,8 @@ static void fill_args32(lbgpu_ctx *ctx, FlowArgs32 &a)
     a.rho0 = (float)ctx->p.rho0;
     a.rho0d = ctx->p.rho0;
     for (int d = 0; d < 3; ++d) a.F[d] = (float)ctx->p.f_ext[d];
+    a.minb_even = ctx->aa_minb[0];
+    a.minb_odd = ctx->aa_minb[1];
 }
 
 int f32_flow_init(lbgpu_ctx *ctx)
@@ -45,6 +47,7 @@ int f32_flow_init(lbgpu_ctx *ctx)
     FlowArgs32 a;
     fill_args32(ctx, a);
     LBG_CK(ctx, launch_init_f32(a, ctx->stream));
+    ctx->aa_phase = 0;  // AA: the zero deviations are the natural-order state n_0
     ctx->cur = 0;
     ctx->prev_kind = PREV_RAW;
     ctx->prev_force_moment = 0;
@@ -63,8 +66,17 @@ int f32_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const d
     double *tmp = nullptr;
     LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
     LBG_CK(ctx, cudaMemcpyAsync(tmp, n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
-    LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->d_g[1], s));
+    LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->aa ? ctx->d_g[0] : ctx->d_g[1], s));
     LBG_CK(ctx, cudaFreeAsync(tmp, s));
+    if (ctx->aa) {
+        // AA: the populations are the natural-order state; the next launch collides them with
+        // the current phase's force.  density and j are implied by n.
+        ctx->aa_phase = 0;
+        ctx->prev_kind = PREV_RAW;
+        ctx->prev_force_moment = ctx->force_last_collide;
+        LBG_CK(ctx, cudaStreamSynchronize(s));
+        return LBGPU_OK;
+    }
     LBG_CK(ctx, cudaMemcpyAsync(ctx->d_rho, density, sizeof(double) * N, cudaMemcpyHostToDevice, s));
     const double *j[3] = {jx, jy, jz};
     for (int q = 0; q < 3; ++q)
@@ -94,7 +106,8 @@ int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double 
         LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
         a.nout = tmp;
     }
-    LBG_CK(ctx, launch_finalize_f32(a, ctx->prev_kind == PREV_POST, s));
+    if (ctx->aa) LBG_CK(ctx, launch_aa_finalize_f32(a, ctx->aa_phase == 1, s));
+    else LBG_CK(ctx, launch_finalize_f32(a, ctx->prev_kind == PREV_POST, s));
     if (n) LBG_CK(ctx, cudaMemcpyAsync(n, tmp, sizeof(double) * Q * N, cudaMemcpyDeviceToHost, s));
     if (density) LBG_CK(ctx, cudaMemcpyAsync(density, ctx->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
     double *j[3] = {jx, jy, jz};
@@ -105,10 +118,69 @@ int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double 
     return LBGPU_OK;
 }
 
-int f32_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
+// AA launches.  A launch computes the moments of the state it reads (force of the collision
+// that produced it: prev_force_moment) and performs the next collision (force_last_collide);
+// then the force of the following collision becomes force_on.  This reproduces the A/B
+// bookkeeping step for step, so both layouts give identical results.
+static int aa_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
 {
     cudaStream_t s = ctx->stream;
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    auto one = [&]() -> int {
+        a.force_moment = ctx->prev_force_moment;
+        a.force_collide = ctx->force_last_collide;
+        LBG_CK(ctx, launch_aa_step_f32(a, ctx->aa_phase == 1, s));
+        ctx->aa_phase ^= 1;
+        ctx->prev_force_moment = ctx->force_last_collide;
+        ctx->force_last_collide = force_on;
+        ctx->prev_kind = PREV_POST;
+        return LBGPU_OK;
+    };
+    int rc;
+    if (!ms) {
+        for (int t = 0; t < nsteps; ++t)
+            if ((rc = one())) return rc;
+        return LBGPU_OK;
+    }
+    // settle the force bookkeeping and the parity outside the timed region
+    int guard = 0;
+    while ((ctx->prev_force_moment != force_on || ctx->force_last_collide != force_on ||
+            ctx->aa_phase != 0) && guard++ < 4)
+        if ((rc = one())) return rc;
+    if (!ctx->graph_fixed[force_on] || ctx->graph_fixed_parity[force_on] != 0) {
+        if (ctx->graph_fixed[force_on]) cudaGraphExecDestroy(ctx->graph_fixed[force_on]);
+        cudaGraph_t g;
+        LBG_CK(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        a.force_moment = force_on;
+        a.force_collide = force_on;
+        for (int k = 0; k < 2; ++k) {
+            cudaError_t e = launch_aa_step_f32(a, k == 1, s);
+            if (e != cudaSuccess) {
+                cudaStreamEndCapture(s, &g);
+                return ctx_cuda(ctx, e, "capture");
+            }
+        }
+        LBG_CK(ctx, cudaStreamEndCapture(s, &g));
+        LBG_CK(ctx, cudaGraphInstantiate(&ctx->graph_fixed[force_on], g, 0));
+        cudaGraphDestroy(g);
+        ctx->graph_fixed_parity[force_on] = 0;
+    }
+    LBG_CK(ctx, cudaEventRecord(ctx->ev0, s));
+    for (int k = 0; k < nsteps / 2; ++k) LBG_CK(ctx, cudaGraphLaunch(ctx->graph_fixed[force_on], s));
+    if (nsteps & 1)
+        if ((rc = one())) return rc;
+    LBG_CK(ctx, cudaEventRecord(ctx->ev1, s));
+    LBG_CK(ctx, cudaEventSynchronize(ctx->ev1));
+    LBG_CK(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    return LBGPU_OK;
+}
+
+int f32_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
+{
     force_on = force_on ? 1 : 0;
+    if (ctx->aa) return aa_steps(ctx, nsteps, force_on, ms);
+    cudaStream_t s = ctx->stream;
     FlowArgs32 a;
     fill_args32(ctx, a);
     auto one = [&]() -> int {
