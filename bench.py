@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import re
 import statistics
@@ -39,7 +40,7 @@ FEXT = (1e-6, 0.0, 0.0)
 BYTES_F32 = 38 * 4   # 19 reads + 19 writes of one FP32 deviation per fluid node
 BYTES_F64 = 38 * 8
 WORKLOAD = "D3Q19 porous 192^3 spheres r=8 porosity 0.60 seed 20261203, tau 0.8, f_ext (1e-6,0,0)"
-METRIC = "D3Q19 MLUPS (fluid-node updates/us), FP32-deviation populations"
+METRIC = "D3Q19 MLUPS (fluid-node updates per microsecond)"
 
 
 def args_():
@@ -50,6 +51,7 @@ def args_():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=L_BOX)
     ap.add_argument("--fp64-steps", type=int, default=0, help="default: min(steps, 200)")
+    ap.add_argument("--mp-steps", type=int, default=0, help="default: min(steps, 400)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -184,7 +186,7 @@ def run_reference(a):
     oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=1, nthreads=threads)
     mlups, steps, dt, _ = cpu_oracle_mlups(nature, a.cpu_seconds, threads)
     line = {
-        "impl": "reference", "metric": METRIC.replace("FP32-deviation", "FP64"), "value": round(mlups, 4),
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 4),
         "unit": "MLUPS", "n_gpus": a.gpus, "steps": steps, "warmup": 1,
         "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded porous medium)",
@@ -226,6 +228,12 @@ def main():
     box.sync()
     ms32 = max_over_ranks(dist, ms32)
     barrier(dist)
+    # tracer moment propagation on the FP32 flow field (BASELINE: Db 0.01, beta dF = -2)
+    KMP = a.mp_steps or min(K, 400)
+    box.mp_init(f_ext=FEXT, Db=0.01, ka=0.01 * math.exp(2.0), kd=0.01)
+    box.time_mp_steps(W)
+    ms_mp32 = max_over_ranks(dist, box.time_mp_steps(KMP))
+    box.mp_release()
 
     # ---------------------------------------------------------- FP64 strict
     box64 = Box(nature, relaxation_time=TAU, f_ext=FEXT, precision=FP64, device=local)
@@ -237,6 +245,11 @@ def main():
     box64.sync()
     ms64 = max_over_ranks(dist, ms64)
     barrier(dist)
+    box64.mp_init(f_ext=FEXT, Db=0.01, ka=0.01 * math.exp(2.0), kd=0.01)
+    box64.time_mp_steps(W)
+    KMP64 = max(KMP // 4, 20)
+    ms_mp64 = max_over_ranks(dist, box64.time_mp_steps(KMP64))
+    box64.mp_release()
     # initial state for e2e: the FP64 populations after the warm-up (realistic, non-trivial)
     n0, rho0, j0 = box64.flow_get()
     box64.close()
@@ -303,6 +316,18 @@ def main():
                               "unit": "GB/s", "frac": round(achieved64 / hbm, 4),
                               "algorithmic_bytes_per_fluid_node": BYTES_F64},
                  "speedup_fp32_over_fp64": round(value / mlups64, 2)},
+        "moment_propagation": {
+            "fp32": {"value": round(world * nfluid * KMP / (ms_mp32 * 1e-3) / 1e6, 2),
+                     "unit": "M fluid-node steps/s", "steps": KMP,
+                     "ms_per_step": round(ms_mp32 / KMP, 5),
+                     "roofline": {"bound": "hbm", "achieved": round(40 * nfluid / (ms_mp32 / KMP * 1e-3) / 1e9, 1),
+                                  "peak": hbm, "unit": "GB/s",
+                                  "frac": round(40 * nfluid / (ms_mp32 / KMP * 1e-3) / 1e9 / hbm, 4),
+                                  "algorithmic_bytes_per_fluid_node": 40}},
+            "fp64": {"value": round(world * nfluid * KMP64 / (ms_mp64 * 1e-3) / 1e6, 2),
+                     "unit": "M fluid-node steps/s", "steps": KMP64,
+                     "ms_per_step": round(ms_mp64 / KMP64, 4)},
+            "tracer": "Db 0.01, K = e^2 (kd 0.01), adsorption on interfacial fluid nodes"},
         "e2e": {"value": round(world * nfluid * K / t_e2e / 1e6, 2), "unit": "MLUPS",
                 "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
                 "what": "lbgpu_flow_set (n, density, j from pinned host) + K fused steps + "

@@ -50,6 +50,13 @@ __host__ __device__ constexpr int inv(int l)
                                   : l == 15 ? 18 : l == 18 ? 15 : l == 16 ? 17 : 16));
 }
 
+// The 9 pairs (l, inv l) of opposite velocities; l is the first of pair p.
+__host__ __device__ constexpr int pair_l(int p)
+{
+    return p == 0 ? 1 : p == 1 ? 3 : p == 2 ? 5 : p == 3 ? 7 : p == 4 ? 8 : p == 5 ? 11 : p == 6 ? 12
+           : p == 7 ? 15 : 16;
+}
+
 // weight class: 0 rest (1/3), 1 axis (1/18), 2 face diagonal (1/36)
 __host__ __device__ constexpr int wclass(int l) { return l == 0 ? 0 : (l < 7 ? 1 : 2); }
 

@@ -63,7 +63,7 @@ struct lbgpu_ctx {
     // FP32 deviations: in-place AA streaming (one buffer) unless LBGPU_FP32_STREAMING=ab
     bool aa = true;
     int aa_phase = 0;            // parity of the next AA launch (1: buffer holds swapped f*)
-    int aa_minb[2] = {4, 3};     // AA kernel variants for even / odd launches
+    int aa_minb[2] = {4, 4};     // AA kernel variants for even / odd launches
 
     // cached CUDA graphs of the step loop
     cudaGraphExec_t graph_ref = nullptr;

@@ -45,6 +45,9 @@ struct FlowArgs32 {
     float w[3], a1[3], a2[3], two_a2[3];
     float c1, c2, c3, rho0;
     float F[3];
+    // collision constants of the pair-symmetric form (flow_f32.cu)
+    float c2w[3], c2a1[3], c2a2[3], c2a2cs2[3], c3a1[3];
+    float kF[9], kT[9];
     double rho0d;
     double w64[3];
     int minb_even, minb_odd;     // AA kernel variants (resident blocks per SM)

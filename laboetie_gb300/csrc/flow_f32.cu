@@ -67,6 +67,13 @@ __device__ __forceinline__ void pull19f(float (&g)[Q], const float *__restrict__
     });
 }
 
+// BGK + Guo forcing on deviations, split into the parts even and odd in c for each pair of
+// opposite velocities (c.j, c.u and c.F change sign, everything else does not):
+//   dneq = E +- O,  E = w drho + a2 ((c.j)(c.u) - cs^2 j.u),  O = a1 c.j
+//   T    = TE +- TO, TE = 2 a2 (c.u)(c.F) - a1 u.F,           TO = a1 c.F
+//   d*_l = c1 d_l + (c2 E + c3 TE) +- (c2 O + c3 TO)
+// which halves the arithmetic of a direction-by-direction evaluation.  The per-pair force
+// constants kF = c3 a1 c.F and kT = c3 2 a2 c.F are precomputed on the host.
 template <int FMASK>
 __device__ __forceinline__ void collide_dev(float (&g)[Q], const float drho, const float jx,
                                             const float jy, const float jz, const FlowArgs32 &a,
@@ -76,25 +83,35 @@ __device__ __forceinline__ void collide_dev(float (&g)[Q], const float drho, con
     const float ir = 1.0f / rho;
     const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
     const float ju = jx * ux + jy * uy + jz * uz;
-    const float cs2 = 1.0f / 3.0f;
-    float uF = 0.0f;
-    if (FMASK && force) uF = ux * a.F[0] + uy * a.F[1] + uz * a.F[2];
-    static_for<0, Q>([&](auto L) {
-        constexpr int l = decltype(L)::value;
+    float base[3];
+#pragma unroll
+    for (int w = 0; w < 3; ++w) base[w] = a.c2w[w] * drho - a.c2a2cs2[w] * ju;
+    if constexpr (FMASK != 0) {
+        if (force) {
+            const float uF = ux * a.F[0] + uy * a.F[1] + uz * a.F[2];
+#pragma unroll
+            for (int w = 0; w < 3; ++w) base[w] -= a.c3a1[w] * uF;
+        }
+    }
+    g[0] = a.c1 * g[0] + base[0];
+    static_for<0, 9>([&](auto P) {
+        constexpr int p = decltype(P)::value;
+        constexpr int l = pair_l(p);
+        constexpr int li = inv(l);
         constexpr Vel c = vel(l);
         constexpr int w = wclass(l);
         const float cj = dotf<c.x, c.y, c.z>(jx, jy, jz);
         const float cu = dotf<c.x, c.y, c.z>(ux, uy, uz);
-        const float neq = a.w[w] * drho + a.a1[w] * cj + a.a2[w] * (cj * cu - cs2 * ju);
-        float r = a.c1 * g[l] + a.c2 * neq;
+        float A = base[w] + a.c2a2[w] * (cj * cu);
+        float B = a.c2a1[w] * cj;
         if constexpr (FMASK != 0) {
             if (force) {
-                const float cF = dotf<(FMASK & 1) ? c.x : 0, (FMASK & 2) ? c.y : 0, (FMASK & 4) ? c.z : 0>(
-                    a.F[0], a.F[1], a.F[2]);
-                r += a.c3 * (a.a1[w] * (cF - uF) + a.two_a2[w] * cu * cF);
+                A += a.kT[p] * cu;
+                B += a.kF[p];
             }
         }
-        g[l] = r;
+        g[l] = a.c1 * g[l] + (A + B);
+        g[li] = a.c1 * g[li] + (A - B);
     });
 }
 
@@ -149,28 +166,34 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
     if (node >= (unsigned)a.N) return;
     const uint32_t m = __ldg(a.mask + node);
     if (!(m & FLUID_BIT)) return;
-    float *g = a.g0;
+    // Each thread writes only the slots it has read, and every value it writes depends on all
+    // of them: no store can overtake a load, so the two views of the buffer may be restricted.
+    const float *__restrict__ gin = a.g0;
+    float *__restrict__ gout = a.g0;
     const unsigned N = (unsigned)a.N;  // 19*N < 2^32 is checked when the context is created
     float f[Q];
-    unsigned off[Q];  // element index of the slot read for direction l (odd launches)
+    // odd launches: element index of the slot read for direction l, parked in shared memory
+    // ([l][thread], conflict-free) so that it does not occupy registers across the collision
+    __shared__ unsigned soff[ODD ? Q : 1][BLOCK];
     if constexpr (ODD) {
         const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
         static_for<0, Q>([&](auto L) {
             constexpr int l = decltype(L)::value;
             constexpr Vel c = vel(l);
+            unsigned o;
             if constexpr (l == 0) {
-                off[0] = node;
+                o = node;
             } else {
                 const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);  // node - c_l
-                off[l] = ((m >> l) & 1u) ? (unsigned)l * N + node : (unsigned)inv(l) * N + s;
+                o = ((m >> l) & 1u) ? (unsigned)l * N + node : (unsigned)inv(l) * N + s;
             }
+            soff[l][threadIdx.x] = o;
+            f[l] = __ldg(gin + o);
         });
-#pragma unroll
-        for (int l = 0; l < Q; ++l) f[l] = g[off[l]];
     } else {
-        const float *p = g + node;
+        const float *p = gin + node;
 #pragma unroll
-        for (int l = 0; l < Q; ++l, p += N) f[l] = *p;
+        for (int l = 0; l < Q; ++l, p += N) f[l] = __ldg(p);
     }
     float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
     static_for<0, Q>([&](auto L) {
@@ -193,9 +216,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
     if constexpr (ODD) {
         // the population leaving along l goes to the slot the opposite direction was read from
 #pragma unroll
-        for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
+        for (int l = 0; l < Q; ++l) gout[soff[inv(l)][threadIdx.x]] = f[l];
     } else {
-        float *p = g + node;
+        float *p = gout + node;
 #pragma unroll
         for (int l = 0; l < Q; ++l, p += N) *p = f[inv(l)];
     }
@@ -374,14 +397,9 @@ cudaError_t launch_collide_f32(const FlowArgs32 &a, cudaStream_t s)
 cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_t s)
 {
     if (!grid) grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
-    int fm = (a.F[0] != 0.0f ? 1 : 0) | (a.F[1] != 0.0f ? 2 : 0) | (a.F[2] != 0.0f ? 4 : 0);
-    switch (fm) {
-    case 0: k_step32<0><<<grid, BLOCK, 0, s>>>(a); break;
-    case 1: k_step32<1><<<grid, BLOCK, 0, s>>>(a); break;
-    case 2: k_step32<2><<<grid, BLOCK, 0, s>>>(a); break;
-    case 4: k_step32<4><<<grid, BLOCK, 0, s>>>(a); break;
-    default: k_step32<7><<<grid, BLOCK, 0, s>>>(a); break;
-    }
+    const bool fm = a.F[0] != 0.0f || a.F[1] != 0.0f || a.F[2] != 0.0f;
+    if (fm) k_step32<7><<<grid, BLOCK, 0, s>>>(a);
+    else k_step32<0><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -405,15 +423,9 @@ static void aa_launch_minb(const FlowArgs32 &a, bool odd, int minb, unsigned gri
 cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s)
 {
     const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
-    const int fm = (a.F[0] != 0.0f ? 1 : 0) | (a.F[1] != 0.0f ? 2 : 0) | (a.F[2] != 0.0f ? 4 : 0);
-    const int minb = odd ? a.minb_odd : a.minb_even;
-    switch (fm) {
-    case 0: aa_launch_minb<0>(a, odd, minb, grid, s); break;
-    case 1: aa_launch_minb<1>(a, odd, minb, grid, s); break;
-    case 2: aa_launch_minb<2>(a, odd, minb, grid, s); break;
-    case 4: aa_launch_minb<4>(a, odd, minb, grid, s); break;
-    default: aa_launch_minb<7>(a, odd, minb, grid, s); break;
-    }
+    // one instantiation: with the force switched off (force_collide = 0) the force terms are
+    // skipped at run time
+    aa_launch_minb<7>(a, odd, odd ? a.minb_odd : a.minb_even, grid, s);
     return cudaGetLastError();
 }
 

@@ -40,6 +40,21 @@ static void fill_args32(lbgpu_ctx *ctx, FlowArgs32 &a)
     for (int d = 0; d < 3; ++d) a.F[d] = (float)ctx->p.f_ext[d];
     a.minb_even = ctx->aa_minb[0];
     a.minb_odd = ctx->aa_minb[1];
+    const double c2 = K.c2, c3 = K.c3, cs2 = 1.0 / 3.0;
+    for (int w = 0; w < 3; ++w) {
+        a.c2w[w] = (float)(c2 * K.a0[w]);
+        a.c2a1[w] = (float)(c2 * K.a1[w]);
+        a.c2a2[w] = (float)(c2 * K.a2[w]);
+        a.c2a2cs2[w] = (float)(c2 * K.a2[w] * cs2);
+        a.c3a1[w] = (float)(c3 * K.a1[w]);
+    }
+    for (int p = 0; p < 9; ++p) {
+        const int l = pair_l(p);
+        const Vel c = vel(l);
+        const double cF = c.x * ctx->p.f_ext[0] + c.y * ctx->p.f_ext[1] + c.z * ctx->p.f_ext[2];
+        a.kF[p] = (float)(c3 * K.a1[wclass(l)] * cF);
+        a.kT[p] = (float)(c3 * K.two_a2[wclass(l)] * cF);
+    }
 }
 
 int f32_flow_init(lbgpu_ctx *ctx)

@@ -62,6 +62,12 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
             float frac = 1.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
             float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
             float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+            float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f;
+            if constexpr (!INIT) {
+                p0 = Px[r];
+                p1 = Py[r];
+                p2 = Pz[r];
+            }
             static_for<1, Q>([&](auto L) {
                 constexpr int l = decltype(L)::value;
                 constexpr Vel c = vel(l);
@@ -84,9 +90,12 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                     n1 -= c.y * spp;
                     n2 -= c.z * spp;
                 } else {
-                    n0 += Px[rp] * spp;
-                    n1 += Py[rp] * spp;
-                    n2 += Pz[rp] * spp;
+                    // flux form: what arrives from r + c_l minus what leaves along l.  The
+                    // probability a node keeps, 1 - sum(sp), is never formed, so its FP32
+                    // rounding cannot bias the total probability step after step.
+                    n0 += Px[rp] * spp - p0 * sp;
+                    n1 += Py[rp] * spp - p1 * sp;
+                    n2 += Pz[rp] * spp - p2 * sp;
                 }
             });
             if constexpr (INIT) {
@@ -99,20 +108,18 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                 const float fr = (a.ads && (m & INTERFACIAL_BIT)) ? frac - a.ka : frac;
                 if (fr < 1.1920929e-07f) bad = LBGPU_ERR_FRACTION;
             } else {
-                const float p0 = Px[r], p1 = Py[r], p2 = Pz[r];
                 v[0] = (double)p0 * ux;
                 v[1] = (double)p1 * uy;
                 v[2] = (double)p2 * uz;
                 if (!a.ads || !(m & INTERFACIAL_BIT)) {
-                    n0 += frac * p0;
-                    n1 += frac * p1;
-                    n2 += frac * p2;
+                    n0 += p0;
+                    n1 += p1;
+                    n2 += p2;
                 } else {
-                    const float f2 = frac - a.ka;
                     const float q0 = a.A[par][0][r], q1 = a.A[par][1][r], q2 = a.A[par][2][r];
-                    n0 += f2 * p0 + q0 * a.kd;
-                    n1 += f2 * p1 + q1 * a.kd;
-                    n2 += f2 * p2 + q2 * a.kd;
+                    n0 += (p0 - a.ka * p0) + q0 * a.kd;
+                    n1 += (p1 - a.ka * p1) + q1 * a.kd;
+                    n2 += (p2 - a.ka * p2) + q2 * a.kd;
                     a.A[par ^ 1][0][r] = q0 * a.one_minus_kd + p0 * a.ka;
                     a.A[par ^ 1][1][r] = q1 * a.one_minus_kd + p1 * a.ka;
                     a.A[par ^ 1][2][r] = q2 * a.one_minus_kd + p2 * a.ka;

@@ -67,7 +67,7 @@ def test_mp_c1_fp64(oracle_mod, adsorb):
 
 def test_mp_from_device_flow_state(oracle_mod):
     """drop_tracers after equilibration with no host round trip: moments taken on the device."""
-    nat = geo.porous_spheres(L=10, radius=2.0, porosity=0.7, seed=3)
+    nat = geo.cc(12, 12, 12)
     f_ext = (2e-5, 0.0, 0.0)
     ref = oracle_mod.equilibration(nat, tau=0.8, target_error=1e-9, f_ext=f_ext, max_steps=50000)
     v0, P1, vac, conv, P, A = oracle_mp(oracle_mod, nat, ref["rho"], ref["j"], f_ext, 100,
