@@ -74,26 +74,29 @@ __device__ __forceinline__ void pull19f(float (&g)[Q], const float *__restrict__
 //   d*_l = c1 d_l + (c2 E + c3 TE) +- (c2 O + c3 TO)
 // which halves the arithmetic of a direction-by-direction evaluation.  The per-pair force
 // constants kF = c3 a1 c.F and kT = c3 2 a2 c.F are precomputed on the host.
+// Every product and sum below is an explicit fused or separately rounded intrinsic, so the
+// same inputs give the same bits in every kernel that inlines this function (the compiler may
+// not re-contract it differently in different kernels).
 template <int FMASK>
 __device__ __forceinline__ void collide_dev(float (&g)[Q], const float drho, const float jx,
                                             const float jy, const float jz, const FlowArgs32 &a,
                                             const bool force)
 {
-    const float rho = a.rho0 + drho;
-    const float ir = 1.0f / rho;
-    const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
-    const float ju = jx * ux + jy * uy + jz * uz;
+    const float rho = __fadd_rn(a.rho0, drho);
+    const float ir = __fdiv_rn(1.0f, rho);
+    const float ux = __fmul_rn(jx, ir), uy = __fmul_rn(jy, ir), uz = __fmul_rn(jz, ir);
+    const float ju = __fmaf_rn(jx, ux, __fmaf_rn(jy, uy, __fmul_rn(jz, uz)));
     float base[3];
 #pragma unroll
-    for (int w = 0; w < 3; ++w) base[w] = a.c2w[w] * drho - a.c2a2cs2[w] * ju;
+    for (int w = 0; w < 3; ++w) base[w] = __fmaf_rn(a.c2w[w], drho, -__fmul_rn(a.c2a2cs2[w], ju));
     if constexpr (FMASK != 0) {
         if (force) {
-            const float uF = ux * a.F[0] + uy * a.F[1] + uz * a.F[2];
+            const float uF = __fmaf_rn(ux, a.F[0], __fmaf_rn(uy, a.F[1], __fmul_rn(uz, a.F[2])));
 #pragma unroll
-            for (int w = 0; w < 3; ++w) base[w] -= a.c3a1[w] * uF;
+            for (int w = 0; w < 3; ++w) base[w] = __fmaf_rn(-a.c3a1[w], uF, base[w]);
         }
     }
-    g[0] = a.c1 * g[0] + base[0];
+    g[0] = __fmaf_rn(a.c1, g[0], base[0]);
     static_for<0, 9>([&](auto P) {
         constexpr int p = decltype(P)::value;
         constexpr int l = pair_l(p);
@@ -102,16 +105,16 @@ __device__ __forceinline__ void collide_dev(float (&g)[Q], const float drho, con
         constexpr int w = wclass(l);
         const float cj = dotf<c.x, c.y, c.z>(jx, jy, jz);
         const float cu = dotf<c.x, c.y, c.z>(ux, uy, uz);
-        float A = base[w] + a.c2a2[w] * (cj * cu);
-        float B = a.c2a1[w] * cj;
+        float A = __fmaf_rn(a.c2a2[w], __fmul_rn(cj, cu), base[w]);
+        float B = __fmul_rn(a.c2a1[w], cj);
         if constexpr (FMASK != 0) {
             if (force) {
-                A += a.kT[p] * cu;
-                B += a.kF[p];
+                A = __fmaf_rn(a.kT[p], cu, A);
+                B = __fadd_rn(B, a.kF[p]);
             }
         }
-        g[l] = a.c1 * g[l] + (A + B);
-        g[li] = a.c1 * g[li] + (A - B);
+        g[l] = __fmaf_rn(a.c1, g[l], __fadd_rn(A, B));
+        g[li] = __fmaf_rn(a.c1, g[li], __fsub_rn(A, B));
     });
 }
 
@@ -142,9 +145,9 @@ __global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
         if constexpr (c.z < 0) jz -= g[l];
     });
     if (FMASK && a.force_moment) {
-        jx += 0.5f * a.F[0];
-        jy += 0.5f * a.F[1];
-        jz += 0.5f * a.F[2];
+        jx = __fadd_rn(jx, __fmul_rn(0.5f, a.F[0]));
+        jy = __fadd_rn(jy, __fmul_rn(0.5f, a.F[1]));
+        jz = __fadd_rn(jz, __fmul_rn(0.5f, a.F[2]));
     }
     collide_dev<FMASK>(g, drho, jx, jy, jz, a, a.force_collide != 0);
 #pragma unroll
@@ -208,9 +211,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
         if constexpr (c.z < 0) jz -= f[l];
     });
     if (FMASK && a.force_moment) {
-        jx += 0.5f * a.F[0];
-        jy += 0.5f * a.F[1];
-        jz += 0.5f * a.F[2];
+        jx = __fadd_rn(jx, __fmul_rn(0.5f, a.F[0]));
+        jy = __fadd_rn(jy, __fmul_rn(0.5f, a.F[1]));
+        jz = __fadd_rn(jz, __fmul_rn(0.5f, a.F[2]));
     }
     collide_dev<FMASK>(f, drho, jx, jy, jz, a, a.force_collide != 0);
     if constexpr (ODD) {

@@ -47,9 +47,9 @@ struct MpArgs64 {
 
 struct MpArgs32 {
     const uint32_t *mask;
-    const float *V[3];                 // (j + f_ext)/rho at every fluid node
-    float *P[2][3];
-    float *A[2][3];
+    const float4 *V;                   // (j + f_ext)/rho at every fluid node (w unused)
+    float4 *P[2];                      // propagated quantity (x, y, z, 0), now/next by parity
+    float4 *A[2];                      // adsorbed part
     double *partial;
     MpCtl *ctl;
     double *hist;
@@ -63,7 +63,7 @@ struct MpArgs32 {
 cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_mp_reduce_init(double *partial, unsigned nblocks, MpCtl *ctl, cudaStream_t s);
-cudaError_t launch_mp_v32(const MpArgs64 &a64, float *V0, float *V1, float *V2, cudaStream_t s);
+cudaError_t launch_mp_v32(const MpArgs64 &a64, float4 *V, cudaStream_t s);
 cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_mp_init_f32(const MpArgs32 &a, float bw, unsigned grid, cudaStream_t s);
 

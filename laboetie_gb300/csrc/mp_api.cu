@@ -162,16 +162,13 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
         MpArgs32 &b = s->a32;
         std::memset(&b, 0, sizeof(b));
         b.mask = ctx->d_mask;
-        float *V[3];
-        for (int d = 0; d < 3; ++d) {
-            if ((rc = alloc_zero(ctx, s, &V[d], (size_t)N))) return rc;
-            b.V[d] = V[d];
+        float4 *V;
+        if ((rc = alloc_zero(ctx, s, &V, (size_t)N))) return rc;
+        b.V = V;
+        for (int q = 0; q < 2; ++q) {
+            if ((rc = alloc_zero(ctx, s, &b.P[q], (size_t)N))) return rc;
+            if (s->ads && (rc = alloc_zero(ctx, s, &b.A[q], (size_t)N))) return rc;
         }
-        for (int q = 0; q < 2; ++q)
-            for (int d = 0; d < 3; ++d) {
-                if ((rc = alloc_zero(ctx, s, &b.P[q][d], (size_t)N))) return rc;
-                if (s->ads && (rc = alloc_zero(ctx, s, &b.A[q][d], (size_t)N))) return rc;
-            }
         b.partial = a.partial;
         b.ctl = a.ctl;
         b.N = N;
@@ -186,7 +183,7 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
             b.a1[w] = (float)a.a1[w];
             b.lwh[w] = (float)a.lwh[w];
         }
-        LBG_CK(ctx, launch_mp_v32(a, V[0], V[1], V[2], st));
+        LBG_CK(ctx, launch_mp_v32(a, V, st));
         LBG_CK(ctx, launch_mp_init_f32(b, (float)s->bw, s->nblocks, st));
     }
     LBG_CK(ctx, launch_mp_reduce_init(a.partial, s->nblocks, a.ctl, st));
@@ -242,8 +239,9 @@ static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done,
     cudaGraphExec_t exec;
     LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < G; ++k) {
-        cudaError_t e = s->prec == LBGPU_FP64 ? launch_mp_step_f64(s->a64, s->nblocks, st)
-                                              : launch_mp_step_f32(s->a32, s->nblocks, st);
+        const unsigned grid = std::min(s->nblocks, MP_MAX_BLOCKS);
+        cudaError_t e = s->prec == LBGPU_FP64 ? launch_mp_step_f64(s->a64, grid, st)
+                                              : launch_mp_step_f32(s->a32, grid, st);
         if (e != cudaSuccess) {
             cudaStreamEndCapture(st, &g);
             return ctx_cuda(ctx, e, "capture moment propagation");
@@ -326,12 +324,16 @@ int lbgpu_mp_get(lbgpu_ctx *ctx, double *P, double *P_ads)
             if (s->prec == LBGPU_FP64) {
                 const double *src = q == 0 ? s->a64.P[par][d] : s->a64.A[par][d];
                 LBG_CK(ctx, cudaMemcpyAsync(comp.data() + d * N, src, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
-            } else {
-                std::vector<float> f(N);
-                const float *src = q == 0 ? s->a32.P[par][d] : s->a32.A[par][d];
-                LBG_CK(ctx, cudaMemcpyAsync(f.data(), src, sizeof(float) * N, cudaMemcpyDeviceToHost, st));
+            } else if (d == 0) {
+                std::vector<float4> f(N);
+                const float4 *src = q == 0 ? s->a32.P[par] : s->a32.A[par];
+                LBG_CK(ctx, cudaMemcpyAsync(f.data(), src, sizeof(float4) * N, cudaMemcpyDeviceToHost, st));
                 LBG_CK(ctx, cudaStreamSynchronize(st));
-                for (long long i = 0; i < N; ++i) comp[d * N + i] = f[i];
+                for (long long i = 0; i < N; ++i) {
+                    comp[i] = f[i].x;
+                    comp[N + i] = f[i].y;
+                    comp[2 * N + i] = f[i].z;
+                }
             }
         }
         LBG_CK(ctx, cudaStreamSynchronize(st));

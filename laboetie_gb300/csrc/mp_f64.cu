@@ -122,57 +122,57 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
     if (bad) atomicOr(&a.ctl->status, bad);
 }
 
-// module_moment_propagation.f90:164-289, one step.
+// module_moment_propagation.f90:164-289, one step.  Grid-stride over the nodes.  The gathers
+// are branch-free: a link to a solid neighbour has coefficient 0 and the neighbour's P is 0, so
+// it adds an exact zero where the reference skips it (only the sign of an exact zero can differ).
 __global__ void __launch_bounds__(MP_BLOCK) k_mp_step(const MpArgs64 a)
 {
     const volatile MpCtl *vc = a.ctl;
     if (vc->done) return;
     const int par = vc->parity;
     const long long N = a.N;
-    const long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x;
+    const double *__restrict__ Px = a.P[par][0];
+    const double *__restrict__ Py = a.P[par][1];
+    const double *__restrict__ Pz = a.P[par][2];
     double v[3] = {0.0, 0.0, 0.0};
-    if (r < N) {
+    for (long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x; r < N;
+         r += (long long)gridDim.x * MP_BLOCK) {
         const uint32_t m = a.mask[r];
-        if (m & FLUID_BIT) {
-            long long X[3], Y[3], Z[3];
-            nb_offsets(r, a.lx, a.ly, a.lz, X, Y, Z);
-            const double *__restrict__ Px = a.P[par][0];
-            const double *__restrict__ Py = a.P[par][1];
-            const double *__restrict__ Pz = a.P[par][2];
-            double n0 = 0.0, n1 = 0.0, n2 = 0.0;
-            static_for<1, Q>([&](auto L) {
-                constexpr int l = decltype(L)::value;
-                constexpr Vel c = vel(l);
-                if ((m >> inv(l)) & 1u) return;
-                const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
-                const double cf = a.coef[(long long)(l - 1) * N + r];
-                n0 = n0 + Px[rp] * cf;
-                n1 = n1 + Py[rp] * cf;
-                n2 = n2 + Pz[rp] * cf;
-            });
-            const double p0 = Px[r], p1 = Py[r], p2 = Pz[r];
-            v[0] = p0 * a.us[0][r];
-            v[1] = p1 * a.us[1][r];
-            v[2] = p2 * a.us[2][r];
-            const double frac = a.frac[r];
-            if (!a.ads || !(m & INTERFACIAL_BIT)) {
-                n0 = n0 + frac * p0;
-                n1 = n1 + frac * p1;
-                n2 = n2 + frac * p2;
-            } else {
-                const double f2 = frac - a.ka;
-                const double q0 = a.A[par][0][r], q1 = a.A[par][1][r], q2 = a.A[par][2][r];
-                n0 = n0 + f2 * p0 + q0 * a.kd;
-                n1 = n1 + f2 * p1 + q1 * a.kd;
-                n2 = n2 + f2 * p2 + q2 * a.kd;
-                a.A[par ^ 1][0][r] = q0 * a.one_minus_kd + p0 * a.ka;
-                a.A[par ^ 1][1][r] = q1 * a.one_minus_kd + p1 * a.ka;
-                a.A[par ^ 1][2][r] = q2 * a.one_minus_kd + p2 * a.ka;
-            }
-            a.P[par ^ 1][0][r] = n0;
-            a.P[par ^ 1][1][r] = n1;
-            a.P[par ^ 1][2][r] = n2;
+        if (!(m & FLUID_BIT)) continue;
+        long long X[3], Y[3], Z[3];
+        nb_offsets(r, a.lx, a.ly, a.lz, X, Y, Z);
+        double n0 = 0.0, n1 = 0.0, n2 = 0.0;
+        static_for<1, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
+            const double cf = a.coef[(long long)(l - 1) * N + r];
+            n0 = n0 + Px[rp] * cf;
+            n1 = n1 + Py[rp] * cf;
+            n2 = n2 + Pz[rp] * cf;
+        });
+        const double p0 = Px[r], p1 = Py[r], p2 = Pz[r];
+        v[0] = v[0] + p0 * a.us[0][r];
+        v[1] = v[1] + p1 * a.us[1][r];
+        v[2] = v[2] + p2 * a.us[2][r];
+        const double frac = a.frac[r];
+        if (!a.ads || !(m & INTERFACIAL_BIT)) {
+            n0 = n0 + frac * p0;
+            n1 = n1 + frac * p1;
+            n2 = n2 + frac * p2;
+        } else {
+            const double f2 = frac - a.ka;
+            const double q0 = a.A[par][0][r], q1 = a.A[par][1][r], q2 = a.A[par][2][r];
+            n0 = n0 + f2 * p0 + q0 * a.kd;
+            n1 = n1 + f2 * p1 + q1 * a.kd;
+            n2 = n2 + f2 * p2 + q2 * a.kd;
+            a.A[par ^ 1][0][r] = q0 * a.one_minus_kd + p0 * a.ka;
+            a.A[par ^ 1][1][r] = q1 * a.one_minus_kd + p1 * a.ka;
+            a.A[par ^ 1][2][r] = q2 * a.one_minus_kd + p2 * a.ka;
         }
+        a.P[par ^ 1][0][r] = n0;
+        a.P[par ^ 1][1][r] = n1;
+        a.P[par ^ 1][2][r] = n2;
     }
     grid_sum3(v, a.partial, &a.ctl->blocks_done,
               [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });

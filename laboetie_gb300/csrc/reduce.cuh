@@ -33,17 +33,35 @@ __device__ __forceinline__ double block_sum_fixed(double v, double *sh)
     return v;
 }
 
+// Sum of 3 values over a block of MP_BLOCK threads in one pass (fixed order); valid in thread 0.
+__device__ __forceinline__ void block_sum3_fixed(double (&v)[3])
+{
+    __shared__ double sh[3][MP_BLOCK / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = warp_sum_fixed(v[d]);
+    __syncthreads();  // sh may still be read by a previous call
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) sh[d][wid] = v[d];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            v[d] = lane < MP_BLOCK / 32 ? sh[d][lane] : 0.0;
+            v[d] = warp_sum_fixed(v[d]);
+        }
+    }
+}
+
 // Every block stores its 3 partial sums; the last block to finish adds the partials in block
-// order and runs `finish(total)` in thread 0.  Returns true in the last block.
+// order and runs `finish(total)` in thread 0.
 template <typename Fin>
 __device__ __forceinline__ void grid_sum3(const double (&v)[3], double *partial, unsigned *counter,
                                           Fin &&finish)
 {
-    __shared__ double sh[MP_BLOCK / 32];
     __shared__ bool last;
-    double b[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) b[d] = block_sum_fixed(v[d], sh);
+    double b[3] = {v[0], v[1], v[2]};
+    block_sum3_fixed(b);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) partial[3 * blockIdx.x + d] = b[d];
@@ -59,14 +77,16 @@ __device__ __forceinline__ void grid_sum3(const double (&v)[3], double *partial,
 #pragma unroll
         for (int d = 0; d < 3; ++d) t[d] += p[d];
     }
-    double tot[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) tot[d] = block_sum_fixed(t[d], sh);
+    block_sum3_fixed(t);
     if (threadIdx.x == 0) {
         *counter = 0;
-        finish(tot);
+        finish(t);
     }
 }
+
+// Blocks of the propagation kernels: grid-stride over the nodes with at most 8 blocks per SM
+// of a 152-SM GB300, so the last block adds at most 1216 partials.
+constexpr unsigned MP_MAX_BLOCKS = 152 * 8;
 
 // module_moment_propagation.f90:262-288 after the sweep of step ctl->it: record VACF, rotate
 // now/next, test convergence (it > 2 and |VACF| below both thresholds).
