@@ -10,6 +10,9 @@
 namespace lbg {
 
 constexpr int MP_BLOCK = 256;
+// Blocks of the propagation kernels: grid-stride over the nodes with at most 8 blocks per SM
+// of a 152-SM GB300, so the last block adds at most 1216 partials.
+constexpr unsigned MP_MAX_BLOCKS = 152 * 8;
 
 // Device control block of the propagation loop (module_moment_propagation.f90:164-289).
 struct MpCtl {

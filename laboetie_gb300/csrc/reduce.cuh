@@ -84,10 +84,6 @@ __device__ __forceinline__ void grid_sum3(const double (&v)[3], double *partial,
     }
 }
 
-// Blocks of the propagation kernels: grid-stride over the nodes with at most 8 blocks per SM
-// of a 152-SM GB300, so the last block adds at most 1216 partials.
-constexpr unsigned MP_MAX_BLOCKS = 152 * 8;
-
 // module_moment_propagation.f90:262-288 after the sweep of step ctl->it: record VACF, rotate
 // now/next, test convergence (it > 2 and |VACF| below both thresholds).
 __device__ __forceinline__ void mp_control(MpCtl *c, double *hist, const double (&v)[3])
