@@ -158,6 +158,20 @@ int lbgpu_sync(lbgpu_ctx *ctx);
 int lbgpu_host_register(void *ptr, size_t bytes);
 int lbgpu_host_unregister(void *ptr);
 
+/* ---------------------------------------------------------------- no-allocation variant
+ * No counterpart in the reference.  For callers that cannot let the library allocate device
+ * memory (their populations already live on the GPU under their own allocator, or their loop
+ * runs under a fixed device-memory budget): the moments of lbgpu_moments on caller-owned
+ * device arrays, with no context and no cudaMalloc.  d_n is n(lx,ly,lz,19); d_jx/d_jy/d_jz hold
+ * j_old on entry and j on exit; *l2err (host, optional) = max|j - j_old|.  Boxes of more than
+ * 16,777,216 nodes (256^3) are rejected (LBGPU_ERR_INVALID): the reduction scratch is a fixed
+ * ~1 MiB device array per GPU, shared by all calls, so calls that overlap on the GPU race.  The
+ * first call on each device looks up that array's address; make it before any stream capture.
+ * stream: a cudaStream_t, or NULL for the default stream.  The call waits for its stream. */
+int lbgpu_moments_noalloc(int lx, int ly, int lz, const double *d_n, const double *d_fx,
+                          const double *d_fy, const double *d_fz, double *d_density,
+                          double *d_jx, double *d_jy, double *d_jz, double *l2err, void *stream);
+
 /* ---------------------------------------------------------------- tracer moment propagation */
 
 /* The lb.in tracer tags (drop_tracers.f90:88-92, module_moment_propagation.f90:41-71). */

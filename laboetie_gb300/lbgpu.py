@@ -117,6 +117,7 @@ def library():
         ("lbgpu_just_eq_smolu", [vp, pi]),
         ("lbgpu_poisson_nernst_planck", [vp, i, pi, pi]),
         ("lbgpu_charge_test", [vp, C.POINTER(d), C.POINTER(d)]),
+        ("lbgpu_moments_noalloc", [i, i, i] + [vp] * 8 + [C.POINTER(d), vp]),
     ):
         if hasattr(L, name):
             getattr(L, name).argtypes = args
