@@ -210,6 +210,48 @@ int lbgpu_mp_release(lbgpu_ctx *ctx);
 /* Time nsteps propagation steps (convergence test disabled) with CUDA events. */
 int lbgpu_time_mp_steps(lbgpu_ctx *ctx, int nsteps, float *ms);
 
+/* ---------------------------------------------------------------- Poisson + Nernst-Planck */
+
+enum lbgpu_poisson_solver {
+    LBGPU_POISSON_REFERENCE = 0,  /* sor.f90: over-relaxed Jacobi, omega 1.4, stop when
+                                     sum|phi* - phi| <= 1e-5 * anormf0 (bit-identical sweeps) */
+    LBGPU_POISSON_SOR4 = 1        /* 4-colour SOR of the same discrete equation with the given
+                                     omega and tol (stop when sum|dphi| <= tol * anormf0); needs
+                                     even lx, ly, lz, otherwise Jacobi with omega 1.4 and tol */
+};
+
+/* The lb.in tags of the charged system (charges_init.f90:23-134, poisson_nernst_planck.f90). */
+typedef struct {
+    double bjl, sigma, lambda_D, D_plus, D_minus;
+    int charge_distrib;   /* 0 = 'int' (charge on interfacial solid nodes); 1 = 'sol' (refused,
+                             as the reference stops on it) */
+    int solver;           /* enum lbgpu_poisson_solver */
+    double omega, tol;    /* LBGPU_POISSON_SOR4 only */
+    int max_iter;         /* sweeps per solve; 0 = the reference's 500 000 */
+    int np_loop_bug;      /* 1: Nernst-Planck links start only on the line (i, ly, lz), as the
+                             loop bounds of just_eq_smolu.f90:68-70 do; 0: every site */
+} lbgpu_pnp_params;
+
+/* charges_init.f90:23-135: c+, c- on the device, phi = 0; *anormf0 as the reference. */
+int lbgpu_pnp_init(lbgpu_ctx *ctx, const lbgpu_pnp_params *p, double *anormf0);
+int lbgpu_pnp_set(lbgpu_ctx *ctx, const double *c_plus, const double *c_minus, const double *phi,
+                  double anormf0);
+int lbgpu_pnp_get(lbgpu_ctx *ctx, double *c_plus, double *c_minus, double *phi, double *anormf0);
+
+/* sor.f90:7-91 (then anormf0 = sum|phi|).  *iters = the count the reference prints (iter-1). */
+int lbgpu_sor(lbgpu_ctx *ctx, int *iters);
+
+/* just_eq_smolu.f90:6-135 (eD = 0.1 D, at most 10 iterations, since time = 0 there). */
+int lbgpu_just_eq_smolu(lbgpu_ctx *ctx, int *iters);
+
+/* poisson_nernst_planck.f90:38-48 (until the relative changes of phi, c+ and c- are all below
+ * 1e-12, or max_outer iterations: LBGPU_ERR_STEP_CAP), then charge_test.f90. */
+int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *sor_iters_total);
+
+/* charge_test.f90:15-24: charges on solid and fluid nodes; LBGPU_ERR_CHARGE if they differ from
+ * sigma and -sigma by more than 1e-10. */
+int lbgpu_charge_test(lbgpu_ctx *ctx, double *solid_charge, double *fluid_charge);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,7 +5,8 @@
 // (drop_tracers.f90:97-100 divided by rho), so every probability of a step follows from V at
 // the node and at its neighbours.  V and the propagated quantity P are stored as float4
 // records (x, y, z, unused): a link costs two 16-byte gathers.  A step moves 52 bytes per fluid
-// node (V and P read, P written, the flag word); the VACF node sum is accumulated in FP64.
+// node (V and P read, P written, the flag word); the VACF node sum is formed per thread in FP32
+// over a few nodes and in FP64 across threads and blocks.
 // Solid neighbours hold V = 0 and P = 0 and their links are masked to zero, so the gathers are
 // branch-free and can all be in flight at once.
 #include "common.cuh"
@@ -43,7 +44,8 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
     const int par = INIT ? 0 : vc->parity;
     const float4 *__restrict__ Pn = a.P[par];
     const float4 *__restrict__ V = a.V;
-    double v[3] = {0.0, 0.0, 0.0};
+    // VACF partial of this thread: a few nodes summed in FP32, then FP64 across threads/blocks
+    float vt[3] = {0.0f, 0.0f, 0.0f};
     unsigned bad = 0;
     const unsigned N = (unsigned)a.N;
     for (unsigned r = blockIdx.x * MP_BLOCK + threadIdx.x; r < N; r += gridDim.x * MP_BLOCK) {
@@ -92,15 +94,15 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
         });
         if constexpr (INIT) {
             a.P[0][r] = make_float4(n0 * bw, n1 * bw, n2 * bw, 0.0f);
-            v[0] += (double)bw * v0;
-            v[1] += (double)bw * v1;
-            v[2] += (double)bw * v2;
+            vt[0] += v0;
+            vt[1] += v1;
+            vt[2] += v2;
             const float fr = (a.ads && (m & INTERFACIAL_BIT)) ? frac - a.ka : frac;
             if (fr < 1.1920929e-07f) bad = LBGPU_ERR_FRACTION;
         } else {
-            v[0] += (double)p.x * ux;
-            v[1] += (double)p.y * uy;
-            v[2] += (double)p.z * uz;
+            vt[0] += p.x * ux;
+            vt[1] += p.y * uy;
+            vt[2] += p.z * uz;
             n0 += p.x;
             n1 += p.y;
             n2 += p.z;
@@ -116,7 +118,9 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
             __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
         }
     }
+    double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     if constexpr (INIT) {
+        for (int d = 0; d < 3; ++d) v[d] *= (double)bw;
         block_sum3_fixed(v);
         if (threadIdx.x == 0)
             for (int d = 0; d < 3; ++d) a.partial[3 * blockIdx.x + d] = v[d];

@@ -1,0 +1,676 @@
+// pnp.cu -- Poisson + Nernst-Planck equilibration of the ion densities (compiled with
+// -fmad=false): charges_init.f90, sor.f90, just_eq_smolu.f90, poisson_nernst_planck.f90,
+// check_charge_distribution_equilibrium.f90, charge_test.f90.
+//
+// The potential and the ion densities stay in FP64.  The reference solver ("SOR", sor.f90) is an
+// over-relaxed Jacobi sweep with the D3Q19 weights including the self weight 1/3; each sweep is
+// reproduced operation for operation, so the iterates are bit-identical to the reference's.  The
+// fast solver is a 4-colour successive over-relaxation of the same discrete equation
+// (2/3) phi - sum_{l>0} w_l phi(x - c_l) = 4 pi bjl kBT/2 (c+ - c-): no two D3Q19 neighbours share
+// a colour ((x+z) mod 2, (y+z) mod 2) when lx, ly, lz are even.
+//
+// Sums that decide a stopping rule are formed in a fixed order (block partials added in block
+// order), so runs are reproducible; the normalisations that the reference forms once per call
+// (anormf0 = sum|phi|, charges_init.f90:126) are summed on the host in the reference's order.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "ctx.h"
+#include "lbgpu.h"
+#include "reduce.cuh"
+
+namespace lbg {
+
+namespace {
+constexpr int PB = MP_BLOCK;
+constexpr double PI_D = 3.141592653589793;   // acos(-1.0_dp), module_constants.f90:19
+}
+
+struct PnpCtl {
+    int iter, done, converged, parity;
+    int max_iter;
+    unsigned blocks_done;
+    double anorm, limit;  // stop when anorm <= limit
+};
+
+struct PnpState {
+    lbgpu_pnp_params p{};
+    double *phi[2] = {nullptr, nullptr};
+    double *cp = nullptr, *cm = nullptr;
+    double *fp = nullptr, *fm = nullptr;    // flux_site_plus / flux_site_minus
+    double *bak[3] = {nullptr, nullptr, nullptr};  // phi_old, c_plus_old, c_minus_old
+    double *partial = nullptr;              // 4 per block
+    double *result = nullptr;               // 4 reduced sums
+    PnpCtl *ctl = nullptr;
+    int par = 0;                            // buffer holding phi
+    double anormf0 = 0.0, rho_ch = 0.0;
+    bool charged = false;
+    std::vector<void *> allocs;
+};
+
+void pnp_release(lbgpu_ctx *ctx)
+{
+    if (!ctx->pnp) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void *p : ctx->pnp->allocs) cudaFree(p);
+    delete ctx->pnp;
+    ctx->pnp = nullptr;
+}
+
+namespace {
+
+struct PnpArgs {
+    const uint32_t *mask;
+    const double *phi;
+    double *phi_out;
+    const double *cp, *cm;
+    double *fp, *fm;
+    double *partial;
+    PnpCtl *ctl;
+    long long N;
+    int lx, ly, lz;
+    double a0[3];
+    double factor, omega, one_minus_omega;
+    double eDp, eDm;
+    double delta_axis, delta_diag;
+    int color;        // 4-colour SOR
+    int loop_bug;     // just_eq_smolu.f90:68-70
+};
+
+__device__ __forceinline__ void coords(long long r, int lx, int ly, int &x, int &y, int &z)
+{
+    const unsigned nd = (unsigned)r;
+    x = (int)(nd % (unsigned)lx);
+    const unsigned yz = nd / (unsigned)lx;
+    y = (int)(yz % (unsigned)ly);
+    z = (int)(yz / (unsigned)ly);
+}
+
+// offset of (x + dx, y + dy, z + dz), periodic, dx.. in {-1,0,1}
+__device__ __forceinline__ long long nb(int x, int y, int z, int dx, int dy, int dz, int lx, int ly, int lz)
+{
+    const int xx = dx > 0 ? wrap_plus(x, lx) : (dx < 0 ? wrap_minus(x, lx) : x);
+    const int yy = dy > 0 ? wrap_plus(y, ly) : (dy < 0 ? wrap_minus(y, ly) : y);
+    const int zz = dz > 0 ? wrap_plus(z, lz) : (dz < 0 ? wrap_minus(z, lz) : z);
+    return xx + (long long)lx * (yy + (long long)ly * zz);
+}
+
+// Final sum of the 4-value block partials of the last kernel, in block order.
+__global__ void __launch_bounds__(PB) k_sum4(const double *partial, unsigned nb, double *out)
+{
+    __shared__ double sh[4][PB / 32];
+    double t[4] = {0, 0, 0, 0};
+    for (unsigned i = threadIdx.x; i < nb; i += PB)
+        for (int q = 0; q < 4; ++q) t[q] += partial[4 * i + q];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int q = 0; q < 4; ++q) t[q] = warp_sum_fixed(t[q]);
+    if (lane == 0)
+        for (int q = 0; q < 4; ++q) sh[q][wid] = t[q];
+    __syncthreads();
+    if (wid == 0) {
+        for (int q = 0; q < 4; ++q) {
+            double v = lane < PB / 32 ? sh[q][lane] : 0.0;
+            v = warp_sum_fixed(v);
+            if (lane == 0) out[q] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void block_partial4(double (&t)[4], double *partial)
+{
+    __shared__ double sh[4][PB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int q = 0; q < 4; ++q) t[q] = warp_sum_fixed(t[q]);
+    if (lane == 0)
+        for (int q = 0; q < 4; ++q) sh[q][wid] = t[q];
+    __syncthreads();
+    if (wid == 0) {
+        for (int q = 0; q < 4; ++q) {
+            double v = lane < PB / 32 ? sh[q][lane] : 0.0;
+            v = warp_sum_fixed(v);
+            if (lane == 0) partial[4 * blockIdx.x + q] = v;
+        }
+    }
+}
+
+// sor.f90:48-70 one Jacobi sweep over every node (solid included), then the stopping test of
+// sor.f90:78 by the last block.
+__global__ void __launch_bounds__(PB) k_sor_jacobi(const PnpArgs a, double *phi0, double *phi1)
+{
+    const volatile PnpCtl *vc = a.ctl;
+    if (vc->done) return;
+    const int par = vc->parity;
+    const double *__restrict__ src = par ? phi1 : phi0;
+    double *__restrict__ dst = par ? phi0 : phi1;
+    double t[3] = {0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        int x, y, z;
+        coords(r, a.lx, a.ly, x, y, z);
+        double phistar = 0.0;
+        static_for<0, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            // phi(pbc(i - c_l)) (sor.f90:54-57)
+            phistar = phistar + a.a0[wclass(l)] * src[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)];
+        });
+        phistar = phistar + a.factor * (a.cp[r] - a.cm[r]);
+        const double phiold = src[r];
+        dst[r] = a.omega * phistar + a.one_minus_omega * phiold;
+        t[0] = t[0] + fabs(phistar - phiold);
+    }
+    grid_sum3(t, a.partial, &a.ctl->blocks_done, [&](const double (&tot)[3]) {
+        PnpCtl *c = a.ctl;
+        c->anorm = tot[0];
+        c->parity ^= 1;  // phi = phitmp (sor.f90:70)
+        c->iter += 1;
+        if (tot[0] <= c->limit) {
+            c->converged = 1;
+            c->done = 1;
+        } else if (c->iter >= c->max_iter) {
+            c->done = 1;
+        }
+    });
+}
+
+// One colour of the 4-colour SOR: phi <- (1-omega) phi + omega * 1.5 (sum_{l>0} w_l phi(x-c_l) + b).
+// The sum of |change| over the four colours is the stopping measure; colour 3 decides.
+__global__ void __launch_bounds__(PB) k_sor_color(const PnpArgs a, double *phi)
+{
+    const volatile PnpCtl *vc = a.ctl;
+    if (vc->done) return;
+    double t[3] = {0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        int x, y, z;
+        coords(r, a.lx, a.ly, x, y, z);
+        const int col = ((x + z) & 1) | (((y + z) & 1) << 1);
+        if (col != a.color) continue;
+        double s = 0.0;
+        static_for<1, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            s = s + a.a0[wclass(l)] * phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)];
+        });
+        const double target = 1.5 * (s + a.factor * (a.cp[r] - a.cm[r]));
+        const double old = phi[r];
+        const double nw = a.one_minus_omega * old + a.omega * target;
+        phi[r] = nw;
+        t[0] = t[0] + fabs(nw - old);
+    }
+    grid_sum3(t, a.partial, &a.ctl->blocks_done, [&](const double (&tot)[3]) {
+        PnpCtl *c = a.ctl;
+        c->anorm += tot[0];
+        if (a.color == 3) {
+            c->iter += 1;
+            if (c->anorm <= c->limit) {
+                c->converged = 1;
+                c->done = 1;
+            } else if (c->iter >= c->max_iter) {
+                c->done = 1;
+            }
+            if (!c->done) c->anorm = 0.0;
+        }
+    });
+}
+
+// Link flux of just_eq_smolu.f90:86-99 from site a (origin) to site b along direction l.
+__device__ __forceinline__ void link_flux(const PnpArgs &k, long long ra, long long rb, double delta,
+                                          double &Jp, double &Jm)
+{
+    const double e = exp(k.phi[rb] - k.phi[ra]);
+    const double em = 1.0 / e;
+    Jp = 0.5 * (1.0 + em) * (k.cp[rb] * e - k.cp[ra]);
+    Jp = Jp * k.eDp / delta;
+    Jm = 0.5 * (1.0 + e) * (k.cm[rb] * em - k.cm[ra]);
+    Jm = Jm * k.eDm / delta;
+}
+
+// flux_site_plus/minus of just_eq_smolu.f90:61-103 in gather form: every site adds the fluxes
+// of the links it starts (l = 2,4,..,18 of the reference) and subtracts those that end on it;
+// with loop_bug only sites of the line (i, ly, lz) start links.  Also the four sums of the
+// conservation test (108-112) and of the norm (122-129).
+__global__ void __launch_bounds__(PB) k_np_flux(const PnpArgs a)
+{
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        int x, y, z;
+        coords(r, a.lx, a.ly, x, y, z);
+        const bool fl = a.mask[r] & FLUID_BIT;
+        double sp = 0.0, sm = 0.0;
+        if (fl) {
+            const bool origin_me = !a.loop_bug || (y == a.ly - 1 && z == a.lz - 1);
+            static_for<0, 9>([&](auto P) {
+                // l = 2, 4, ..., 18 of the reference (just_eq_smolu.f90:66): one of each pair
+                constexpr int l = 2 * decltype(P)::value + 1;
+                constexpr Vel c = vel(l);
+                const double delta = wclass(l) == 1 ? a.delta_axis : a.delta_diag;
+                if (origin_me) {
+                    const long long rb = nb(x, y, z, c.x, c.y, c.z, a.lx, a.ly, a.lz);
+                    if (a.mask[rb] & FLUID_BIT) {
+                        double Jp, Jm;
+                        link_flux(a, r, rb, delta, Jp, Jm);
+                        sp = sp + Jp;
+                        sm = sm + Jm;
+                    }
+                }
+                // link that ends here: starts at r - c_l
+                const int ox = c.x > 0 ? wrap_minus(x, a.lx) : (c.x < 0 ? wrap_plus(x, a.lx) : x);
+                const int oy = c.y > 0 ? wrap_minus(y, a.ly) : (c.y < 0 ? wrap_plus(y, a.ly) : y);
+                const int oz = c.z > 0 ? wrap_minus(z, a.lz) : (c.z < 0 ? wrap_plus(z, a.lz) : z);
+                const bool origin_o = !a.loop_bug || (oy == a.ly - 1 && oz == a.lz - 1);
+                const long long ro = ox + (long long)a.lx * (oy + (long long)a.ly * oz);
+                if (origin_o && (a.mask[ro] & FLUID_BIT)) {
+                    double Jp, Jm;
+                    link_flux(a, ro, r, delta, Jp, Jm);
+                    sp = sp - Jp;
+                    sm = sm - Jm;
+                }
+            });
+        }
+        a.fp[r] = sp;
+        a.fm[r] = sm;
+        t[0] = t[0] + sp;
+        t[1] = t[1] + sm;
+        if (fl) {
+            t[2] = t[2] + sp * sp;
+            t[3] = t[3] + sm * sm;
+        }
+    }
+    block_partial4(t, a.partial);
+}
+
+// c+- += flux on fluid nodes (just_eq_smolu.f90:115-118)
+__global__ void __launch_bounds__(PB) k_np_update(const PnpArgs a, double *cp, double *cm)
+{
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        if (a.mask[r] & FLUID_BIT) {
+            cp[r] = cp[r] + a.fp[r];
+            cm[r] = cm[r] + a.fm[r];
+        }
+    }
+}
+
+// check_charge_distribution_equilibrium.f90:30-37: sums of |(v - v_old)/v_old| over |v_old| > 1e-12
+// and the counts, for phi (q = 0), c+ (1), c- (2).  Two launches: (phi, c+) and (c-).
+__global__ void __launch_bounds__(PB) k_rel_change(const double *v0, const double *o0, const double *v1,
+                                                   const double *o1, long long N, double *partial)
+{
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < N; r += (long long)gridDim.x * PB) {
+        const double eps = 1.0e-12;
+        if (fabs(o0[r]) > eps) {
+            t[0] = t[0] + fabs((v0[r] - o0[r]) / o0[r]);
+            t[1] = t[1] + 1.0;
+        }
+        if (v1 && fabs(o1[r]) > eps) {
+            t[2] = t[2] + fabs((v1[r] - o1[r]) / o1[r]);
+            t[3] = t[3] + 1.0;
+        }
+    }
+    block_partial4(t, partial);
+}
+
+// charge_test.f90:15-19: charge on solid and on fluid nodes.
+__global__ void __launch_bounds__(PB) k_charges(const uint32_t *mask, const double *cp, const double *cm,
+                                                long long N, double *partial)
+{
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < N; r += (long long)gridDim.x * PB) {
+        const double q = cp[r] - cm[r];
+        if (mask[r] & FLUID_BIT) t[1] = t[1] + q;
+        else t[0] = t[0] + q;
+    }
+    block_partial4(t, partial);
+}
+
+unsigned grid_for(long long N)
+{
+    const long long g = (N + PB - 1) / PB;
+    return (unsigned)std::min<long long>(g, MP_MAX_BLOCKS);
+}
+
+void fill_pnp_args(lbgpu_ctx *ctx, PnpArgs &a)
+{
+    PnpState *s = ctx->pnp;
+    std::memset(&a, 0, sizeof(a));
+    a.mask = ctx->d_mask;
+    a.phi = s->phi[s->par];
+    a.cp = s->cp;
+    a.cm = s->cm;
+    a.fp = s->fp;
+    a.fm = s->fm;
+    a.partial = s->partial;
+    a.ctl = s->ctl;
+    a.N = ctx->N;
+    a.lx = ctx->p.lx;
+    a.ly = ctx->p.ly;
+    a.lz = ctx->p.lz;
+    for (int w = 0; w < 3; ++w) a.a0[w] = ctx->K64.a0[w];
+    const volatile double kBT = 1.0 / 3.0;
+    a.factor = 4.0 * PI_D * s->p.bjl * kBT / 2.0;   // sor.f90:36
+    a.eDp = 0.1 * s->p.D_plus;                      // just_eq_smolu.f90:35-38
+    a.eDm = 0.1 * s->p.D_minus;
+    a.delta_axis = 1.0;
+    a.delta_diag = std::sqrt(2.0);
+    a.loop_bug = s->p.np_loop_bug;
+}
+
+int read4(lbgpu_ctx *ctx, unsigned nb, double out[4])
+{
+    PnpState *s = ctx->pnp;
+    LBG_CK(ctx, cudaGetLastError());
+    k_sum4<<<1, PB, 0, ctx->stream>>>(s->partial, nb, s->result);
+    LBG_CK(ctx, cudaGetLastError());
+    LBG_CK(ctx, cudaMemcpyAsync(out, s->result, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return LBGPU_OK;
+}
+
+// anormf0 = sum(abs(phi)) in the reference's order (sor.f90:90), on the host
+int sum_abs_phi(lbgpu_ctx *ctx, double *out)
+{
+    PnpState *s = ctx->pnp;
+    std::vector<double> h(ctx->N);
+    LBG_CK(ctx, cudaMemcpyAsync(h.data(), s->phi[s->par], sizeof(double) * ctx->N, cudaMemcpyDeviceToHost, ctx->stream));
+    LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    double a = 0.0;
+    for (long long i = 0; i < ctx->N; ++i) a = a + std::fabs(h[i]);
+    *out = a;
+    return LBGPU_OK;
+}
+
+int need_pnp(lbgpu_ctx *ctx, const char *fn)
+{
+    if (!ctx->pnp)
+        return ctx_fail(ctx, LBGPU_ERR_INVALID, std::string(fn) + ": call lbgpu_pnp_init first");
+    return LBGPU_OK;
+}
+
+}  // namespace
+}  // namespace lbg
+
+using namespace lbg;
+
+extern "C" {
+
+int lbgpu_pnp_init(lbgpu_ctx *ctx, const lbgpu_pnp_params *p, double *anormf0)
+{
+    if (!ctx || !p) return LBGPU_ERR_INVALID;
+    const double eps = 2.220446049250313e-16;
+    if (p->D_plus < 0.0) return ctx_fail(ctx, LBGPU_ERR_INVALID, "D_plus <0. critical.");
+    if (p->D_minus < 0.0) return ctx_fail(ctx, LBGPU_ERR_INVALID, "D_minus <0. critical.");
+    if (p->solver != LBGPU_POISSON_REFERENCE && p->solver != LBGPU_POISSON_SOR4)
+        return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_pnp_init: unknown solver");
+    pnp_release(ctx);
+    PnpState *s = new PnpState();
+    ctx->pnp = s;
+    s->p = *p;
+    const long long N = ctx->N;
+    cudaStream_t st = ctx->stream;
+    auto alloc = [&](double **q, size_t n) -> int {
+        LBG_CK(ctx, cudaMalloc((void **)q, n * sizeof(double)));
+        s->allocs.push_back(*q);
+        LBG_CK(ctx, cudaMemsetAsync(*q, 0, n * sizeof(double), st));
+        return LBGPU_OK;
+    };
+    int rc;
+    for (int b = 0; b < 2; ++b)
+        if ((rc = alloc(&s->phi[b], N))) return rc;
+    if ((rc = alloc(&s->cp, N)) || (rc = alloc(&s->cm, N)) || (rc = alloc(&s->fp, N)) ||
+        (rc = alloc(&s->fm, N)))
+        return rc;
+    for (int q = 0; q < 3; ++q)
+        if ((rc = alloc(&s->bak[q], N))) return rc;
+    if ((rc = alloc(&s->partial, 4 * (size_t)MP_MAX_BLOCKS)) || (rc = alloc(&s->result, 4))) return rc;
+    LBG_CK(ctx, cudaMalloc((void **)&s->ctl, sizeof(PnpCtl)));
+    s->allocs.push_back(s->ctl);
+    LBG_CK(ctx, cudaMemsetAsync(s->ctl, 0, sizeof(PnpCtl), st));
+
+    // charges_init.f90:23-135 on the host, node by node in the reference's order
+    if (p->bjl <= eps) {                       // :25 no charge at all
+        if (anormf0) *anormf0 = 0.0;
+        return lbgpu_sync(ctx);
+    }
+    const double pi = PI_D, kBT = 1.0 / 3.0;
+    double rho_0 = std::fabs(p->lambda_D) <= eps ? 0.0 : 1.0 / (4.0 * pi * p->bjl * (p->lambda_D * p->lambda_D));
+    s->rho_ch = 1.0 / (4.0 * pi * p->bjl * (p->lambda_D * p->lambda_D));
+    if (!(std::fabs(p->sigma) > eps)) {
+        if (anormf0) *anormf0 = 0.0;
+        return lbgpu_sync(ctx);
+    }
+    if (p->charge_distrib != 0)                // 'sol' stops the reference (charges_init.f90:96-100)
+        return ctx_fail(ctx, LBGPU_ERR_UNSUPPORTED, "only surface charge is implemented for now in charge_init.f90");
+    s->charged = true;
+    std::vector<uint32_t> m(N);
+    LBG_CK(ctx, cudaMemcpyAsync(m.data(), ctx->d_mask, sizeof(uint32_t) * N, cudaMemcpyDeviceToHost, st));
+    LBG_CK(ctx, cudaStreamSynchronize(st));
+    const long long count_fluid = (long long)ctx->counts[0], count_solid_int = (long long)ctx->counts[3];
+    const double sigma_solid = count_solid_int != 0 ? p->sigma / count_solid_int : 0.0;
+    const double sigma_fluid = count_fluid != 0 ? -1.0 * p->sigma / count_fluid : 0.0;
+    const double cps = +0.5 * sigma_solid, cms = -0.5 * sigma_solid;
+    double cpf, cmf;
+    if (sigma_fluid > 0.0) {
+        cpf = 0.5 * rho_0 + sigma_fluid;
+        cmf = 0.5 * rho_0;
+    } else {
+        cpf = 0.5 * rho_0;
+        cmf = 0.5 * rho_0 - sigma_fluid;
+    }
+    std::vector<double> hp(N), hm(N);
+    double sum = 0.0;
+    for (long long i = 0; i < N; ++i) {
+        const bool fluid = m[i] & FLUID_BIT, inter = m[i] & INTERFACIAL_BIT;
+        if (!fluid && inter) { hp[i] = cps; hm[i] = cms; }
+        else if (!fluid) { hp[i] = 0.0; hm[i] = 0.0; }
+        else { hp[i] = cpf; hm[i] = cmf; }
+        sum = sum + (hp[i] + hm[i]);
+    }
+    s->anormf0 = 4.0 * pi * p->bjl * kBT / 2.0 * sum;   // charges_init.f90:126
+    LBG_CK(ctx, cudaMemcpyAsync(s->cp, hp.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+    LBG_CK(ctx, cudaMemcpyAsync(s->cm, hm.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st));
+    LBG_CK(ctx, cudaStreamSynchronize(st));
+    if (anormf0) *anormf0 = s->anormf0;
+    return LBGPU_OK;
+}
+
+int lbgpu_pnp_set(lbgpu_ctx *ctx, const double *c_plus, const double *c_minus, const double *phi,
+                  double anormf0)
+{
+    if (!ctx || !c_plus || !c_minus || !phi) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_pnp_set");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    const size_t b = sizeof(double) * ctx->N;
+    LBG_CK(ctx, cudaMemcpyAsync(s->cp, c_plus, b, cudaMemcpyHostToDevice, ctx->stream));
+    LBG_CK(ctx, cudaMemcpyAsync(s->cm, c_minus, b, cudaMemcpyHostToDevice, ctx->stream));
+    LBG_CK(ctx, cudaMemcpyAsync(s->phi[s->par], phi, b, cudaMemcpyHostToDevice, ctx->stream));
+    s->anormf0 = anormf0;
+    s->charged = true;
+    return lbgpu_sync(ctx);
+}
+
+int lbgpu_pnp_get(lbgpu_ctx *ctx, double *c_plus, double *c_minus, double *phi, double *anormf0)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_pnp_get");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    const size_t b = sizeof(double) * ctx->N;
+    if (c_plus) LBG_CK(ctx, cudaMemcpyAsync(c_plus, s->cp, b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (c_minus) LBG_CK(ctx, cudaMemcpyAsync(c_minus, s->cm, b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (phi) LBG_CK(ctx, cudaMemcpyAsync(phi, s->phi[s->par], b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (anormf0) *anormf0 = s->anormf0;
+    return lbgpu_sync(ctx);
+}
+
+int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_sor");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    cudaStream_t st = ctx->stream;
+    if (iters) *iters = 0;
+    if (s->p.sigma == 0.0) {   // sor.f90:29-33
+        LBG_CK(ctx, cudaMemsetAsync(s->phi[s->par], 0, sizeof(double) * ctx->N, st));
+        return lbgpu_sync(ctx);
+    }
+    PnpArgs a;
+    fill_pnp_args(ctx, a);
+    const bool four = s->p.solver == LBGPU_POISSON_SOR4 && ctx->p.lx % 2 == 0 && ctx->p.ly % 2 == 0 &&
+                      ctx->p.lz % 2 == 0;
+    PnpCtl c;
+    std::memset(&c, 0, sizeof(c));
+    c.parity = s->par;
+    if (s->p.solver == LBGPU_POISSON_REFERENCE) {
+        a.omega = 1.4;                                  // sor.f90:19
+        c.limit = (double)1.0e-5f * s->anormf0;         // sor.f90:18,78
+        c.max_iter = s->p.max_iter > 0 ? s->p.max_iter : 500000;
+    } else {
+        a.omega = four ? s->p.omega : 1.4;
+        c.limit = s->p.tol * s->anormf0;
+        c.max_iter = s->p.max_iter > 0 ? s->p.max_iter : 500000;
+    }
+    a.one_minus_omega = 1.0 - a.omega;
+    LBG_CK(ctx, cudaMemcpyAsync(s->ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
+    const unsigned grid = grid_for(ctx->N);
+    const int G = 64;
+    cudaGraph_t g;
+    cudaGraphExec_t exec;
+    LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < G; ++k) {
+        if (four) {
+            for (int col = 0; col < 4; ++col) {
+                PnpArgs b = a;
+                b.color = col;
+                k_sor_color<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
+            }
+        } else {
+            k_sor_jacobi<<<grid, PB, 0, st>>>(a, s->phi[0], s->phi[1]);
+        }
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess) return ctx_cuda(ctx, e, "capture sor");
+    LBG_CK(ctx, cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+    for (;;) {
+        e = cudaGraphLaunch(exec, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&c, s->ctl, sizeof(c), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess || c.done) break;
+    }
+    cudaGraphExecDestroy(exec);
+    if (e != cudaSuccess) return ctx_cuda(ctx, e, "lbgpu_sor");
+    if (!four) s->par = c.parity;
+    if (iters) *iters = s->p.solver == LBGPU_POISSON_REFERENCE ? c.iter - 1 : c.iter;  // sor.f90:87
+    if ((rc = sum_abs_phi(ctx, &s->anormf0))) return rc;          // sor.f90:90
+    if (!c.converged)
+        return ctx_fail(ctx, LBGPU_ERR_STEP_CAP, "maximum iterations 500 000 reached without convergence in sor");
+    return LBGPU_OK;
+}
+
+int lbgpu_just_eq_smolu(lbgpu_ctx *ctx, int *iters)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_just_eq_smolu");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    cudaStream_t st = ctx->stream;
+    PnpArgs a;
+    fill_pnp_args(ctx, a);
+    const unsigned grid = grid_for(ctx->N);
+    const double crit = (double)5.e-6f;           // just_eq_smolu.f90:20
+    const double big = 1.7976931348623157e308;
+    double tot_p = big, tot_m = big;
+    const int max_iter = 10;                      // just_eq_smolu.f90:35-38
+    const double cf = (double)ctx->counts[0];
+    int iter = 0;
+    while (tot_m + tot_p > crit && iter < max_iter) {
+        k_np_flux<<<grid, PB, 0, st>>>(a);
+        double r4[4];
+        if ((rc = read4(ctx, grid, r4))) return rc;
+        if (std::fabs(r4[0]) > (double)1.e-12f || std::fabs(r4[1]) > (double)1.e-12f)
+            return ctx_fail(ctx, LBGPU_ERR_FLUX_SUM,
+                            "the sum of all flux does not add up. problem in just_eq_smolu.f90");
+        k_np_update<<<grid, PB, 0, st>>>(a, s->cp, s->cm);
+        LBG_CK(ctx, cudaGetLastError());
+        if (s->p.sigma != 0 && a.eDp != 0.0 && a.eDm != 0.0) {
+            tot_p = std::sqrt(r4[2]) / cf / (0.5 * s->rho_ch * a.eDp) / s->p.sigma;
+            tot_m = std::sqrt(r4[3]) / cf / (0.5 * s->rho_ch * a.eDm) / s->p.sigma;
+        }
+        iter = iter + 1;
+    }
+    if (iters) *iters = iter;
+    return lbgpu_sync(ctx);
+}
+
+int lbgpu_charge_test(lbgpu_ctx *ctx, double *solid_charge, double *fluid_charge)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_charge_test");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    const unsigned grid = grid_for(ctx->N);
+    k_charges<<<grid, PB, 0, ctx->stream>>>(ctx->d_mask, s->cp, s->cm, ctx->N, s->partial);
+    double r4[4];
+    if ((rc = read4(ctx, grid, r4))) return rc;
+    if (solid_charge) *solid_charge = r4[0];
+    if (fluid_charge) *fluid_charge = r4[1];
+    const double tol = (double)1.0e-10f;         // charge_test.f90:10
+    if (std::fabs(r4[0] - s->p.sigma) > tol || std::fabs(r4[1] + s->p.sigma) > tol)
+        return ctx_fail(ctx, LBGPU_ERR_CHARGE, "charge is not conserved. check charge_test.f90. stop");
+    return LBGPU_OK;
+}
+
+int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *sor_iters_total)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_poisson_nernst_planck");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    cudaStream_t st = ctx->stream;
+    if (outer) *outer = 0;
+    if (sor_iters_total) *sor_iters_total = 0;
+    if (!(std::fabs(s->p.sigma) > 2.220446049250313e-16)) return LBGPU_OK;   // poisson_nernst_planck.f90:20-21
+    const size_t b = sizeof(double) * ctx->N;
+    const unsigned grid = grid_for(ctx->N);
+    int n = 0, total = 0;
+    bool converged = false;
+    while (!converged) {
+        if (max_outer > 0 && n >= max_outer) {
+            if (outer) *outer = n;
+            if (sor_iters_total) *sor_iters_total = total;
+            return ctx_fail(ctx, LBGPU_ERR_STEP_CAP, "Equilibrium distribution of salts not found");
+        }
+        // backup_phi_c_plus_c_minus.f90
+        LBG_CK(ctx, cudaMemcpyAsync(s->bak[0], s->phi[s->par], b, cudaMemcpyDeviceToDevice, st));
+        LBG_CK(ctx, cudaMemcpyAsync(s->bak[1], s->cp, b, cudaMemcpyDeviceToDevice, st));
+        LBG_CK(ctx, cudaMemcpyAsync(s->bak[2], s->cm, b, cudaMemcpyDeviceToDevice, st));
+        int it = 0;
+        if ((rc = lbgpu_sor(ctx, &it))) return rc;
+        total += it;
+        if ((rc = lbgpu_just_eq_smolu(ctx, nullptr))) return rc;
+        // check_charge_distribution_equilibrium.f90:24-44
+        double r4[4], q4[4];
+        k_rel_change<<<grid, PB, 0, st>>>(s->phi[s->par], s->bak[0], s->cp, s->bak[1], ctx->N, s->partial);
+        if ((rc = read4(ctx, grid, r4))) return rc;
+        k_rel_change<<<grid, PB, 0, st>>>(s->cm, s->bak[2], nullptr, nullptr, ctx->N, s->partial);
+        if ((rc = read4(ctx, grid, q4))) return rc;
+        const double eps = 1.0e-12;
+        const double dphi = r4[1] != 0 ? r4[0] / r4[1] : 0.0;
+        const double dcp = r4[3] != 0 ? r4[2] / r4[3] : 0.0;
+        const double dcm = q4[1] != 0 ? q4[0] / q4[1] : 0.0;
+        converged = dphi < eps && dcp < eps && dcm < eps;
+        n++;
+    }
+    if (outer) *outer = n;
+    if (sor_iters_total) *sor_iters_total = total;
+    double sc, fc;
+    return lbgpu_charge_test(ctx, &sc, &fc);   // poisson_nernst_planck.f90:50
+}
+
+}  // extern "C"

@@ -328,3 +328,68 @@ Box.mp_propagate = _mp_propagate
 Box.mp_get = _mp_get
 Box.time_mp_steps = _time_mp_steps
 Box.mp_release = lambda self: self._chk(self.L.lbgpu_mp_release(self.ctx), "mp_release")
+
+
+POISSON_REFERENCE = 0
+POISSON_SOR4 = 1
+
+
+def _pnp_init(self, bjl=0.4, sigma=0.0, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
+              charge_distrib="int", solver=POISSON_REFERENCE, omega=1.8, tol=1e-10, max_iter=0,
+              np_loop_bug=True):
+    """charges_init.f90 on the device; returns anormf0."""
+    p = PnpParams()
+    p.bjl, p.sigma, p.lambda_D, p.D_plus, p.D_minus = bjl, sigma, lambda_D, D_plus, D_minus
+    p.charge_distrib = 0 if charge_distrib[:3] == "int" else 1
+    p.solver, p.omega, p.tol, p.max_iter, p.np_loop_bug = solver, omega, tol, max_iter, int(np_loop_bug)
+    an = C.c_double(0)
+    self._chk(self.L.lbgpu_pnp_init(self.ctx, C.byref(p), C.byref(an)), "pnp_init")
+    return an.value
+
+
+def _pnp_get(self):
+    cp, cm, phi = (np.zeros(self.shape) for _ in range(3))
+    an = C.c_double(0)
+    self._chk(self.L.lbgpu_pnp_get(self.ctx, _ptr(cp), _ptr(cm), _ptr(phi), C.byref(an)), "pnp_get")
+    return cp, cm, phi, an.value
+
+
+def _pnp_set(self, cp, cm, phi, anormf0):
+    a = [_f64(x, self.shape) for x in (cp, cm, phi)]
+    self._chk(self.L.lbgpu_pnp_set(self.ctx, *(_ptr(x) for x in a), C.c_double(anormf0)), "pnp_set")
+
+
+def _sor(self):
+    it = C.c_int(0)
+    self._chk(self.L.lbgpu_sor(self.ctx, C.byref(it)), "sor")
+    return it.value
+
+
+def _just_eq_smolu(self):
+    it = C.c_int(0)
+    self._chk(self.L.lbgpu_just_eq_smolu(self.ctx, C.byref(it)), "just_eq_smolu")
+    return it.value
+
+
+def _pnp(self, max_outer=0, check=True):
+    o, t = C.c_int(0), C.c_int(0)
+    rc = self.L.lbgpu_poisson_nernst_planck(self.ctx, max_outer, C.byref(o), C.byref(t))
+    if not check:
+        return o.value, t.value, rc
+    self._chk(rc, "poisson_nernst_planck")
+    return o.value, t.value
+
+
+def _charge_test(self):
+    s, f = C.c_double(0), C.c_double(0)
+    rc = self.L.lbgpu_charge_test(self.ctx, C.byref(s), C.byref(f))
+    return rc, s.value, f.value
+
+
+Box.pnp_init = _pnp_init
+Box.pnp_get = _pnp_get
+Box.pnp_set = _pnp_set
+Box.sor = _sor
+Box.just_eq_smolu = _just_eq_smolu
+Box.poisson_nernst_planck = _pnp
+Box.charge_test = _charge_test

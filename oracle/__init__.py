@@ -303,7 +303,7 @@ def charge_test(nature, cp, cm, sigma):
 
 
 def pnp(nature, bjl, sigma, D_plus, D_minus, rho_ch, cp, cm, phi, anormf0, loop_bug=True,
-        max_outer=10000):
+        max_outer=10000, check=True):
     nature = np.ascontiguousarray(nature, dtype=np.int8)
     cp = np.array(cp, dtype=np.float64, order="C")
     cm = np.array(cm, dtype=np.float64, order="C")
@@ -313,6 +313,7 @@ def pnp(nature, bjl, sigma, D_plus, D_minus, rho_ch, cp, cm, phi, anormf0, loop_
     rc = lib().orc_pnp(*_dims(nature), nature, bjl, sigma, D_plus, D_minus, rho_ch,
                        int(loop_bug), cp, cm, phi, C.byref(an), max_outer, C.byref(outer),
                        C.byref(tot))
-    _chk(rc, "pnp")
+    if check:
+        _chk(rc, "pnp")
     return dict(c_plus=cp, c_minus=cm, phi=phi, anormf0=an.value, outer=outer.value,
-                sor_iters=tot.value)
+                sor_iters=tot.value, status=rc)
