@@ -142,6 +142,20 @@ enum lbgpu_flow_mode {
 int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap,
                         int *steps_out);
 
+/* compensate_f_ext (equilibration.f90:388-487): the per-node field of f_ext spread over a
+ * spherical particle of odd diameter centred at particle_coords (1-based; NULL or zeros: the
+ * box centre), compensated by a uniform background force when geometry_label is -1.  Computed
+ * on the host from the context's geometry into fx/fy/fz (lx*ly*lz each); the reference's
+ * errors (even diameter, even box side, particle on a solid node) are returned as
+ * LBGPU_ERR_INVALID with its message. */
+int lbgpu_compensated_force_field(lbgpu_ctx *ctx, int particle_diameter,
+                                  const int particle_coords[3], int geometry_label, double *fx,
+                                  double *fy, double *fz);
+
+/* Force field applied by lbgpu_equilibration from the first convergence on, instead of the
+ * uniform f_ext on fluid nodes (FP64 contexts).  All three NULL: back to the uniform f_ext. */
+int lbgpu_set_force_field(lbgpu_ctx *ctx, const double *fx, const double *fy, const double *fz);
+
 /* Fixed-step flow: nsteps fused steps with the force of the given phase (0 = no force,
  * 1 = f_ext on fluid nodes), no convergence test (the timing mode). */
 int lbgpu_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on);

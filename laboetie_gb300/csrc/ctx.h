@@ -51,6 +51,8 @@ struct lbgpu_ctx {
     float *d_g[2] = {nullptr, nullptr};
     double *d_j[3] = {nullptr, nullptr, nullptr};
     double *d_rho = nullptr;
+    // per-node force field applied from the first convergence on (compensate_f_ext), or null
+    double *d_F[3] = {nullptr, nullptr, nullptr};
     lbg::FlowCtl *d_ctl = nullptr;
     lbg::Scratch *d_scratch = nullptr;
     lbg::LbConst64 K64{};

@@ -107,7 +107,10 @@ void ctx_release_device(lbgpu_ctx *ctx)
         cudaFree(ctx->d_f[b]);
         cudaFree(ctx->d_g[b]);
     }
-    for (int d = 0; d < 3; ++d) cudaFree(ctx->d_j[d]);
+    for (int d = 0; d < 3; ++d) {
+        cudaFree(ctx->d_j[d]);
+        cudaFree(ctx->d_F[d]);
+    }
     cudaFree(ctx->d_rho);
     cudaFree(ctx->d_ctl);
     cudaFree(ctx->d_scratch);
@@ -383,6 +386,10 @@ int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int h
     a.ctl = ctx->d_ctl;
     a.hist = d_hist;
     const int fmask = force_mask(ctx->p.f_ext);
+    const bool field = ctx->d_F[0] != nullptr;  // compensate_f_ext: a per-node force field
+    a.Fx = ctx->d_F[0];
+    a.Fy = ctx->d_F[1];
+    a.Fz = ctx->d_F[2];
     // one CUDA graph of G launches; the control block makes launches after the exit no-ops
     const long long N = ctx->N;
     int G = (int)std::min<long long>(512, std::max<long long>(8, (1LL << 24) / std::max<long long>(N, 1)));
@@ -391,7 +398,7 @@ int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int h
     cudaGraphExec_t exec;
     LBG_CK(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     for (int g = 0; g < G; ++g) {
-        cudaError_t e = launch_flow_step_f64(a, fmask, false, true, true, 0, s);
+        cudaError_t e = launch_flow_step_f64(a, fmask, field, true, true, 0, s);
         if (e != cudaSuccess) {
             cudaStreamEndCapture(s, &graph);
             return ctx_cuda(ctx, e, "capture flow step");

@@ -118,6 +118,8 @@ def library():
         ("lbgpu_poisson_nernst_planck", [vp, i, pi, pi]),
         ("lbgpu_charge_test", [vp, C.POINTER(d), C.POINTER(d)]),
         ("lbgpu_moments_noalloc", [i, i, i] + [vp] * 8 + [C.POINTER(d), vp]),
+        ("lbgpu_compensated_force_field", [vp, i, vp, i, vp, vp, vp]),
+        ("lbgpu_set_force_field", [vp, vp, vp, vp]),
     ):
         if hasattr(L, name):
             getattr(L, name).argtypes = args
@@ -393,3 +395,24 @@ Box.sor = _sor
 Box.just_eq_smolu = _just_eq_smolu
 Box.poisson_nernst_planck = _pnp
 Box.charge_test = _charge_test
+
+
+def _compensated_force_field(self, particle_diameter=1, particle_coords=(0, 0, 0), geometry_label=0):
+    f = [np.zeros(self.shape) for _ in range(3)]
+    pc = (C.c_int * 3)(*particle_coords)
+    rc = self.L.lbgpu_compensated_force_field(self.ctx, particle_diameter, pc, geometry_label,
+                                              *(_ptr(x) for x in f))
+    self._chk(rc, "compensated_force_field")
+    return f
+
+
+def _set_force_field(self, f):
+    if f is None:
+        self._chk(self.L.lbgpu_set_force_field(self.ctx, None, None, None), "set_force_field")
+        return
+    a = [_f64(x, self.shape) for x in f]
+    self._chk(self.L.lbgpu_set_force_field(self.ctx, *(_ptr(x) for x in a)), "set_force_field")
+
+
+Box.compensated_force_field = _compensated_force_field
+Box.set_force_field = _set_force_field

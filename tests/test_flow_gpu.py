@@ -250,3 +250,28 @@ def test_fp32_in_place_and_two_buffer_streaming_agree(monkeypatch):
         assert np.array_equal(na, nb) and np.array_equal(ra, rb)
         for d in range(3):
             assert np.array_equal(ja[d], jb[d])
+
+
+@pytest.mark.parametrize("label,make", [(-1, lambda: geo.bulk(9, 9, 9)),
+                                        (1, lambda: geo.slit(9, 7, 11))])
+def test_equilibration_compensated_force_bit_exact(oracle_mod, label, make):
+    """compensate_f_ext (equilibration.f90:388-487): a force on a particle of diameter 3 at the
+    box centre, compensated by a background force in the solid-free box."""
+    nat = make()
+    fe = (1e-4, 2e-5, 0.0)
+    ref = oracle_mod.equilibration(nat, tau=1.0, target_error=1e-10, f_ext=fe, max_steps=20000,
+                                   compensate_f_ext=True, particle_diameter=3,
+                                   geometry_label=label)
+    with Box(nat, relaxation_time=1.0, f_ext=fe, target_error=1e-10) as box:
+        f = box.compensated_force_field(particle_diameter=3, geometry_label=label)
+        for d in range(3):
+            assert np.array_equal(f[d], ref["f"][d])
+        box.set_force_field(f)
+        box.flow_init()
+        steps, hist = box.equilibration(max_steps=20000, hist_cap=20000)
+        n, rho, j = box.flow_get()
+    assert steps == ref["steps"]
+    assert np.array_equal(hist, ref["l2err"])
+    assert np.array_equal(n, ref["n"])
+    for d in range(3):
+        assert np.array_equal(j[d], ref["j"][d])
