@@ -54,6 +54,21 @@ def args_():
     ap.add_argument("--mp-steps", type=int, default=0, help="default: min(steps, 400)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # batched cells (1024 chromatography cells + 64 modulated tubes, flow then tracer)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-cells", type=int, default=1024)
+    ap.add_argument("--batch-tubes", type=int, default=64)
+    ap.add_argument("--batch-flow-steps", type=int, default=10000)
+    ap.add_argument("--batch-mp-steps", type=int, default=10000)
+    ap.add_argument("--batch-chunk", type=int, default=500, help="steps per call (one CUDA graph)")
+    ap.add_argument("--one-at-a-time-sample", type=int, default=6,
+                    help="cells (and a third as many tubes) timed one at a time")
+    # serving stream (Poisson arrivals, continuous batching)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-n", type=int, default=48)
+    ap.add_argument("--serve-rates", default="2,8,32")
+    ap.add_argument("--serve-max-steps", type=int, default=20000)
+    ap.add_argument("--serve-mp-steps", type=int, default=10000)
     return ap.parse_args()
 
 
@@ -169,6 +184,123 @@ def cpu_oracle_mlups(nature, seconds, threads):
         steps *= 2
     # subtract nothing: init_populations is part of every run but is one pass out of ~60 per step
     return nfluid * steps / dt / 1e6, steps, dt, time.perf_counter() - t0
+
+
+def bench_batched(a):
+    """1024 chromatography cells + 64 tubes in one batch: flow steps, tracer start, tracer steps.
+    Wall-clock solves/s through the public API, against the same solves one at a time through
+    the single-box API (a timed sample, extrapolated per family)."""
+    from laboetie_gb300 import FP32_DEV, Box
+    from laboetie_gb300 import workloads as wl
+    from laboetie_gb300.lbgpu import Batch
+
+    cells = wl.batched_cells(n_cells=a.batch_cells, n_tubes=a.batch_tubes)
+    KF, KM, CH = a.batch_flow_steps, a.batch_mp_steps, a.batch_chunk
+    if KF % CH or KM % CH or CH % 2:
+        raise SystemExit("batch steps must be multiples of an even --batch-chunk")
+    tracer = lambda fe: dict(wl.TRACER, f_ext=fe)
+    with Batch() as w:   # warm-up on a throwaway batch: module load, graph machinery
+        i = w.add(cells[0][0], f_ext=cells[0][1], tracer=tracer(cells[0][1]))
+        w.steps(CH)
+        w.mp_start(i)
+        w.steps(CH)
+    b = Batch()
+    ids = [b.add(n, f_ext=fe, tracer=tracer(fe)) for n, fe, _ in cells]
+    info = b.info()
+    node_steps = info["fluid_nodes"] * (KF + KM)
+    t0 = time.perf_counter()
+    for _ in range(KF // CH):
+        b.steps(CH)
+    for i in ids:
+        b.mp_start(i)
+    for _ in range(KM // CH):
+        b.steps(CH)
+    dt = time.perf_counter() - t0
+    v0, vs, _, st = b.mp_get(ids[0])
+    deff_cell0 = (v0 / 2 + vs).tolist()
+    b.close()
+    # one at a time through the single-box API: a sample of each family, extrapolated
+    fam = {"cell": [], "tube": []}
+    ns = a.one_at_a_time_sample
+    sample = [c for c in cells if c[2] == "cell"][:ns] + [c for c in cells if c[2] == "tube"][:max(1, ns // 3)]
+    for n, fe, f in sample:
+        nf = int((n == 0).sum())
+        t = time.perf_counter()
+        with Box(n, relaxation_time=1.0, f_ext=fe, precision=FP32_DEV) as box:
+            box.flow_init()
+            box.flow_steps(KF, force_on=True)
+            box.mp_init(**tracer(fe))
+            box.mp_propagate(KM)
+        fam[f].append((time.perf_counter() - t, nf))
+    t_one = 0.0
+    for f in ("cell", "tube"):
+        if not fam[f]:
+            continue
+        tot_nf = sum(int((n == 0).sum()) for n, _, g in cells if g == f)
+        rate = sum(x[1] for x in fam[f]) / sum(x[0] for x in fam[f])   # fluid nodes per second
+        t_one += tot_nf / rate
+    n_solves = len(cells)
+    return {
+        "metric": "batched solves/s", "value": round(n_solves / dt, 3), "unit": "solves/s",
+        "seconds": round(dt, 3), "solves": n_solves,
+        "mlups": round(node_steps / dt / 1e6, 1),
+        "config": {"workload": f"{a.batch_cells} chromatography cells 1x50x50 (k discs d=10, k in 1..8) + "
+                               f"{a.batch_tubes} tubes 32x32xL (L in 64..256, radius 6..14), tau 1, "
+                               "f_ext 1e-5 along the flow axis",
+                   "flow_steps": KF, "mp_steps": KM, "steps_per_graph": CH,
+                   "tracer": "Db 0.01, K = e (kd 0.01)", "fluid_nodes": info["fluid_nodes"],
+                   "smem_boxes": info["smem_boxes"], "bytes": info["bytes"]},
+        "one_at_a_time": {"value": round(n_solves / t_one, 3), "unit": "solves/s",
+                          "sample": f"{len(fam['cell'])} cells + {len(fam['tube'])} tubes timed through "
+                                    "lbgpu_flow_steps/lbgpu_mp_propagate one box at a time, "
+                                    "extrapolated per family by fluid nodes",
+                          "seconds_extrapolated": round(t_one, 2)},
+        "speedup_vs_one_at_a_time": round(t_one / dt, 2),
+        "d_eff_cell0": deff_cell0,
+    }
+
+
+def bench_serving(a):
+    """Poisson request streams at several rates through lbgpu_serve (continuous batching):
+    p50/p99 latency (arrival to finish) and solves/s; the same stream served one request at a
+    time (each alone, back to back) as the no-batching baseline of the highest rate."""
+    from laboetie_gb300 import workloads as wl
+    from laboetie_gb300.lbgpu import Batch
+
+    rates = [float(x) for x in a.serve_rates.split(",") if x]
+    out = []
+    fifo = None
+    for k, rate in enumerate(rates):
+        reqs = wl.serving_stream(seed=1000 + k, n=a.serve_n, rate=rate, max_steps=a.serve_max_steps,
+                                 mp_steps=a.serve_mp_steps)
+        fams = [r.pop("family") for r in reqs]
+        with Batch() as b:
+            t = time.perf_counter()
+            res = b.serve(reqs, du_tol=1e-8, check_every=100)
+            wall = time.perf_counter() - t
+        lat = np.array([r["finished"] - q["arrival"] for r, q in zip(res, reqs)])
+        ok = [r for r in res if r["status"] == 0]
+        out.append({"rate_per_s": rate, "n": len(reqs), "ok": len(ok),
+                    "converged": sum(1 for r in ok if r["converged"]),
+                    "solves_per_s": round(len(ok) / wall, 3), "seconds": round(wall, 2),
+                    "p50_s": round(float(np.percentile(lat, 50)), 4),
+                    "p99_s": round(float(np.percentile(lat, 99)), 4),
+                    "mean_flow_steps": round(float(np.mean([r["steps"] for r in ok])), 1),
+                    "families": {f: fams.count(f) for f in sorted(set(fams))}})
+        if k == len(rates) - 1:
+            t = time.perf_counter()
+            for q in reqs:
+                with Batch() as b:
+                    b.serve([dict(q, arrival=0.0)], du_tol=1e-8, check_every=100)
+            t_fifo = time.perf_counter() - t
+            fifo = {"solves_per_s": round(len(reqs) / t_fifo, 3), "seconds": round(t_fifo, 2),
+                    "what": "the highest-rate stream, each request served alone, back to back"}
+    return {"metric": "served solves/s, p50/p99 latency", "rates": out, "one_at_a_time": fifo,
+            "config": {"workload": "Poisson arrivals; slit 4x4x(16..128), cylinder z (16..96)^2 x 32 "
+                                   "r = lx/2-2, touching spheres cubic cell 32..96, spherical cavity "
+                                   "24..80; FP32 flow to max|du| < 1e-8 between 100-step checks "
+                                   f"(cap {a.serve_max_steps}), then {a.serve_mp_steps} tracer steps",
+                       "tracer": "Db 0.01, K = e (kd 0.01)", "f_ext": 1e-5}}
 
 
 def run_reference(a):
@@ -295,7 +427,7 @@ def main():
     mlups64 = world * nfluid * K64 / (ms64 * 1e-3) / 1e6
     achieved32 = BYTES_F32 * nfluid / (ms_step32 * 1e-3) / 1e9
     achieved64 = BYTES_F64 * nfluid / (ms_step64 * 1e-3) / 1e9
-    tr = ncu_traffic("flow_step_f32_192cube.md")
+    tr = ncu_traffic("flow_aa_f32_porous128.md")
     h2d = (19 + 4) * 8 * nature.size
     d2h = 4 * 8 * nature.size
     line = {
@@ -336,6 +468,10 @@ def main():
         "clocks": clocks_out,
         "cpu_baseline": cpu,
     }
+    if world == 1 and not a.no_batch:
+        line["batched"] = bench_batched(a)
+    if world == 1 and not a.no_serve:
+        line["serving"] = bench_serving(a)
     print(json.dumps(line), flush=True)
 
 

@@ -224,6 +224,78 @@ int lbgpu_mp_release(lbgpu_ctx *ctx);
 /* Time nsteps propagation steps (convergence test disabled) with CUDA events. */
 int lbgpu_time_mp_steps(lbgpu_ctx *ctx, int nsteps, float *ms);
 
+/* ---------------------------------------------------------------- batches of boxes, serving
+ * Many independent boxes (cells) of any size stepped together in FP32 deviations with in-place
+ * streaming, each in one of two phases: flow, then (optionally) the moment propagation of a
+ * neutral tracer in the box's final flow field.  Large boxes are stepped by one tiled launch
+ * per step and phase, boxes of up to ~2,700 nodes by one block each that keeps the box in
+ * shared memory for all the steps of a call; one call's launches run as a CUDA graph.  The
+ * force acts from the first step on (a steady-state solve, no two-phase loop); the convergence
+ * test is max|u - u_prev| between two checks.  A box's results do not depend on the other
+ * boxes in the batch.  Errors of these calls are read with lbgpu_last_error(NULL, ...). */
+typedef struct lbgpu_batch lbgpu_batch;
+
+typedef struct {
+    int lx, ly, lz;
+    double relaxation_time;
+    double f_ext[3];
+    double rho0;
+    lbgpu_tracer tracer;   /* Db = 0: no tracer phase; else a neutral tracer (z = 0, Ds = 0) */
+} lbgpu_cell;
+
+/* memory_budget: bytes of device memory the batch may hold (0 = 90 % of the free memory). */
+int lbgpu_batch_create(int device, size_t memory_budget, lbgpu_batch **out);
+void lbgpu_batch_destroy(lbgpu_batch *b);
+/* Device bytes a box of this cell takes (its share of the memory budget). */
+size_t lbgpu_batch_footprint(const lbgpu_cell *cell);
+/* Add a box at rest (rho = rho0, j = 0) in the flow phase; *id is its slot.  LBGPU_ERR_OOM
+ * beyond the budget. */
+int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *cell, const int8_t *nature, int *id);
+int lbgpu_batch_remove(lbgpu_batch *b, int id);
+/* nsteps (even) steps of every box in its phase; with check, du[id] = max|u - u_prev| per slot
+ * of the flow-phase boxes (u_prev: the velocity at the previous check, 0 at the first). */
+int lbgpu_batch_steps(lbgpu_batch *b, int nsteps, int check, float *du);
+int lbgpu_batch_time_steps(lbgpu_batch *b, int nsteps, float *ms);
+/* density and flux (FP64) of box id from its flow populations */
+int lbgpu_batch_moments(lbgpu_batch *b, int id, double *density, double *jx, double *jy,
+                        double *jz);
+/* Tracer phase of box id (drop_tracers.f90, module_moment_propagation.f90:30-160 in FP32):
+ * V = (j + f_ext)/rho from the flow state, P(t=1) and VACF(0); LBGPU_ERR_FRACTION if a
+ * remaining fraction is below epsilon.  The box's later steps propagate the tracer. */
+int lbgpu_batch_mp_start(lbgpu_batch *b, int id);
+/* VACF(0), sum of VACF(t) over the tracer steps so far, VACF of the last step (FP64 sums of
+ * per-tile FP64 partials); D_eff = vacf0/2 + vacf_sum (Green-Kubo, unit time step). */
+int lbgpu_batch_mp_get(lbgpu_batch *b, int id, double vacf0[3], double vacf_sum[3],
+                       double vacf_last[3], int *steps);
+int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *smem_boxes,
+                     size_t *bytes_used);
+
+typedef struct {
+    lbgpu_cell cell;
+    const int8_t *nature;   /* the caller keeps it alive until lbgpu_serve returns */
+    double arrival;         /* seconds after the start of lbgpu_serve */
+    int max_steps;          /* flow step cap (0: none) */
+    int mp_steps;           /* tracer steps after the flow (0: none; needs cell.tracer.Db > 0),
+                               rounded up to whole rounds of check_every */
+    double *out_density, *out_jx, *out_jy, *out_jz;   /* optional: final flow moments */
+} lbgpu_request;
+
+typedef struct {
+    double admitted, finished;   /* seconds after the start; -1 if never */
+    int steps, converged, status, mp_steps;
+    long long fluid_nodes;
+    double vacf0[3], vacf_sum[3];
+} lbgpu_request_result;
+
+/* Request server (continuous batching) on an empty batch: a request is admitted once it has
+ * arrived and its buffers fit the batch's memory budget (in arrival order), is stepped with all
+ * resident boxes in rounds of check_every steps, ends its flow when du < du_tol at a check
+ * after the first or at its step cap, then runs its tracer steps, and leaves.  Admission,
+ * phase changes and departures happen between rounds, so requests that arrive while others
+ * run join the next round. */
+int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *requests, int n, double du_tol,
+                int check_every, lbgpu_request_result *results);
+
 /* ---------------------------------------------------------------- Poisson + Nernst-Planck */
 
 enum lbgpu_poisson_solver {

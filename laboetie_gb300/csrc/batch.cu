@@ -1,0 +1,498 @@
+// batch.cu -- kernels stepping many independent boxes together (FP32 deviations, in-place AA;
+// FP32 tracer moment propagation).
+//
+// Large boxes are cut into tiles of BATCH_BLOCK consecutive nodes; one launch steps every tile
+// of every large box in a phase (a tile never straddles two boxes, so a block reads one
+// descriptor).  Small boxes are stepped by a persistent block each that loads the whole box
+// into shared memory, runs all the steps of a call there with a block barrier between steps,
+// and writes it back: HBM is touched twice per call instead of twice per step.  Every box is
+// updated by its own threads only and its arithmetic does not depend on which other boxes
+// share the launch, so a box gives the same result alone and in any mix.
+#include "batch.h"
+#include "collide32.cuh"
+#include "common.cuh"
+#include "lbgpu.h"
+
+namespace lbg {
+namespace {
+
+// One AA update of one fluid node of a box whose populations start at g (global or shared).
+template <bool ODD>
+__device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uint32_t m,
+                                        const BatchInst &I)
+{
+    float f[Q];
+    unsigned off[Q];
+    if constexpr (ODD) {
+        const int lx = I.lx, ly = I.ly, lz = I.lz;
+        const int x = (int)(node % (unsigned)lx);
+        const unsigned yz = node / (unsigned)lx;
+        const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
+        const int sy = lx, sz = lx * ly;
+        // [c+1] = coordinate of (x - c)
+        const int X[3] = {wrap_plus(x, lx), x, wrap_minus(x, lx)};
+        const int Y[3] = {wrap_plus(y, ly) * sy, y * sy, wrap_minus(y, ly) * sy};
+        const int Z[3] = {wrap_plus(z, lz) * sz, z * sz, wrap_minus(z, lz) * sz};
+        static_for<0, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel c = vel(l);
+            if constexpr (l == 0) {
+                off[0] = node;
+            } else {
+                const unsigned s = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
+                off[l] = ((m >> l) & 1u) ? (unsigned)l * N + node : (unsigned)inv(l) * N + s;
+            }
+        });
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = g[off[l]];
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = g[(unsigned)l * N + node];
+    }
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        drho += f[l];
+        if constexpr (c.x > 0) jx += f[l];
+        if constexpr (c.x < 0) jx -= f[l];
+        if constexpr (c.y > 0) jy += f[l];
+        if constexpr (c.y < 0) jy -= f[l];
+        if constexpr (c.z > 0) jz += f[l];
+        if constexpr (c.z < 0) jz -= f[l];
+    });
+    if (I.force) {
+        jx = __fadd_rn(jx, __fmul_rn(0.5f, I.F[0]));
+        jy = __fadd_rn(jy, __fmul_rn(0.5f, I.F[1]));
+        jz = __fadd_rn(jz, __fmul_rn(0.5f, I.F[2]));
+    }
+    collide_dev<7>(f, drho, jx, jy, jz, I, I.force != 0);
+    if constexpr (ODD) {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[(unsigned)inv(l) * N + node] = f[l];
+    }
+}
+
+template <int CX, int CY, int CZ>
+__device__ __forceinline__ float cdot(const float4 &v)
+{
+    float s = 0.0f;
+    if constexpr (CX > 0) s += v.x;
+    if constexpr (CX < 0) s -= v.x;
+    if constexpr (CY > 0) s += v.y;
+    if constexpr (CY < 0) s -= v.y;
+    if constexpr (CZ > 0) s += v.z;
+    if constexpr (CZ < 0) s -= v.z;
+    return s;
+}
+
+// One tracer step at fluid node r, flux form of mp_f32.cu (module_moment_propagation.f90:207-253);
+// with INIT, P(t=1) and the node's VACF(0) term instead (module_moment_propagation.f90:112-136).
+// vt receives the node's VACF term (before the 1/Pstat factor for INIT).
+template <bool INIT>
+__device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float4 *Pnext,
+                                        const float4 *An, float4 *Anext, unsigned r, uint32_t m,
+                                        const BatchInst &I, double (&vt)[3], unsigned &bad)
+{
+    const int lx = I.lx, ly = I.ly, lz = I.lz;
+    const int x = (int)(r % (unsigned)lx);
+    const unsigned yz = r / (unsigned)lx;
+    const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
+    const int sy = lx, sz = lx * ly;
+    // [c+1] = coordinate of (x + c), periodic
+    const int X[3] = {wrap_minus(x, lx), x, wrap_plus(x, lx)};
+    const int Y[3] = {wrap_minus(y, ly) * sy, y * sy, wrap_plus(y, ly) * sy};
+    const int Z[3] = {wrap_minus(z, lz) * sz, z * sz, wrap_plus(z, lz) * sz};
+    const float4 vr = V[r];
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (!INIT) p = Pn[r];
+    float frac = 1.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+    static_for<1, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        constexpr int w = wclass(l);
+        const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
+        const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
+        const float4 vn = V[rp];
+        const float sp = on * (I.a1[w] * cdot<c.x, c.y, c.z>(vr) + I.lwh[w]);
+        const float spp = on * (I.a1[w] * cdot<-c.x, -c.y, -c.z>(vn) + I.lwh[w]);
+        frac -= sp;
+        ux += c.x * sp;
+        uy += c.y * sp;
+        uz += c.z * sp;
+        if constexpr (INIT) {
+            v0 += c.x * c.x * sp;
+            v1 += c.y * c.y * sp;
+            v2 += c.z * c.z * sp;
+            n0 -= c.x * spp;
+            n1 -= c.y * spp;
+            n2 -= c.z * spp;
+        } else {
+            const float4 pn = Pn[rp];
+            n0 += pn.x * spp - p.x * sp;
+            n1 += pn.y * spp - p.y * sp;
+            n2 += pn.z * spp - p.z * sp;
+        }
+    });
+    if constexpr (INIT) {
+        Pnext[r] = make_float4(n0 * I.bw, n1 * I.bw, n2 * I.bw, 0.0f);
+        vt[0] += (double)v0;
+        vt[1] += (double)v1;
+        vt[2] += (double)v2;
+        const float fr = (I.ads && (m & INTERFACIAL_BIT)) ? frac - I.ka : frac;
+        if (fr < 1.1920929e-07f) bad = 1u;
+    } else {
+        vt[0] += (double)(p.x * ux);
+        vt[1] += (double)(p.y * uy);
+        vt[2] += (double)(p.z * uz);
+        n0 += p.x;
+        n1 += p.y;
+        n2 += p.z;
+        if (I.ads && (m & INTERFACIAL_BIT)) {
+            const float4 q = An[r];
+            n0 += q.x * I.kd - I.ka * p.x;
+            n1 += q.y * I.kd - I.ka * p.y;
+            n2 += q.z * I.kd - I.ka * p.z;
+            Anext[r] = make_float4(q.x * I.one_minus_kd + p.x * I.ka, q.y * I.one_minus_kd + p.y * I.ka,
+                                   q.z * I.one_minus_kd + p.z * I.ka, 0.0f);
+        }
+        Pnext[r] = make_float4(n0, n1, n2, 0.0f);
+    }
+}
+
+// Sum of 3 doubles over the block in a fixed order (lanes by shuffle tree, then warps in index
+// order); valid in thread 0.  Any block size that is a multiple of 32, up to 1024.
+__device__ __forceinline__ void block_sum3(double (&v)[3])
+{
+    __shared__ double sh[3][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[d] += __shfl_down_sync(0xffffffffu, v[d], o);
+    __syncthreads();  // sh may still be read by a previous call
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) sh[d][wid] = v[d];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (int k = 0; k < nw; ++k) s += sh[d][k];
+            v[d] = s;
+        }
+}
+
+__device__ __forceinline__ unsigned *status_word(const BatchInst &I)
+{
+    const unsigned ntile = ((unsigned)I.N + BATCH_BLOCK - 1) / BATCH_BLOCK;
+    return reinterpret_cast<unsigned *>(I.tacc + (size_t)ntile * BATCH_TACC);
+}
+
+// Velocity u = j/rho of a node in natural order (after an even number of AA launches).
+__device__ __forceinline__ float3 node_velocity(const float *g, unsigned N, unsigned node,
+                                                const BatchInst &I)
+{
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        const float v = g[(unsigned)l * N + node];
+        drho += v;
+        if constexpr (c.x > 0) jx += v;
+        if constexpr (c.x < 0) jx -= v;
+        if constexpr (c.y > 0) jy += v;
+        if constexpr (c.y < 0) jy -= v;
+        if constexpr (c.z > 0) jz += v;
+        if constexpr (c.z < 0) jz -= v;
+    });
+    if (I.force) {
+        jx += 0.5f * I.F[0];
+        jy += 0.5f * I.F[1];
+        jz += 0.5f * I.F[2];
+    }
+    const float ir = 1.0f / (I.rho0 + drho);
+    return make_float3(jx * ir, jy * ir, jz * ir);
+}
+
+__device__ __forceinline__ float du_and_store(float4 *uprev, unsigned node, const float3 u)
+{
+    const float4 p = uprev[node];
+    uprev[node] = make_float4(u.x, u.y, u.z, 0.0f);
+    return fmaxf(fmaxf(fabsf(u.x - p.x), fabsf(u.y - p.y)), fabsf(u.z - p.z));
+}
+
+// FP64 density and flux of a node in natural order (solid nodes: zeros).
+__device__ __forceinline__ void node_moments64(const BatchInst &I, unsigned node, double &rho,
+                                               double &X, double &Y, double &Z)
+{
+    const unsigned N = (unsigned)I.N;
+    double d = 0.0;
+    X = Y = Z = 0.0;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        const double v = (double)I.g[(unsigned)l * N + node];
+        d += v;
+        X += c.x * v;
+        Y += c.y * v;
+        Z += c.z * v;
+    });
+    if (I.force) {
+        X += 0.5 * (double)I.F[0];
+        Y += 0.5 * (double)I.F[1];
+        Z += 0.5 * (double)I.F[2];
+    }
+    rho = (double)I.rho0 + d;
+}
+
+template <bool ODD>
+__global__ void __launch_bounds__(BATCH_BLOCK, 3) k_batch_aa(const BatchInst *__restrict__ insts,
+                                                             const BatchTile *__restrict__ tiles)
+{
+    const BatchTile t = tiles[blockIdx.x];
+    const BatchInst &I = insts[t.inst];
+    const unsigned N = (unsigned)I.N;
+    const unsigned node = (unsigned)t.start + threadIdx.x;
+    if (node >= N) return;
+    const uint32_t m = __ldg(I.mask + node);
+    if (!(m & FLUID_BIT)) return;
+    aa_node<ODD>(I.g, N, node, m, I);
+}
+
+// One tracer step of every tiled box in the tracer phase; with INIT (one box, the tiles of
+// `inst` in order), the start of its tracer phase.  Each tile keeps its own running sums.
+template <bool INIT>
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__restrict__ insts,
+                                                          const BatchTile *__restrict__ tiles,
+                                                          int inst, int par)
+{
+    BatchTile t;
+    if constexpr (INIT) t = BatchTile{inst, (int)blockIdx.x * BATCH_BLOCK};
+    else t = tiles[blockIdx.x];
+    const BatchInst &I = insts[t.inst];
+    const unsigned N = (unsigned)I.N;
+    const unsigned node = (unsigned)t.start + threadIdx.x;
+    double vt[3] = {0.0, 0.0, 0.0};
+    unsigned bad = 0;
+    if (node < N) {
+        const uint32_t m = __ldg(I.mask + node);
+        if (m & FLUID_BIT) {
+            if constexpr (INIT) mp_node<true>(I.V, nullptr, I.P[0], nullptr, nullptr, node, m, I, vt, bad);
+            else mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], node, m, I, vt, bad);
+        }
+    }
+    block_sum3(vt);
+    if (threadIdx.x == 0) {
+        double *acc = I.tacc + (size_t)(t.start / BATCH_BLOCK) * BATCH_TACC;
+        if constexpr (INIT) {
+            for (int d = 0; d < 3; ++d) {
+                acc[d] = vt[d] * (double)I.bw;
+                acc[3 + d] = 0.0;
+                acc[6 + d] = 0.0;
+            }
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                acc[3 + d] += vt[d];
+                acc[6 + d] = vt[d];
+            }
+        }
+    }
+    if constexpr (INIT) {
+        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status_word(I), (unsigned)LBGPU_ERR_FRACTION);
+    }
+}
+
+// V = (j + f_ext)/rho of one box from its flow state (FP64 moments rounded once to FP32).
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_v(const BatchInst *__restrict__ insts, int inst)
+{
+    const BatchInst &I = insts[inst];
+    const unsigned node = blockIdx.x * BATCH_BLOCK + threadIdx.x;
+    if (node >= (unsigned)I.N) return;
+    if (!(I.mask[node] & FLUID_BIT)) {
+        I.V[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    double rho, J[3];
+    node_moments64(I, node, rho, J[0], J[1], J[2]);
+    float o[3];
+    for (int d = 0; d < 3; ++d) o[d] = (float)((J[d] + I.tfext[d]) / rho);
+    I.V[node] = make_float4(o[0], o[1], o[2], 0.0f);
+}
+
+// One block per small box, for all the steps of a call: load, nsteps steps of the box's phase
+// in shared memory, optional convergence check (flow), store.  nsteps is even, so a flow box
+// ends in natural order and a tracer box with P(now) in P[0].
+__global__ void __launch_bounds__(BATCH_SMEM_THREADS) k_batch_smem(const BatchInst *__restrict__ insts,
+                                                                   const int *__restrict__ list,
+                                                                   int nsteps, int check,
+                                                                   unsigned *du_out)
+{
+    extern __shared__ float4 sm4[];
+    const int id = list[blockIdx.x];
+    const BatchInst &I = insts[id];
+    const unsigned N = (unsigned)I.N;
+    const unsigned T = blockDim.x;
+    if (I.phase == BATCH_FLOW) {
+        float *g = reinterpret_cast<float *>(sm4);
+        uint32_t *msk = reinterpret_cast<uint32_t *>(g + (size_t)Q * N);
+        for (unsigned i = threadIdx.x; i < (unsigned)Q * N; i += T) g[i] = I.g[i];
+        for (unsigned i = threadIdx.x; i < N; i += T) msk[i] = I.mask[i];
+        __syncthreads();
+        for (int s = 0; s < nsteps; ++s) {
+            for (unsigned node = threadIdx.x; node < N; node += T) {
+                const uint32_t m = msk[node];
+                if (!(m & FLUID_BIT)) continue;
+                if (s & 1) aa_node<true>(g, N, node, m, I);
+                else aa_node<false>(g, N, node, m, I);
+            }
+            __syncthreads();
+        }
+        if (check) {
+            float du = 0.0f;
+            for (unsigned node = threadIdx.x; node < N; node += T)
+                if (msk[node] & FLUID_BIT) du = fmaxf(du, du_and_store(I.uprev, node, node_velocity(g, N, node, I)));
+            for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
+            if ((threadIdx.x & 31) == 0) atomicMax(du_out + id, __float_as_uint(du));
+        }
+        for (unsigned i = threadIdx.x; i < (unsigned)Q * N; i += T) I.g[i] = g[i];
+        return;
+    }
+    // tracer phase
+    const int ads = I.ads;
+    float4 *V = sm4, *P0 = sm4 + N, *P1 = sm4 + 2 * (size_t)N;
+    float4 *A0 = ads ? sm4 + 3 * (size_t)N : nullptr, *A1 = ads ? sm4 + 4 * (size_t)N : nullptr;
+    uint32_t *msk = reinterpret_cast<uint32_t *>(sm4 + (size_t)(ads ? 5 : 3) * N);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (unsigned i = threadIdx.x; i < N; i += T) {
+        V[i] = I.V[i];
+        P0[i] = I.P[0][i];
+        P1[i] = zero;
+        if (ads) {
+            A0[i] = I.A[0][i];
+            A1[i] = zero;
+        }
+        msk[i] = I.mask[i];
+    }
+    __syncthreads();
+    double sum[3] = {0.0, 0.0, 0.0}, last[3] = {0.0, 0.0, 0.0};
+    unsigned bad = 0;
+    for (int s = 0; s < nsteps; ++s) {
+        const bool odd = s & 1;
+        const float4 *Pn = odd ? P1 : P0, *An = odd ? A1 : A0;
+        float4 *Px = odd ? P0 : P1, *Ax = odd ? A0 : A1;
+        double vt[3] = {0.0, 0.0, 0.0};
+        for (unsigned node = threadIdx.x; node < N; node += T) {
+            const uint32_t m = msk[node];
+            if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, node, m, I, vt, bad);
+        }
+        block_sum3(vt);  // its barriers also separate this step from the next
+        if (threadIdx.x == 0)
+            for (int d = 0; d < 3; ++d) {
+                sum[d] += vt[d];
+                last[d] = vt[d];
+            }
+    }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < N; i += T) {
+        I.P[0][i] = P0[i];
+        if (ads) I.A[0][i] = A0[i];
+    }
+    if (threadIdx.x == 0 && nsteps > 0)
+        for (int d = 0; d < 3; ++d) {
+            I.tacc[3 + d] += sum[d];
+            I.tacc[6 + d] = last[d];
+        }
+}
+
+// Convergence check of the tiled boxes (natural order): du_out[box] = max |u - u_prev|.
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_check(const BatchInst *__restrict__ insts,
+                                                             const BatchTile *__restrict__ tiles,
+                                                             unsigned *du_out)
+{
+    const BatchTile t = tiles[blockIdx.x];
+    const BatchInst &I = insts[t.inst];
+    const unsigned N = (unsigned)I.N;
+    const unsigned node = (unsigned)t.start + threadIdx.x;
+    float du = 0.0f;
+    if (node < N && (I.mask[node] & FLUID_BIT))
+        du = du_and_store(I.uprev, node, node_velocity(I.g, N, node, I));
+    for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(du_out + t.inst, __float_as_uint(du));
+}
+
+// Density and flux (FP64) of one box in natural order; solid nodes report zeros.
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_moments(const BatchInst *__restrict__ insts, int inst,
+                                                               double *rho, double *jx, double *jy,
+                                                               double *jz)
+{
+    const BatchInst &I = insts[inst];
+    const unsigned node = blockIdx.x * BATCH_BLOCK + threadIdx.x;
+    if (node >= (unsigned)I.N) return;
+    if (!(I.mask[node] & FLUID_BIT)) {
+        rho[node] = jx[node] = jy[node] = jz[node] = 0.0;
+        return;
+    }
+    node_moments64(I, node, rho[node], jx[node], jy[node], jz[node]);
+}
+
+}  // namespace
+
+cudaError_t batch_configure(int max_smem_bytes)
+{
+    return cudaFuncSetAttribute(k_batch_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
+}
+
+cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd,
+                            cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    if (odd) k_batch_aa<true><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
+    else k_batch_aa<false><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
+                            cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    k_batch_mp<false><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles, 0, par);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, int N, cudaStream_t s)
+{
+    const unsigned grid = (unsigned)((N + BATCH_BLOCK - 1) / BATCH_BLOCK);
+    k_batch_mp_v<<<grid, BATCH_BLOCK, 0, s>>>(insts, inst);
+    k_batch_mp<true><<<grid, BATCH_BLOCK, 0, s>>>(insts, nullptr, inst, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist, int nsteps,
+                              bool check, unsigned *du, int smem_bytes, int threads, cudaStream_t s)
+{
+    if (nlist <= 0) return cudaSuccess;
+    k_batch_smem<<<nlist, threads, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_check(const BatchInst *insts, const BatchTile *tiles, int ntiles,
+                               unsigned *du, cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    k_batch_check<<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles, du);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_moments(const BatchInst *insts, int inst, int N, double *rho, double *jx,
+                                 double *jy, double *jz, cudaStream_t s)
+{
+    k_batch_moments<<<(N + BATCH_BLOCK - 1) / BATCH_BLOCK, BATCH_BLOCK, 0, s>>>(insts, inst, rho, jx, jy, jz);
+    return cudaGetLastError();
+}
+
+}  // namespace lbg

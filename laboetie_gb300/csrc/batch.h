@@ -1,0 +1,68 @@
+// batch.h -- many independent boxes of uneven size stepped together (FP32 deviations).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace lbg {
+
+constexpr int BATCH_BLOCK = 256;        // threads per tile of the HBM kernels
+constexpr int BATCH_SMEM_THREADS = 512; // threads of a shared-memory-resident box
+constexpr int BATCH_SMEM_BYTES_MAX = 227 * 1024;
+constexpr int BATCH_TACC = 9;           // doubles per tile: VACF(0) part, sum over steps, last step
+
+// Shared memory a box needs while its phase runs with the whole box resident:
+// flow: 19 FP32 populations + the flag word; tracer: V, P now/next (+ A now/next) as float4
+// records + the flag word.
+__host__ __device__ constexpr int batch_smem_flow(int N) { return N * (Q * 4 + 4); }
+__host__ __device__ constexpr int batch_smem_mp(int N, int ads) { return N * (16 * (ads ? 5 : 3) + 4); }
+
+enum BatchPhase { BATCH_FLOW = 0, BATCH_MP = 1 };
+
+// Device descriptor of one box.  The collision constants follow collide32.cuh; the tracer
+// constants follow mp_f32.cu.
+struct BatchInst {
+    float *g;               // Q*N deviations, structure-of-arrays within the box
+    const uint32_t *mask;   // N node flag words
+    float4 *uprev;          // velocity at the previous convergence check
+    float4 *V;              // tracer phase: (j + f_ext)/rho per node (0 on solid nodes)
+    float4 *P[2], *A[2];    // propagated quantity / adsorbed part, by step parity
+    double *tacc;           // BATCH_TACC doubles per tile of BATCH_BLOCK nodes, then a status word
+    int lx, ly, lz, N;
+    int phase, ads;
+    float c1, c2w[3], c2a1[3], c2a2[3], c2a2cs2[3], c3a1[3];
+    float kF[9], kT[9];
+    float F[3];
+    float rho0;
+    int force;              // f_ext in moments and collisions
+    float a1[3], lwh[3], ka, kd, one_minus_kd;
+    float bw;               // 1 / (fluid + K * interfacial fluid) nodes, rounded to FP32
+    double tfext[3];        // tracer f_ext added to j in V
+};
+
+struct BatchTile {
+    int inst;   // index into the descriptor array
+    int start;  // first node of the tile
+};
+
+cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd,
+                            cudaStream_t s);
+// one tracer step of the tiled boxes: P[par] -> P[par^1]
+cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
+                            cudaStream_t s);
+// du: one word per descriptor, max |u - u_prev| of the check as IEEE bits (non-negative)
+cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist, int nsteps,
+                              bool check, unsigned *du, int smem_bytes, int threads,
+                              cudaStream_t s);
+cudaError_t launch_batch_check(const BatchInst *insts, const BatchTile *tiles, int ntiles,
+                               unsigned *du, cudaStream_t s);
+cudaError_t launch_batch_moments(const BatchInst *insts, int inst, int N, double *rho, double *jx,
+                                 double *jy, double *jz, cudaStream_t s);
+// start of the tracer phase of one box: V from the flow state, P(t=1) and VACF(0) per tile
+cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, int N, cudaStream_t s);
+cudaError_t batch_configure(int max_smem_bytes);
+
+}  // namespace lbg

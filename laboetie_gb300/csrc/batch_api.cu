@@ -1,0 +1,704 @@
+// batch_api.cu -- C ABI of batches of boxes and of the request server built on them.
+//
+// A batch owns any number of boxes (slots) of any size, each with one device allocation taken
+// from the stream-ordered pool.  Boxes can be added and removed and change phase between
+// calls; the descriptor table and the work lists are rebuilt on the next call and one call's
+// launches are replayed from a CUDA graph.  lbgpu_serve runs a request loop on a batch:
+// requests are admitted when they have arrived and their buffers fit the memory budget, stay
+// resident and are stepped together with whatever else is resident, and leave as soon as
+// their own convergence test (or step cap) and tracer steps are done -- continuous batching.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "batch.h"
+#include "ctx.h"
+#include "flow.h"
+#include "lbgpu.h"
+
+using namespace lbg;
+
+namespace {
+
+constexpr double EPS = 2.220446049250313e-16;  // epsilon(1._dp)
+constexpr size_t ALIGN = 256;
+
+struct Slot {
+    bool active = false;
+    BatchInst d{};            // device descriptor (pointers into this slot's allocation)
+    void *mem = nullptr;      // the slot's one device allocation
+    long long fluid = 0;
+    size_t bytes = 0;
+    bool smem = false;        // stepped with the whole box in shared memory
+    bool tracer = false;
+    int ntile = 0;
+    int mp_steps = 0;
+};
+
+struct GraphEntry {
+    int nsteps = 0;
+    bool check = false;
+    cudaGraphExec_t exec = nullptr;
+};
+
+size_t up(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
+
+bool tracer_ads(const lbgpu_tracer &t)
+{
+    const double K = std::fabs(t.kd) <= EPS ? 0.0 : t.ka / t.kd;
+    return std::fabs(K) > EPS;
+}
+
+// Byte layout of a slot's allocation: g, mask, uprev, nature, then the tracer buffers.
+struct Layout {
+    size_t g, mask, uprev, nature, V, P0, P1, A0, A1, tacc, total;
+};
+
+Layout layout(long long N, bool tracer, bool ads)
+{
+    Layout L{};
+    size_t o = 0;
+    L.g = o;      o += up(sizeof(float) * Q * (size_t)N);
+    L.mask = o;   o += up(sizeof(uint32_t) * (size_t)N);
+    L.uprev = o;  o += up(sizeof(float4) * (size_t)N);
+    L.nature = o; o += up((size_t)N);
+    if (tracer) {
+        const size_t f4 = up(sizeof(float4) * (size_t)N);
+        L.V = o;  o += f4;
+        L.P0 = o; o += f4;
+        L.P1 = o; o += f4;
+        if (ads) {
+            L.A0 = o; o += f4;
+            L.A1 = o; o += f4;
+        }
+        const size_t ntile = ((size_t)N + BATCH_BLOCK - 1) / BATCH_BLOCK;
+        L.tacc = o; o += up(sizeof(double) * (ntile * BATCH_TACC + 1));
+    }
+    L.total = o;
+    return L;
+}
+
+}  // namespace
+
+struct lbgpu_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr, side = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr, join = nullptr;
+    size_t budget = 0, used = 0;
+    int smem_max = BATCH_SMEM_BYTES_MAX;
+    std::vector<Slot> slots;
+    unsigned long long *d_counts = nullptr;
+    // device tables, rebuilt when the set of boxes or a phase changes
+    bool dirty = true;
+    BatchInst *d_insts = nullptr;
+    int cap_insts = 0;
+    BatchTile *d_tiles = nullptr;   // flow tiles, then tracer tiles
+    int cap_tiles = 0, nflow = 0, nmp = 0;
+    int *d_smem = nullptr;
+    int cap_smem = 0, nsmem = 0, smem_bytes = 0, smem_threads = BATCH_SMEM_THREADS;
+    unsigned *d_du = nullptr;
+    int cap_du = 0;
+    std::vector<int> desc_slot;   // descriptor index -> slot
+    std::vector<GraphEntry> graphs;
+};
+
+namespace {
+
+int bfail(int code, const std::string &msg) { return ctx_fail(nullptr, code, msg); }
+
+#define LBB_CK(call)                                                                   \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) return bfail(LBGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+int grow(T **p, int &cap, int need, cudaStream_t s)
+{
+    if (need <= cap) return LBGPU_OK;
+    int nc = std::max(need, cap * 2 + 16);
+    if (*p) LBB_CK(cudaFreeAsync(*p, s));
+    LBB_CK(cudaMallocAsync((void **)p, sizeof(T) * nc, s));
+    cap = nc;
+    return LBGPU_OK;
+}
+
+void drop_graphs(lbgpu_batch *b)
+{
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
+    b->graphs.clear();
+}
+
+void fill_consts(BatchInst &d, const lbgpu_cell &c)
+{
+    const LbConst64 K = make_const64(c.relaxation_time);
+    const double c2 = K.c2, c3 = K.c3, cs2 = 1.0 / 3.0;
+    d.c1 = (float)K.c1;
+    for (int w = 0; w < 3; ++w) {
+        d.c2w[w] = (float)(c2 * K.a0[w]);
+        d.c2a1[w] = (float)(c2 * K.a1[w]);
+        d.c2a2[w] = (float)(c2 * K.a2[w]);
+        d.c2a2cs2[w] = (float)(c2 * K.a2[w] * cs2);
+        d.c3a1[w] = (float)(c3 * K.a1[w]);
+    }
+    for (int p = 0; p < 9; ++p) {
+        const int l = pair_l(p);
+        const Vel v = vel(l);
+        const double cF = v.x * c.f_ext[0] + v.y * c.f_ext[1] + v.z * c.f_ext[2];
+        d.kF[p] = (float)(c3 * K.a1[wclass(l)] * cF);
+        d.kT[p] = (float)(c3 * K.two_a2[wclass(l)] * cF);
+    }
+    for (int q = 0; q < 3; ++q) d.F[q] = (float)c.f_ext[q];
+    d.rho0 = (float)c.rho0;
+    d.force = (c.f_ext[0] != 0.0 || c.f_ext[1] != 0.0 || c.f_ext[2] != 0.0) ? 1 : 0;
+    // tracer constants as in mp_api.cu (module_moment_propagation.f90:331-337)
+    const lbgpu_tracer &t = c.tracer;
+    const volatile double kBT = 1.0 / 3.0;
+    const double lambda = 4.0 * t.Db / kBT;
+    for (int w = 0; w < 3; ++w) {
+        d.a1[w] = (float)K.a1[w];
+        const volatile double lw = lambda * K.a0[w];
+        d.lwh[w] = (float)(lw * 0.5);
+    }
+    d.ka = (float)t.ka;
+    d.kd = (float)t.kd;
+    d.one_minus_kd = (float)(1.0 - t.kd);
+    for (int q = 0; q < 3; ++q) d.tfext[q] = t.f_ext[q];
+}
+
+int rebuild(lbgpu_batch *b)
+{
+    if (!b->dirty) return LBGPU_OK;
+    cudaStream_t s = b->stream;
+    drop_graphs(b);
+    std::vector<BatchInst> descs;
+    std::vector<BatchTile> flow, mp;
+    std::vector<int> smem;
+    b->desc_slot.clear();
+    int smem_bytes = 0;
+    for (size_t k = 0; k < b->slots.size(); ++k) {
+        const Slot &sl = b->slots[k];
+        if (!sl.active) continue;
+        const int id = (int)descs.size();
+        descs.push_back(sl.d);
+        b->desc_slot.push_back((int)k);
+        if (sl.smem) {
+            smem.push_back(id);
+            smem_bytes = std::max(smem_bytes, sl.d.phase == BATCH_FLOW ? batch_smem_flow(sl.d.N)
+                                                                       : batch_smem_mp(sl.d.N, sl.d.ads));
+        } else {
+            auto &list = sl.d.phase == BATCH_FLOW ? flow : mp;
+            for (int st = 0; st < sl.d.N; st += BATCH_BLOCK) list.push_back({id, st});
+        }
+    }
+    std::vector<BatchTile> tiles(flow);
+    tiles.insert(tiles.end(), mp.begin(), mp.end());
+    int rc;
+    if ((rc = grow(&b->d_insts, b->cap_insts, (int)descs.size(), s))) return rc;
+    if ((rc = grow(&b->d_tiles, b->cap_tiles, (int)tiles.size(), s))) return rc;
+    if ((rc = grow(&b->d_smem, b->cap_smem, (int)smem.size(), s))) return rc;
+    if ((rc = grow(&b->d_du, b->cap_du, std::max<int>((int)descs.size(), 1), s))) return rc;
+    if (!descs.empty())
+        LBB_CK(cudaMemcpyAsync(b->d_insts, descs.data(), sizeof(BatchInst) * descs.size(), cudaMemcpyHostToDevice, s));
+    if (!tiles.empty())
+        LBB_CK(cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(BatchTile) * tiles.size(), cudaMemcpyHostToDevice, s));
+    if (!smem.empty())
+        LBB_CK(cudaMemcpyAsync(b->d_smem, smem.data(), sizeof(int) * smem.size(), cudaMemcpyHostToDevice, s));
+    LBB_CK(cudaStreamSynchronize(s));  // host vectors above go out of scope
+    b->nflow = (int)flow.size();
+    b->nmp = (int)mp.size();
+    b->nsmem = (int)smem.size();
+    b->smem_bytes = smem_bytes;
+    b->dirty = false;
+    return LBGPU_OK;
+}
+
+// The launches of one call: the shared-memory boxes on the side stream, concurrently with the
+// per-step launches of the tiled boxes on the main stream.
+int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
+{
+    cudaStream_t s = b->stream;
+    if (check) LBB_CK(cudaMemsetAsync(b->d_du, 0, sizeof(unsigned) * std::max<size_t>(b->desc_slot.size(), 1), s));
+    if (b->nsmem) {
+        LBB_CK(cudaEventRecord(b->fork, s));
+        LBB_CK(cudaStreamWaitEvent(b->side, b->fork, 0));
+        LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem, nsteps, check, b->d_du, b->smem_bytes,
+                                 b->smem_threads, b->side));
+        LBB_CK(cudaEventRecord(b->join, b->side));
+    }
+    for (int t = 0; t < nsteps; ++t) {
+        LBB_CK(launch_batch_aa(b->d_insts, b->d_tiles, b->nflow, t & 1, s));
+        LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
+    }
+    if (check) LBB_CK(launch_batch_check(b->d_insts, b->d_tiles, b->nflow, b->d_du, s));
+    if (b->nsmem) LBB_CK(cudaStreamWaitEvent(s, b->join, 0));
+    return LBGPU_OK;
+}
+
+// The graph of one call (nsteps, check), captured on first use and kept until the batch's
+// tables change.
+int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
+{
+    for (auto &g : b->graphs)
+        if (g.nsteps == nsteps && g.check == check) {
+            *out = g.exec;
+            return LBGPU_OK;
+        }
+    cudaStream_t s = b->stream;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    LBB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_steps(b, nsteps, check);
+    const cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc) {
+        if (e == cudaSuccess) cudaGraphDestroy(graph);
+        return rc;
+    }
+    LBB_CK(e);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    LBB_CK(ei);
+    if (b->graphs.size() >= 4) {
+        cudaGraphExecDestroy(b->graphs.front().exec);
+        b->graphs.erase(b->graphs.begin());
+    }
+    b->graphs.push_back({nsteps, check, exec});
+    *out = exec;
+    return LBGPU_OK;
+}
+
+int run_steps(lbgpu_batch *b, int nsteps, bool check)
+{
+    cudaGraphExec_t exec = nullptr;
+    int rc = graph_of(b, nsteps, check, &exec);
+    if (rc) return rc;
+    LBB_CK(cudaGraphLaunch(exec, b->stream));
+    for (auto &sl : b->slots)
+        if (sl.active && sl.d.phase == BATCH_MP) sl.mp_steps += nsteps;
+    return LBGPU_OK;
+}
+
+int desc_of(lbgpu_batch *b, int id)
+{
+    for (size_t i = 0; i < b->desc_slot.size(); ++i)
+        if (b->desc_slot[i] == id) return (int)i;
+    return -1;
+}
+
+bool valid_slot(lbgpu_batch *b, int id)
+{
+    return b && id >= 0 && id < (int)b->slots.size() && b->slots[id].active;
+}
+
+double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t lbgpu_batch_footprint(const lbgpu_cell *c)
+{
+    if (!c || c->lx <= 0 || c->ly <= 0 || c->lz <= 0) return 0;
+    const long long N = (long long)c->lx * c->ly * c->lz;
+    const bool tracer = c->tracer.Db != 0.0;
+    return layout(N, tracer, tracer && tracer_ads(c->tracer)).total;
+}
+
+int lbgpu_batch_create(int device, size_t memory_budget, lbgpu_batch **out)
+{
+    if (!out) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_create: null argument");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return bfail(LBGPU_ERR_CUDA, "no CUDA device");
+    if (device < 0 || device >= ndev) return bfail(LBGPU_ERR_INVALID, "bad device ordinal");
+    LBB_CK(cudaSetDevice(device));
+    lbgpu_batch *b = new lbgpu_batch();
+    b->device = device;
+    size_t fr = 0, tot = 0;
+    e = cudaMemGetInfo(&fr, &tot);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_counts, 4 * sizeof(unsigned long long));
+    int optin = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e == cudaSuccess) {
+        // the shared-memory kernel also holds a small static reduction buffer
+        b->smem_max = std::min(b->smem_max, optin) - 1024;
+        e = batch_configure(b->smem_max);
+    }
+    if (e != cudaSuccess) {
+        lbgpu_batch_destroy(b);
+        return bfail(LBGPU_ERR_CUDA, std::string("lbgpu_batch_create: ") + cudaGetErrorString(e));
+    }
+    b->budget = memory_budget ? memory_budget : (size_t)(0.9 * (double)fr);
+    // LBGPU_BATCH_SMEM=0 steps every box with the tiled kernels (same per-node arithmetic)
+    const char *mode = std::getenv("LBGPU_BATCH_SMEM");
+    if (mode && std::string(mode) == "0") b->smem_max = 0;
+    *out = b;
+    return LBGPU_OK;
+}
+
+void lbgpu_batch_destroy(lbgpu_batch *b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->side) cudaStreamSynchronize(b->side);
+    drop_graphs(b);
+    for (auto &sl : b->slots)
+        if (sl.active) cudaFree(sl.mem);
+    cudaFree(b->d_insts);
+    cudaFree(b->d_tiles);
+    cudaFree(b->d_smem);
+    cudaFree(b->d_du);
+    cudaFree(b->d_counts);
+    for (cudaEvent_t ev : {b->ev0, b->ev1, b->fork, b->join})
+        if (ev) cudaEventDestroy(ev);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, int *id)
+{
+    if (!b || !c || !nature || !id) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: null argument");
+    if (c->lx <= 0 || c->ly <= 0 || c->lz <= 0) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: bad size");
+    if (!(c->relaxation_time > 0.5)) return bfail(LBGPU_ERR_INVALID, "relaxation_time must be > 0.5");
+    const lbgpu_tracer &t = c->tracer;
+    const bool tracer = t.Db != 0.0;
+    if (tracer) {   // drop_tracers.f90:88-89, module_moment_propagation.f90:41-79
+        if (!(t.Db > EPS)) return bfail(LBGPU_ERR_INVALID, "The diffusion coefficient (tracer_Db in input file) is invalid");
+        if (t.ka < -EPS) return bfail(LBGPU_ERR_INVALID, "I detected tracer%ka to be <0");
+        if (t.kd < -EPS) return bfail(LBGPU_ERR_INVALID, "I detected tracer%kd to be <0");
+        if (std::fabs(t.Ds) > EPS) return bfail(LBGPU_ERR_UNSUPPORTED, "Tracers you defined have non-zero surface diffusion coefficient");
+        if (std::fabs(t.z) > EPS) return bfail(LBGPU_ERR_UNSUPPORTED, "charged tracers are not implemented");
+    }
+    const long long N = (long long)c->lx * c->ly * c->lz;
+    if ((unsigned long long)Q * N >= (1ULL << 32)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: box too large");
+    const bool ads = tracer && tracer_ads(t);
+    const Layout L = layout(N, tracer, ads);
+    if (b->used + L.total > b->budget)
+        return bfail(LBGPU_ERR_OOM, "lbgpu_batch_add: box needs " + std::to_string(L.total >> 20) +
+                                        " MiB beyond the batch memory budget");
+    for (long long i = 0; i < N; ++i)
+        if (nature[i] != 0 && nature[i] != 1) return bfail(LBGPU_ERR_INVALID, "nature must be 0 or 1");
+    cudaStream_t s = b->stream;
+    Slot sl;
+    sl.active = true;
+    sl.bytes = L.total;
+    sl.tracer = tracer;
+    sl.ntile = (int)((N + BATCH_BLOCK - 1) / BATCH_BLOCK);
+    sl.smem = batch_smem_flow((int)N) <= b->smem_max && (!tracer || batch_smem_mp((int)N, ads) <= b->smem_max);
+    LBB_CK(cudaMallocAsync(&sl.mem, L.total, s));
+    char *base = static_cast<char *>(sl.mem);
+    BatchInst &d = sl.d;
+    std::memset(&d, 0, sizeof(d));
+    d.lx = c->lx;
+    d.ly = c->ly;
+    d.lz = c->lz;
+    d.N = (int)N;
+    d.phase = BATCH_FLOW;
+    d.ads = ads ? 1 : 0;
+    fill_consts(d, *c);
+    d.g = reinterpret_cast<float *>(base + L.g);
+    uint32_t *mask = reinterpret_cast<uint32_t *>(base + L.mask);
+    d.mask = mask;
+    d.uprev = reinterpret_cast<float4 *>(base + L.uprev);
+    int8_t *d_nature = reinterpret_cast<int8_t *>(base + L.nature);
+    if (tracer) {
+        d.V = reinterpret_cast<float4 *>(base + L.V);
+        d.P[0] = reinterpret_cast<float4 *>(base + L.P0);
+        d.P[1] = reinterpret_cast<float4 *>(base + L.P1);
+        if (ads) {
+            d.A[0] = reinterpret_cast<float4 *>(base + L.A0);
+            d.A[1] = reinterpret_cast<float4 *>(base + L.A1);
+        }
+        d.tacc = reinterpret_cast<double *>(base + L.tacc);
+    }
+    LBB_CK(cudaMemsetAsync(sl.mem, 0, L.total, s));   // rest state rho = rho0, j = 0; P = A = 0
+    LBB_CK(cudaMemcpyAsync(d_nature, nature, N, cudaMemcpyHostToDevice, s));
+    LBB_CK(launch_node_flags(d_nature, mask, c->lx, c->ly, c->lz, s));
+    LBB_CK(cudaMemsetAsync(b->d_counts, 0, 4 * sizeof(unsigned long long), s));
+    LBB_CK(launch_count_nodes(mask, N, b->d_counts, s));
+    unsigned long long counts[4];
+    LBB_CK(cudaMemcpyAsync(counts, b->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    LBB_CK(cudaStreamSynchronize(s));   // the caller may reuse nature
+    if (!counts[0]) {
+        cudaFreeAsync(sl.mem, s);
+        return bfail(LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
+    }
+    sl.fluid = (long long)counts[0];
+    if (tracer) {   // module_moment_propagation.f90:97
+        const double K = std::fabs(t.kd) <= EPS ? 0.0 : t.ka / t.kd;
+        d.bw = (float)(1.0 / ((double)counts[0] + K * (double)counts[2]));
+    }
+    int k = 0;
+    while (k < (int)b->slots.size() && b->slots[k].active) ++k;
+    if (k == (int)b->slots.size()) b->slots.push_back(sl);
+    else b->slots[k] = sl;
+    b->used += L.total;
+    b->dirty = true;
+    *id = k;
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_remove(lbgpu_batch *b, int id)
+{
+    if (!valid_slot(b, id)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_remove: no such box");
+    Slot &sl = b->slots[id];
+    LBB_CK(cudaFreeAsync(sl.mem, b->stream));
+    b->used -= sl.bytes;
+    sl = Slot();
+    b->dirty = true;
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_steps(lbgpu_batch *b, int nsteps, int check, float *du)
+{
+    if (!b || nsteps < 0 || (nsteps & 1)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_steps: nsteps must be even and >= 0");
+    int rc = rebuild(b);
+    if (rc) return rc;
+    if (b->desc_slot.empty() || nsteps == 0) return LBGPU_OK;
+    if ((rc = run_steps(b, nsteps, check != 0))) return rc;
+    if (check && du) {
+        std::vector<unsigned> h(b->desc_slot.size());
+        LBB_CK(cudaMemcpyAsync(h.data(), b->d_du, sizeof(unsigned) * h.size(), cudaMemcpyDeviceToHost, b->stream));
+        LBB_CK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < h.size(); ++i) {
+            float f;
+            std::memcpy(&f, &h[i], sizeof(f));
+            du[b->desc_slot[i]] = f;
+        }
+        return LBGPU_OK;
+    }
+    LBB_CK(cudaStreamSynchronize(b->stream));
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_time_steps(lbgpu_batch *b, int nsteps, float *ms)
+{
+    if (!b || !ms || nsteps < 0 || (nsteps & 1)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_time_steps: bad argument");
+    int rc = rebuild(b);
+    if (rc) return rc;
+    const bool work = !b->desc_slot.empty() && nsteps > 0;
+    cudaGraphExec_t exec = nullptr;
+    if (work && (rc = graph_of(b, nsteps, false, &exec))) return rc;   // outside the timed region
+    LBB_CK(cudaEventRecord(b->ev0, b->stream));
+    if (work && (rc = run_steps(b, nsteps, false))) return rc;
+    LBB_CK(cudaEventRecord(b->ev1, b->stream));
+    LBB_CK(cudaEventSynchronize(b->ev1));
+    LBB_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_moments(lbgpu_batch *b, int id, double *rho, double *jx, double *jy, double *jz)
+{
+    if (!valid_slot(b, id) || !rho || !jx || !jy || !jz)
+        return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_moments: bad argument");
+    int rc = rebuild(b);
+    if (rc) return rc;
+    const int desc = desc_of(b, id);
+    const int N = b->slots[id].d.N;
+    cudaStream_t s = b->stream;
+    double *tmp = nullptr;
+    LBB_CK(cudaMallocAsync((void **)&tmp, sizeof(double) * 4 * (size_t)N, s));
+    LBB_CK(launch_batch_moments(b->d_insts, desc, N, tmp, tmp + N, tmp + 2 * (size_t)N, tmp + 3 * (size_t)N, s));
+    double *out[4] = {rho, jx, jy, jz};
+    for (int q = 0; q < 4; ++q)
+        LBB_CK(cudaMemcpyAsync(out[q], tmp + q * (size_t)N, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    LBB_CK(cudaFreeAsync(tmp, s));
+    LBB_CK(cudaStreamSynchronize(s));
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_mp_start(lbgpu_batch *b, int id)
+{
+    if (!valid_slot(b, id)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_start: no such box");
+    Slot &sl = b->slots[id];
+    if (!sl.tracer) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_start: the box has no tracer (tracer.Db = 0)");
+    if (sl.d.phase != BATCH_FLOW) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_start: tracer phase already started");
+    int rc = rebuild(b);
+    if (rc) return rc;
+    cudaStream_t s = b->stream;
+    LBB_CK(launch_batch_mp_start(b->d_insts, desc_of(b, id), sl.d.N, s));
+    unsigned st = 0;
+    LBB_CK(cudaMemcpyAsync(&st, sl.d.tacc + (size_t)sl.ntile * BATCH_TACC, sizeof(st), cudaMemcpyDeviceToHost, s));
+    LBB_CK(cudaStreamSynchronize(s));
+    if (st & LBGPU_ERR_FRACTION)   // module_moment_propagation.f90:249-257
+        return bfail(LBGPU_ERR_FRACTION, "remaining fraction below epsilon: reduce the adsorption rate");
+    sl.d.phase = BATCH_MP;
+    sl.mp_steps = 0;
+    b->dirty = true;
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_mp_get(lbgpu_batch *b, int id, double vacf0[3], double vacf_sum[3],
+                       double vacf_last[3], int *steps)
+{
+    if (!valid_slot(b, id)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_get: no such box");
+    const Slot &sl = b->slots[id];
+    if (sl.d.phase != BATCH_MP) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_get: no tracer phase");
+    std::vector<double> h((size_t)sl.ntile * BATCH_TACC);
+    LBB_CK(cudaMemcpyAsync(h.data(), sl.d.tacc, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, b->stream));
+    LBB_CK(cudaStreamSynchronize(b->stream));
+    double *outs[3] = {vacf0, vacf_sum, vacf_last};
+    for (int q = 0; q < 3; ++q) {
+        if (!outs[q]) continue;
+        for (int d = 0; d < 3; ++d) {
+            double acc = 0.0;
+            for (int t = 0; t < sl.ntile; ++t) acc += h[(size_t)t * BATCH_TACC + 3 * q + d];
+            outs[q][d] = acc;
+        }
+    }
+    if (steps) *steps = sl.mp_steps;
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *smem_boxes,
+                     size_t *bytes_used)
+{
+    if (!b) return LBGPU_ERR_INVALID;
+    int a = 0, sm = 0;
+    long long f = 0;
+    for (auto &sl : b->slots)
+        if (sl.active) {
+            ++a;
+            f += sl.fluid;
+            sm += sl.smem;
+        }
+    if (active) *active = a;
+    if (fluid_nodes) *fluid_nodes = f;
+    if (smem_boxes) *smem_boxes = sm;
+    if (bytes_used) *bytes_used = b->used;
+    return LBGPU_OK;
+}
+
+int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *req, int n, double du_tol, int check_every,
+                lbgpu_request_result *out)
+{
+    if (!b || n < 0 || (n > 0 && (!req || !out)) || check_every <= 0 || (check_every & 1))
+        return bfail(LBGPU_ERR_INVALID, "lbgpu_serve: bad argument (check_every must be even and > 0)");
+    for (auto &sl : b->slots)
+        if (sl.active) return bfail(LBGPU_ERR_INVALID, "lbgpu_serve: the batch must be empty");
+    for (int i = 0; i < n; ++i)
+        if (req[i].mp_steps > 0 && !(req[i].cell.tracer.Db > 0.0))
+            return bfail(LBGPU_ERR_INVALID, "lbgpu_serve: tracer steps requested without a tracer");
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return req[x].arrival < req[y].arrival; });
+    for (int i = 0; i < n; ++i) {
+        std::memset(&out[i], 0, sizeof(out[i]));
+        out[i].admitted = out[i].finished = -1.0;
+    }
+    std::vector<int> slot_req;   // slot -> request index (-1 when free)
+    std::vector<int> checks(n, 0);
+    std::vector<int> phase_before;
+    std::vector<float> du;
+    const double t0 = now_s();
+    int next = 0, done = 0, rc;
+    auto finish = [&](int k, int r, double t) -> int {
+        out[r].finished = t;
+        slot_req[k] = -1;
+        ++done;
+        return lbgpu_batch_remove(b, k);
+    };
+    while (done < n) {
+        double t = now_s() - t0;
+        // admission: in arrival order, while the head request has arrived and fits
+        while (next < n && req[order[next]].arrival <= t) {
+            const int r = order[next];
+            const lbgpu_request &q = req[r];
+            const size_t need = lbgpu_batch_footprint(&q.cell);
+            if (need == 0 || need > b->budget) {   // can never fit: rejected, the queue moves on
+                out[r].status = need == 0 ? LBGPU_ERR_INVALID : LBGPU_ERR_OOM;
+                ++next;
+                ++done;
+                continue;
+            }
+            if (b->used + need > b->budget) break;
+            int id = -1;
+            rc = lbgpu_batch_add(b, &q.cell, q.nature, &id);
+            if (rc == LBGPU_ERR_INVALID || rc == LBGPU_ERR_UNSUPPORTED) {
+                out[r].status = rc;
+                ++next;
+                ++done;
+                continue;
+            }
+            if (rc) return rc;
+            if ((int)slot_req.size() <= id) slot_req.resize(id + 1, -1);
+            slot_req[id] = r;
+            out[r].admitted = now_s() - t0;
+            out[r].fluid_nodes = b->slots[id].fluid;
+            ++next;
+        }
+        bool any = false;
+        for (auto &sl : b->slots) any |= sl.active;
+        if (!any) {
+            if (next >= n) break;
+            const double wait = req[order[next]].arrival - (now_s() - t0);
+            if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.01)));
+            continue;
+        }
+        phase_before.assign(b->slots.size(), -1);
+        for (size_t k = 0; k < b->slots.size(); ++k)
+            if (b->slots[k].active) phase_before[k] = b->slots[k].d.phase;
+        du.assign(b->slots.size(), 0.0f);
+        if ((rc = lbgpu_batch_steps(b, check_every, 1, du.data()))) return rc;
+        t = now_s() - t0;
+        for (size_t k = 0; k < b->slots.size(); ++k) {
+            if (phase_before[k] < 0) continue;
+            const int r = slot_req[k];
+            const lbgpu_request &q = req[r];
+            if (phase_before[k] == BATCH_MP) {
+                const int target = (q.mp_steps + check_every - 1) / check_every * check_every;
+                if (b->slots[k].mp_steps >= target) {
+                    if ((rc = lbgpu_batch_mp_get(b, (int)k, out[r].vacf0, out[r].vacf_sum, nullptr, &out[r].mp_steps)))
+                        return rc;
+                    if ((rc = finish((int)k, r, t))) return rc;
+                }
+                continue;
+            }
+            out[r].steps += check_every;
+            checks[r] += 1;
+            const bool bad = !std::isfinite(du[k]);
+            const bool conv = checks[r] >= 2 && du[k] < du_tol;
+            const bool cap = q.max_steps > 0 && out[r].steps >= q.max_steps;
+            if (!(conv || cap || bad)) continue;
+            out[r].converged = conv ? 1 : 0;
+            if (bad) {
+                out[r].status = LBGPU_ERR_NONFINITE;
+                if ((rc = finish((int)k, r, t))) return rc;
+                continue;
+            }
+            if (q.out_density && q.out_jx && q.out_jy && q.out_jz &&
+                (rc = lbgpu_batch_moments(b, (int)k, q.out_density, q.out_jx, q.out_jy, q.out_jz)))
+                return rc;
+            if (q.mp_steps > 0) {
+                rc = lbgpu_batch_mp_start(b, (int)k);
+                if (rc == LBGPU_OK) continue;
+                if (rc != LBGPU_ERR_FRACTION) return rc;
+                out[r].status = rc;
+            }
+            if ((rc = finish((int)k, r, now_s() - t0))) return rc;
+        }
+    }
+    return LBGPU_OK;
+}
+
+}  // extern "C"

@@ -245,7 +245,13 @@ int lbgpu_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, doubl
         }
         a.err_bits = nullptr;
         a.status = nullptr;
-        LBG_CK(ctx, launch_finalize_f64(a, false, s));
+        // with a per-node force field (compensate_f_ext) the moments take the field once the
+        // force is on, as every moment evaluation of the equilibration loop does
+        const bool field = ctx->d_F[0] != nullptr && ctx->prev_force_moment;
+        a.Fx = ctx->d_F[0];
+        a.Fy = ctx->d_F[1];
+        a.Fz = ctx->d_F[2];
+        LBG_CK(ctx, launch_finalize_f64(a, field, s));
     }
     if (n) LBG_CK(ctx, cudaMemcpyAsync(n, nsrc, sizeof(double) * Q * N, cudaMemcpyDeviceToHost, s));
     if (density) LBG_CK(ctx, cudaMemcpyAsync(density, ctx->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s));

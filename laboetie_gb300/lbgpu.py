@@ -416,3 +416,194 @@ def _set_force_field(self, f):
 
 Box.compensated_force_field = _compensated_force_field
 Box.set_force_field = _set_force_field
+
+
+# ---------------------------------------------------------------- batches of boxes, serving
+
+class Cell(C.Structure):
+    """lbgpu_cell (include/lbgpu.h)."""
+    _fields_ = [
+        ("lx", C.c_int), ("ly", C.c_int), ("lz", C.c_int), ("relaxation_time", C.c_double),
+        ("f_ext", C.c_double * 3), ("rho0", C.c_double), ("tracer", Tracer),
+    ]
+
+
+class Request(C.Structure):
+    """lbgpu_request (include/lbgpu.h)."""
+    _fields_ = [
+        ("cell", Cell), ("nature", C.c_void_p), ("arrival", C.c_double), ("max_steps", C.c_int),
+        ("mp_steps", C.c_int), ("out_density", C.c_void_p), ("out_jx", C.c_void_p),
+        ("out_jy", C.c_void_p), ("out_jz", C.c_void_p),
+    ]
+
+
+class RequestResult(C.Structure):
+    """lbgpu_request_result (include/lbgpu.h)."""
+    _fields_ = [
+        ("admitted", C.c_double), ("finished", C.c_double), ("steps", C.c_int),
+        ("converged", C.c_int), ("status", C.c_int), ("mp_steps", C.c_int),
+        ("fluid_nodes", C.c_longlong), ("vacf0", C.c_double * 3), ("vacf_sum", C.c_double * 3),
+    ]
+
+
+def make_cell(shape, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0), rho0=1.0, tracer=None) -> Cell:
+    """shape = (lx, ly, lz); tracer = dict of lbgpu_tracer fields (Db, ka, kd, f_ext) or None."""
+    c = Cell()
+    c.lx, c.ly, c.lz = (int(v) for v in shape)
+    c.relaxation_time = relaxation_time
+    c.f_ext = (C.c_double * 3)(*f_ext)
+    c.rho0 = rho0
+    if tracer:
+        c.tracer = _tracer(**tracer)
+    return c
+
+
+def _batch_lib():
+    L = library()
+    vp, i, d, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    pi = C.POINTER(C.c_int)
+    for name, args, res in (
+        ("lbgpu_batch_create", [i, sz, C.POINTER(vp)], C.c_int),
+        ("lbgpu_batch_destroy", [vp], None),
+        ("lbgpu_batch_footprint", [C.POINTER(Cell)], C.c_size_t),
+        ("lbgpu_batch_add", [vp, C.POINTER(Cell), vp, pi], C.c_int),
+        ("lbgpu_batch_remove", [vp, i], C.c_int),
+        ("lbgpu_batch_steps", [vp, i, i, vp], C.c_int),
+        ("lbgpu_batch_time_steps", [vp, i, C.POINTER(C.c_float)], C.c_int),
+        ("lbgpu_batch_moments", [vp, i, vp, vp, vp, vp], C.c_int),
+        ("lbgpu_batch_mp_start", [vp, i], C.c_int),
+        ("lbgpu_batch_mp_get", [vp, i, vp, vp, vp, pi], C.c_int),
+        ("lbgpu_batch_info", [vp, pi, C.POINTER(C.c_longlong), pi, C.POINTER(C.c_size_t)], C.c_int),
+        ("lbgpu_serve", [vp, vp, i, d, i, vp], C.c_int),
+    ):
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    return L
+
+
+def footprint(cell: Cell) -> int:
+    return int(_batch_lib().lbgpu_batch_footprint(C.byref(cell)))
+
+
+class Batch:
+    """Many independent boxes stepped together (lbgpu_batch_*).  Boxes are identified by the
+    slot id add() returns; moments are (rho, (jx, jy, jz)) arrays of shape (lz, ly, lx)."""
+
+    def __init__(self, memory_budget=0, device=0):
+        self.L = _batch_lib()
+        self.b = C.c_void_p()
+        self._natures = {}
+        self._shapes = {}
+        self._chk(self.L.lbgpu_batch_create(device, memory_budget, C.byref(self.b)), "batch_create")
+
+    def _chk(self, rc, what=""):
+        if rc != 0:
+            buf = C.create_string_buffer(1024)
+            self.L.lbgpu_last_error(None, buf, len(buf))
+            raise LbgpuError(rc, f"{what}: {buf.value.decode(errors='replace')}")
+
+    def close(self):
+        if getattr(self, "b", None) and self.b.value:
+            self.L.lbgpu_batch_destroy(self.b)
+            self.b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add(self, nature, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0), rho0=1.0, tracer=None) -> int:
+        nat = np.ascontiguousarray(nature, dtype=np.int8)
+        lz, ly, lx = nat.shape
+        cell = make_cell((lx, ly, lz), relaxation_time, f_ext, rho0, tracer)
+        i = C.c_int(-1)
+        self._chk(self.L.lbgpu_batch_add(self.b, C.byref(cell), _ptr(nat), C.byref(i)), "batch_add")
+        self._shapes[i.value] = nat.shape
+        return i.value
+
+    def remove(self, box: int):
+        self._chk(self.L.lbgpu_batch_remove(self.b, box), "batch_remove")
+        self._shapes.pop(box, None)
+
+    def steps(self, nsteps: int, check=False):
+        """nsteps (even) steps of every box; with check, {slot: max|u - u_prev|} of the flow boxes."""
+        n = max(self._shapes) + 1 if self._shapes else 1
+        du = np.zeros(n, dtype=np.float32)
+        self._chk(self.L.lbgpu_batch_steps(self.b, nsteps, 1 if check else 0,
+                                           _ptr(du) if check else None), "batch_steps")
+        return {k: float(du[k]) for k in self._shapes} if check else None
+
+    def time_steps(self, nsteps: int) -> float:
+        ms = C.c_float(0)
+        self._chk(self.L.lbgpu_batch_time_steps(self.b, nsteps, C.byref(ms)), "batch_time_steps")
+        return ms.value
+
+    def moments(self, box: int):
+        shape = self._shapes[box]
+        out = [np.zeros(shape) for _ in range(4)]
+        self._chk(self.L.lbgpu_batch_moments(self.b, box, *(_ptr(x) for x in out)), "batch_moments")
+        return out[0], tuple(out[1:])
+
+    def mp_start(self, box: int):
+        self._chk(self.L.lbgpu_batch_mp_start(self.b, box), "batch_mp_start")
+
+    def mp_get(self, box: int):
+        """(vacf0, vacf_sum, vacf_last, steps); D_eff = vacf0/2 + vacf_sum."""
+        v = [np.zeros(3) for _ in range(3)]
+        st = C.c_int(0)
+        self._chk(self.L.lbgpu_batch_mp_get(self.b, box, *(_ptr(x) for x in v), C.byref(st)),
+                  "batch_mp_get")
+        return v[0], v[1], v[2], st.value
+
+    def info(self):
+        a, sm = C.c_int(0), C.c_int(0)
+        f = C.c_longlong(0)
+        by = C.c_size_t(0)
+        self._chk(self.L.lbgpu_batch_info(self.b, C.byref(a), C.byref(f), C.byref(sm), C.byref(by)),
+                  "batch_info")
+        return dict(active=a.value, fluid_nodes=f.value, smem_boxes=sm.value, bytes=by.value)
+
+    def serve(self, requests, du_tol=1e-8, check_every=100):
+        """requests: list of dicts {nature, arrival, max_steps, mp_steps, relaxation_time, f_ext,
+        rho0, tracer, moments (bool)}.  Returns a list of result dicts (times in seconds after
+        the start), with 'moments' = (rho, (jx, jy, jz)) where asked for."""
+        n = len(requests)
+        reqs = (Request * max(n, 1))()
+        keep = []
+        outs = []
+        for k, r in enumerate(requests):
+            nat = np.ascontiguousarray(r["nature"], dtype=np.int8)
+            keep.append(nat)
+            lz, ly, lx = nat.shape
+            q = reqs[k]
+            q.cell = make_cell((lx, ly, lz), r.get("relaxation_time", 1.0), r.get("f_ext", (0.0, 0.0, 0.0)),
+                               r.get("rho0", 1.0), r.get("tracer"))
+            q.nature = _ptr(nat)
+            q.arrival = float(r.get("arrival", 0.0))
+            q.max_steps = int(r.get("max_steps", 0))
+            q.mp_steps = int(r.get("mp_steps", 0))
+            m = None
+            if r.get("moments"):
+                m = [np.zeros(nat.shape) for _ in range(4)]
+                q.out_density, q.out_jx, q.out_jy, q.out_jz = (_ptr(x) for x in m)
+            outs.append(m)
+        res = (RequestResult * max(n, 1))()
+        self._chk(self.L.lbgpu_serve(self.b, reqs, n, du_tol, check_every, res), "serve")
+        out = []
+        for k in range(n):
+            x = res[k]
+            d = dict(admitted=x.admitted, finished=x.finished, steps=x.steps, converged=bool(x.converged),
+                     status=x.status, mp_steps=x.mp_steps, fluid_nodes=x.fluid_nodes,
+                     vacf0=np.array(list(x.vacf0)), vacf_sum=np.array(list(x.vacf_sum)))
+            if outs[k] is not None:
+                d["moments"] = (outs[k][0], tuple(outs[k][1:]))
+            out.append(d)
+        return out

@@ -70,3 +70,35 @@ def test_no_gpu_means_a_loud_failure_not_a_cpu_fallback():
     with pytest.raises(LbgpuError) as e:
         Box(np.zeros((4, 4, 4), dtype=np.int8))
     assert e.value.status & 2  # LBGPU_ERR_CUDA
+
+
+def test_batch_footprint_and_struct_layout():
+    """lbgpu_batch_footprint is host logic: populations, flags, previous velocity and the
+    nature byte per node (256-byte aligned parts), plus the tracer buffers when Db > 0 (two more
+    float4 records per node with adsorption)."""
+    from laboetie_gb300.lbgpu import Cell, Request, RequestResult, footprint, make_cell
+
+    assert (ctypes.sizeof(Cell), ctypes.sizeof(Request), ctypes.sizeof(RequestResult)) == (144, 200, 88)
+    up = lambda x: (x + 255) // 256 * 256
+    N = 1 * 50 * 50
+    base = up(76 * N) + up(4 * N) + up(16 * N) + up(N)
+    assert footprint(make_cell((1, 50, 50))) == base
+    tiles = (N + 255) // 256
+    mp = 3 * up(16 * N) + up(8 * (9 * tiles + 1))
+    assert footprint(make_cell((1, 50, 50), tracer=dict(Db=0.01))) == base + mp
+    ads = footprint(make_cell((1, 50, 50), tracer=dict(Db=0.01, ka=0.02, kd=0.01)))
+    assert ads == base + mp + 2 * up(16 * N)
+    assert footprint(make_cell((0, 4, 4))) == 0
+
+
+def test_batch_without_gpu_fails_loudly():
+    import subprocess
+
+    from laboetie_gb300.lbgpu import Batch
+
+    has_gpu = subprocess.run(["sh", "-c", "nvidia-smi -L"], capture_output=True).returncode == 0
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(LbgpuError) as e:
+        Batch()
+    assert e.value.status & 2  # LBGPU_ERR_CUDA
