@@ -427,7 +427,7 @@ def main():
     mlups64 = world * nfluid * K64 / (ms64 * 1e-3) / 1e6
     achieved32 = BYTES_F32 * nfluid / (ms_step32 * 1e-3) / 1e9
     achieved64 = BYTES_F64 * nfluid / (ms_step64 * 1e-3) / 1e9
-    tr = ncu_traffic("flow_aa_f32_porous128.md")
+    tr = ncu_traffic("flow_aa_f32_porous192.md")
     h2d = (19 + 4) * 8 * nature.size
     d2h = 4 * 8 * nature.size
     line = {

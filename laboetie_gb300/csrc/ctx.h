@@ -66,6 +66,16 @@ struct lbgpu_ctx {
     bool aa = true;
     int aa_phase = 0;            // parity of the next AA launch (1: buffer holds swapped f*)
     int aa_minb[2] = {4, 4};     // AA kernel variants for even / odd launches
+    bool aa_minb_fixed = false;  // set by LBGPU_AA_MINB
+    bool aa_tuned = false;
+    // AA layout: only the Nf fluid nodes are stored, in lattice order (compact index i);
+    // cpos[i] = x | y << xbits | z << (xbits + ybits), cmask[i] = flag word,
+    // rowtab[row*nw + w] = {fluid bits of word w of lattice row y + ly*z, compact index of the
+    // first fluid node of that word}
+    unsigned Nf = 0;
+    int nw = 0, xbits = 0, ybits = 0;
+    uint32_t *d_cpos = nullptr, *d_cmask = nullptr;
+    uint2 *d_rowtab = nullptr;
 
     // cached CUDA graphs of the step loop
     cudaGraphExec_t graph_ref = nullptr;

@@ -51,6 +51,12 @@ struct FlowArgs32 {
     double rho0d;
     double w64[3];
     int minb_even, minb_odd;     // AA kernel variants (resident blocks per SM)
+    // AA layout over the fluid nodes only (ctx.h): g0 holds Q*Nf deviations
+    unsigned Nf;
+    int nw;
+    const uint32_t *cpos, *cmask;
+    const uint2 *rowtab;
+    int xbits, ybits;            // cpos = x | y << xbits | z << (xbits + ybits)
 };
 
 // FP64 strict ---------------------------------------------------------------------------
@@ -72,6 +78,10 @@ cudaError_t launch_init_f64(const FlowArgs64 &a, double rho0, cudaStream_t s);
 // FP32 deviation ------------------------------------------------------------------------
 cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_init_f32(const FlowArgs32 &a, cudaStream_t s);
+// AA layout: flag word of every compact node
+cudaError_t launch_compact_mask(const FlowArgs32 &a, uint32_t *cmask, cudaStream_t s);
+// AA layout: d[l*Nf + i] = n[l*N + lattice index of i] - w_l rho0
+cudaError_t launch_to_dev_compact32(const FlowArgs32 &a, const double *n, float *out, cudaStream_t s);
 cudaError_t launch_finalize_f32(const FlowArgs32 &a, bool pull, cudaStream_t s);
 cudaError_t launch_collide_f32(const FlowArgs32 &a, cudaStream_t s);
 cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s);

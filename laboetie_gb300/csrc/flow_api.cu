@@ -35,6 +35,67 @@ void free_op(lbgpu_ctx *ctx)
     ctx->op = nullptr;
 }
 
+// AA layout over the fluid nodes (ctx.h): compact index in lattice order, packed positions and
+// row bitmask table built on the host from nature; flag words gathered on the device.
+int build_compact_layout(lbgpu_ctx *ctx, const int8_t *nature)
+{
+    const int lx = ctx->p.lx, ly = ctx->p.ly, lz = ctx->p.lz, rows = ly * lz;
+    const int nw = (lx + 31) / 32;
+    auto bits = [](int n) {
+        int b = 1;
+        while ((1 << b) < n) ++b;
+        return b;
+    };
+    const int xbits = bits(lx), ybits = bits(ly), zbits = bits(lz);
+    if (xbits + ybits + zbits > 32 || (unsigned long long)rows * nw >= (1ULL << 32))
+        return ctx_fail(ctx, LBGPU_ERR_INVALID,
+                        "FP32 in-place streaming: box shape beyond the packed-position limits "
+                        "(use LBGPU_FP32_STREAMING=ab)");
+    std::vector<uint2> tab((size_t)rows * nw);
+    std::vector<uint32_t> pos;
+    pos.reserve((size_t)ctx->counts[0]);
+    uint32_t c = 0;
+    for (int z = 0; z < lz; ++z)
+        for (int y = 0; y < ly; ++y) {
+            const size_t r = (size_t)y + (size_t)ly * z;
+            for (int w = 0; w < nw; ++w) {
+                uint32_t bm = 0;
+                const uint32_t base = c;
+                for (int b = 0; b < 32; ++b) {
+                    const int x = w * 32 + b;
+                    if (x < lx && nature[r * lx + x] == 0) {
+                        bm |= 1u << b;
+                        pos.push_back((uint32_t)x | ((uint32_t)y << xbits) | ((uint32_t)z << (xbits + ybits)));
+                        ++c;
+                    }
+                }
+                tab[r * nw + w] = make_uint2(bm, base);
+            }
+        }
+    ctx->Nf = c;
+    ctx->nw = nw;
+    ctx->xbits = xbits;
+    ctx->ybits = ybits;
+    cudaStream_t s = ctx->stream;
+    LBG_CK(ctx, dalloc(&ctx->d_rowtab, tab.size()));
+    LBG_CK(ctx, dalloc(&ctx->d_cpos, pos.size()));
+    LBG_CK(ctx, dalloc(&ctx->d_cmask, pos.size()));
+    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_rowtab, tab.data(), sizeof(uint2) * tab.size(), cudaMemcpyHostToDevice, s));
+    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_cpos, pos.data(), sizeof(uint32_t) * pos.size(), cudaMemcpyHostToDevice, s));
+    FlowArgs32 a;
+    std::memset(&a, 0, sizeof(a));
+    a.mask = ctx->d_mask;
+    a.Nf = c;
+    a.cpos = ctx->d_cpos;
+    a.lx = lx;
+    a.ly = ly;
+    a.xbits = xbits;
+    a.ybits = ybits;
+    LBG_CK(ctx, launch_compact_mask(a, ctx->d_cmask, s));
+    LBG_CK(ctx, cudaStreamSynchronize(s));   // host tables go out of scope
+    return LBGPU_OK;
+}
+
 }  // namespace
 
 int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
@@ -71,18 +132,25 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     } else {
         const char *mode = std::getenv("LBGPU_FP32_STREAMING");
         ctx->aa = !(mode && std::string(mode) == "ab");
-        if (ctx->aa && (unsigned long long)Q * N >= (1ULL << 32))
+        if (ctx->aa && (unsigned long long)Q * ctx->counts[0] >= (1ULL << 32))
             return ctx_fail(ctx, LBGPU_ERR_INVALID,
-                            "FP32 in-place streaming addresses 19*N populations with 32-bit "
+                            "FP32 in-place streaming addresses 19*Nf populations with 32-bit "
                             "indices: box too large (use LBGPU_FP32_STREAMING=ab)");
         if (const char *e = std::getenv("LBGPU_AA_MINB")) {  // "<even>,<odd>", e.g. "4,3"
             int ev = 0, od = 0;
             if (std::sscanf(e, "%d,%d", &ev, &od) == 2) {
                 ctx->aa_minb[0] = ev;
                 ctx->aa_minb[1] = od;
+                ctx->aa_minb_fixed = true;
             }
         }
-        for (int b = 0; b < (ctx->aa ? 1 : 2); ++b) LBG_CK(ctx, dalloc(&ctx->d_g[b], (size_t)Q * N));
+        if (ctx->aa) {
+            int rc = build_compact_layout(ctx, nature);
+            if (rc) return rc;
+            LBG_CK(ctx, dalloc(&ctx->d_g[0], (size_t)Q * ctx->Nf));
+        } else {
+            for (int b = 0; b < 2; ++b) LBG_CK(ctx, dalloc(&ctx->d_g[b], (size_t)Q * N));
+        }
     }
     for (int d = 0; d < 3; ++d) LBG_CK(ctx, dalloc(&ctx->d_j[d], N));
     LBG_CK(ctx, dalloc(&ctx->d_rho, N));
@@ -103,6 +171,9 @@ void ctx_release_device(lbgpu_ctx *ctx)
         if (ctx->graph_fixed[f]) cudaGraphExecDestroy(ctx->graph_fixed[f]);
     cudaFree(ctx->d_nature);
     cudaFree(ctx->d_mask);
+    cudaFree(ctx->d_cpos);
+    cudaFree(ctx->d_cmask);
+    cudaFree(ctx->d_rowtab);
     for (int b = 0; b < 2; ++b) {
         cudaFree(ctx->d_f[b]);
         cudaFree(ctx->d_g[b]);

@@ -10,6 +10,7 @@
 // which is module_collision.f90:87-104 with the a2 double sum written as a contraction.
 // Storing deviations keeps the ~7 significant digits of FP32 for the flow signal rather than
 // for the rest density.  Moments handed back to the host are accumulated in FP64.
+#include <algorithm>
 #include <cfloat>
 
 #include "collide32.cuh"
@@ -37,6 +38,79 @@ __device__ __forceinline__ Coords32 coords32(unsigned node, int lx, int ly, int 
     k.Y[0] = wrap_plus(y, ly) * sy;  k.Y[1] = y * sy;  k.Y[2] = wrap_minus(y, ly) * sy;
     k.Z[0] = wrap_plus(z, lz) * sz;  k.Z[1] = z * sz;  k.Z[2] = wrap_minus(z, lz) * sz;
     return k;
+}
+
+// AA layout over the fluid nodes: compact index of the fluid node x of the lattice row whose
+// table entries start at rb, from the row's fluid bitmask word and the compact index of its
+// first fluid node.
+__device__ __forceinline__ unsigned compact_in_row(const uint2 *__restrict__ rowtab, unsigned rb, int x)
+{
+    const uint2 e = __ldg(rowtab + rb + (x >> 5));
+    return e.y + (unsigned)__popc(e.x & ((1u << (x & 31)) - 1u));
+}
+
+// Compact node position: x | y << xbits | z << (xbits + ybits) (no division to decode).
+__device__ __forceinline__ unsigned lattice_of(const FlowArgs32 &a, unsigned c)
+{
+    const unsigned x = c & ((1u << a.xbits) - 1u);
+    const unsigned y = (c >> a.xbits) & ((1u << a.ybits) - 1u);
+    const unsigned z = c >> (a.xbits + a.ybits);
+    return x + (unsigned)a.lx * (y + (unsigned)a.ly * z);
+}
+
+// Element index of the slot read for each direction by the gather of an odd AA launch at the
+// compact node i (packed position c, flag word m): slot l of the node itself across a bounce-back
+// link, else slot inv(l) of the fluid node x - c_l.  f(l, o) is called for every l.
+// Within a lattice row the fluid nodes are consecutive compact indices, so one table lookup per
+// neighbouring row gives cnt = the compact index the node x would have in that row (fluid nodes
+// before x); its neighbours x -+ 1 in the row are then cnt - 1 and cnt + fluid(x) (x - 1 and
+// x + 1 fluid), and the node's own row needs no lookup (cnt = i).  Only a wrap across the
+// periodic x boundary takes a second lookup.
+template <typename Fn>
+__device__ __forceinline__ void aa_gather_offsets(const FlowArgs32 &a, unsigned i, unsigned c,
+                                                  uint32_t m, Fn &&f)
+{
+    const int lx = a.lx, ly = a.ly, lz = a.lz, nw = a.nw;
+    const int x = (int)(c & ((1u << a.xbits) - 1u));
+    const int y = (int)((c >> a.xbits) & ((1u << a.ybits) - 1u));
+    const int z = (int)(c >> (a.xbits + a.ybits));
+    const unsigned row = (unsigned)(y + ly * z);
+    // [c+1] = row coordinate of (y - c), (z - c)
+    const int R[3] = {wrap_plus(y, ly), y, wrap_minus(y, ly)};
+    const int Z[3] = {wrap_plus(z, lz) * ly, z * ly, wrap_minus(z, lz) * ly};
+    const unsigned Nf = a.Nf;
+    const int w = x >> 5, b = x & 31;
+    const uint32_t below = (1u << b) - 1u;
+    const uint2 *__restrict__ tab = a.rowtab;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel v = vel(l);
+        if constexpr (l == 0) {
+            f(0, i);
+        } else {
+            unsigned o;
+            if ((m >> l) & 1u) {
+                o = (unsigned)l * Nf + i;
+            } else {
+                unsigned s;
+                if constexpr (v.y == 0 && v.z == 0) {
+                    // own row: the fluid neighbour x - c.x is the previous / next compact node
+                    const unsigned rb = row * (unsigned)nw;
+                    if constexpr (v.x > 0) s = x > 0 ? i - 1u : compact_in_row(tab, rb, lx - 1);
+                    else s = x < lx - 1 ? i + 1u : compact_in_row(tab, rb, 0);
+                } else {
+                    const unsigned rb = (unsigned)(R[v.y + 1] + Z[v.z + 1]) * (unsigned)nw;
+                    const uint2 e = __ldg(tab + rb + w);
+                    const unsigned cnt = e.y + (unsigned)__popc(e.x & below);
+                    if constexpr (v.x == 0) s = cnt;
+                    else if constexpr (v.x > 0) s = x > 0 ? cnt - 1u : compact_in_row(tab, rb, lx - 1);
+                    else s = x < lx - 1 ? cnt + ((e.x >> b) & 1u) : compact_in_row(tab, rb, 0);
+                }
+                o = (unsigned)inv(l) * Nf + s;
+            }
+            f(l, o);
+        }
+    });
 }
 
 __device__ __forceinline__ void pull19f(float (&g)[Q], const float *__restrict__ src,
@@ -106,41 +180,29 @@ __global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
 // odd launch the buffer holds the streamed populations in natural order again.
 // Halfway bounce-back (equilibration.f90:204-243): a population whose source (or destination)
 // across link l is of the other nature is read from (written to) the node itself.
-template <bool ODD, int FMASK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
+// Only fluid nodes are stored (compact index i in lattice order), so the even launch reads and
+// writes 19 dense arrays with no solid node in any sector, and the odd launch finds a fluid
+// neighbour's slot through the row bitmask table.
+// One AA update of the compact node i; odd launches take its flag word m and lattice index p.
+template <bool ODD, int FMASK>
+__device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint32_t m, unsigned p,
+                                          unsigned (*soff)[BLOCK])
 {
-    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
-    if (node >= (unsigned)a.N) return;
-    const uint32_t m = __ldg(a.mask + node);
-    if (!(m & FLUID_BIT)) return;
     // Each thread writes only the slots it has read, and every value it writes depends on all
     // of them: no store can overtake a load, so the two views of the buffer may be restricted.
     const float *__restrict__ gin = a.g0;
     float *__restrict__ gout = a.g0;
-    const unsigned N = (unsigned)a.N;  // 19*N < 2^32 is checked when the context is created
+    const unsigned Nf = a.Nf;  // 19*Nf < 2^32 is checked when the context is created
     float f[Q];
-    // odd launches: element index of the slot read for direction l, parked in shared memory
-    // ([l][thread], conflict-free) so that it does not occupy registers across the collision
-    __shared__ unsigned soff[ODD ? Q : 1][BLOCK];
     if constexpr (ODD) {
-        const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
-        static_for<0, Q>([&](auto L) {
-            constexpr int l = decltype(L)::value;
-            constexpr Vel c = vel(l);
-            unsigned o;
-            if constexpr (l == 0) {
-                o = node;
-            } else {
-                const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);  // node - c_l
-                o = ((m >> l) & 1u) ? (unsigned)l * N + node : (unsigned)inv(l) * N + s;
-            }
+        aa_gather_offsets(a, i, p, m, [&](int l, unsigned o) {
             soff[l][threadIdx.x] = o;
             f[l] = __ldg(gin + o);
         });
     } else {
-        const float *p = gin + node;
+        const float *q = gin + i;
 #pragma unroll
-        for (int l = 0; l < Q; ++l, p += N) f[l] = __ldg(p);
+        for (int l = 0; l < Q; ++l, q += Nf) f[l] = __ldg(q);
     }
     float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
     static_for<0, Q>([&](auto L) {
@@ -165,10 +227,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
 #pragma unroll
         for (int l = 0; l < Q; ++l) gout[soff[inv(l)][threadIdx.x]] = f[l];
     } else {
-        float *p = gout + node;
+        float *q = gout + i;
 #pragma unroll
-        for (int l = 0; l < Q; ++l, p += N) *p = f[inv(l)];
+        for (int l = 0; l < Q; ++l, q += Nf) *q = f[inv(l)];
     }
+}
+
+// One compact node per thread (the odd launches' gather chain position -> neighbour index ->
+// gather is covered by occupancy: the tuner in flow_f32_api.cu picks the launch bounds).
+template <bool ODD, int FMASK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
+{
+    // odd launches: element index of the slot read for direction l, parked in shared memory
+    // ([l][thread], conflict-free) so that it does not occupy registers across the collision
+    __shared__ unsigned soff[ODD ? Q : 1][BLOCK];
+    const unsigned i = blockIdx.x * BLOCK + threadIdx.x;   // compact (fluid) node
+    if (i >= a.Nf) return;
+    if constexpr (!ODD) aa_update<false, FMASK>(a, i, 0u, 0u, soff);
+    else aa_update<true, FMASK>(a, i, __ldg(a.cmask + i), __ldg(a.cpos + i), soff);
 }
 
 // Moments (FP64) of an AA buffer: natural order after an odd launch (SWAPPED = false), or
@@ -177,36 +253,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
 template <bool SWAPPED>
 __global__ void __launch_bounds__(BLOCK) k_aa_finalize32(const FlowArgs32 a)
 {
-    const unsigned node = blockIdx.x * BLOCK + threadIdx.x;
-    if (node >= (unsigned)a.N) return;
-    const uint32_t m = a.mask[node];
+    // solid nodes: the outputs were zeroed by the host (the reference's zeros)
+    const unsigned i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= a.Nf) return;
+    const unsigned c = a.cpos[i];
+    const unsigned p = lattice_of(a, c);
     const size_t N = (size_t)a.N;
-    if (!(m & FLUID_BIT)) {
-        a.rho[node] = 0.0;
-        a.jx[node] = 0.0;
-        a.jy[node] = 0.0;
-        a.jz[node] = 0.0;
-        if (a.nout)
-            for (int l = 0; l < Q; ++l) a.nout[(size_t)l * N + node] = 0.0;
-        return;
-    }
     const float *g = a.g0;
     float f[Q];
     if constexpr (SWAPPED) {
-        const Coords32 k = coords32(node, a.lx, a.ly, a.lz);
-        static_for<0, Q>([&](auto L) {
-            constexpr int l = decltype(L)::value;
-            constexpr Vel c = vel(l);
-            if constexpr (l == 0) {
-                f[0] = g[node];
-            } else {
-                const unsigned s = (unsigned)(k.X[c.x + 1] + k.Y[c.y + 1] + k.Z[c.z + 1]);
-                f[l] = ((m >> l) & 1u) ? g[(size_t)l * N + node] : g[(size_t)inv(l) * N + s];
-            }
-        });
+        aa_gather_offsets(a, i, c, a.cmask[i], [&](int l, unsigned o) { f[l] = g[o]; });
     } else {
 #pragma unroll
-        for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * N + node];
+        for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * a.Nf + i];
     }
     double drho = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
     static_for<0, Q>([&](auto L) {
@@ -217,24 +276,43 @@ __global__ void __launch_bounds__(BLOCK) k_aa_finalize32(const FlowArgs32 a)
         jx += c.x * v;
         jy += c.y * v;
         jz += c.z * v;
-        if (a.nout) a.nout[(size_t)l * N + node] = v + a.w64[wclass(l)] * a.rho0d;
+        if (a.nout) a.nout[(size_t)l * N + p] = v + a.w64[wclass(l)] * a.rho0d;
     });
     if (a.force_moment) {
         jx += 0.5 * (double)a.F[0];
         jy += 0.5 * (double)a.F[1];
         jz += 0.5 * (double)a.F[2];
     }
-    a.rho[node] = a.rho0d + drho;
-    a.jx[node] = jx;
-    a.jy[node] = jy;
-    a.jz[node] = jz;
+    a.rho[p] = a.rho0d + drho;
+    a.jx[p] = jx;
+    a.jy[p] = jy;
+    a.jz[p] = jz;
+}
+
+// cmask[i] = flag word of the compact node i
+__global__ void __launch_bounds__(BLOCK) k_compact_mask(const FlowArgs32 a, uint32_t *cmask)
+{
+    const unsigned i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i < a.Nf) cmask[i] = a.mask[lattice_of(a, a.cpos[i])];
+}
+
+// d_l = n_l - w_l rho0 at the fluid nodes, into the AA layout
+__global__ void __launch_bounds__(BLOCK) k_to_dev_compact32(const FlowArgs32 a, const double *__restrict__ n,
+                                                            float *__restrict__ out)
+{
+    const size_t t = (size_t)blockIdx.x * BLOCK + threadIdx.x;
+    const size_t Nf = a.Nf;
+    if (t >= (size_t)Q * Nf) return;
+    const int l = (int)(t / Nf);
+    const unsigned i = (unsigned)(t - (size_t)l * Nf);
+    out[t] = (float)(n[(size_t)l * (size_t)a.N + lattice_of(a, a.cpos[i])] - a.w64[wclass(l)] * a.rho0d);
 }
 
 // Zero deviations: the rest state rho = rho0, j = 0 (init_simu.f90:283-291 on fluid nodes).
 __global__ void __launch_bounds__(BLOCK) k_init32(const FlowArgs32 a)
 {
     const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;
-    const size_t total = (size_t)Q * (size_t)a.N;
+    const size_t total = (size_t)Q * (a.g1 ? (size_t)a.N : (size_t)a.Nf);  // A/B or AA layout
     if (i < total) {
         a.g0[i] = 0.0f;
         if (a.g1) a.g1[i] = 0.0f;
@@ -350,8 +428,8 @@ cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_
     return cudaGetLastError();
 }
 
-// minb: resident blocks per SM the kernel is compiled for (2, 3 or 4 -> up to 128, 85 or 64
-// registers per thread); picked per device by the tuner in flow_f32_api.cu.
+// minb: resident blocks per SM the kernel is compiled for (3, 4, 5 or 6 -> at most 85, 64, 51
+// or 42 registers per thread); picked per box by the tuner in flow_f32_api.cu.
 template <int FM, int MINB>
 static void aa_launch(const FlowArgs32 &a, bool odd, unsigned grid, cudaStream_t s)
 {
@@ -362,23 +440,37 @@ static void aa_launch(const FlowArgs32 &a, bool odd, unsigned grid, cudaStream_t
 template <int FM>
 static void aa_launch_minb(const FlowArgs32 &a, bool odd, int minb, unsigned grid, cudaStream_t s)
 {
-    if (minb <= 2) aa_launch<FM, 2>(a, odd, grid, s);
-    else if (minb == 3) aa_launch<FM, 3>(a, odd, grid, s);
-    else aa_launch<FM, 4>(a, odd, grid, s);
+    if (minb <= 3) aa_launch<FM, 3>(a, odd, grid, s);
+    else if (minb == 4) aa_launch<FM, 4>(a, odd, grid, s);
+    else if (minb == 5) aa_launch<FM, 5>(a, odd, grid, s);
+    else aa_launch<FM, 6>(a, odd, grid, s);
 }
 
 cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    const unsigned grid = (a.Nf + BLOCK - 1) / BLOCK;
     // one instantiation: with the force switched off (force_collide = 0) the force terms are
     // skipped at run time
     aa_launch_minb<7>(a, odd, odd ? a.minb_odd : a.minb_even, grid, s);
     return cudaGetLastError();
 }
 
+cudaError_t launch_compact_mask(const FlowArgs32 &a, uint32_t *cmask, cudaStream_t s)
+{
+    k_compact_mask<<<(a.Nf + BLOCK - 1) / BLOCK, BLOCK, 0, s>>>(a, cmask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_dev_compact32(const FlowArgs32 &a, const double *n, float *out, cudaStream_t s)
+{
+    const size_t total = (size_t)Q * a.Nf;
+    k_to_dev_compact32<<<(unsigned)((total + BLOCK - 1) / BLOCK), BLOCK, 0, s>>>(a, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((a.N + BLOCK - 1) / BLOCK);
+    const unsigned grid = (a.Nf + BLOCK - 1) / BLOCK;
     if (swapped) k_aa_finalize32<true><<<grid, BLOCK, 0, s>>>(a);
     else k_aa_finalize32<false><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
@@ -386,7 +478,7 @@ cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream
 
 cudaError_t launch_init_f32(const FlowArgs32 &a, cudaStream_t s)
 {
-    const size_t total = (size_t)Q * (size_t)a.N;
+    const size_t total = (size_t)Q * (a.g1 ? (size_t)a.N : (size_t)a.Nf);
     k_init32<<<(unsigned)((total + BLOCK - 1) / BLOCK), BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }

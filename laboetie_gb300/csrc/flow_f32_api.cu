@@ -40,6 +40,13 @@ static void fill_args32(lbgpu_ctx *ctx, FlowArgs32 &a)
     for (int d = 0; d < 3; ++d) a.F[d] = (float)ctx->p.f_ext[d];
     a.minb_even = ctx->aa_minb[0];
     a.minb_odd = ctx->aa_minb[1];
+    a.Nf = ctx->Nf;
+    a.nw = ctx->nw;
+    a.cpos = ctx->d_cpos;
+    a.cmask = ctx->d_cmask;
+    a.rowtab = ctx->d_rowtab;
+    a.xbits = ctx->xbits;
+    a.ybits = ctx->ybits;
     const double c2 = K.c2, c3 = K.c3, cs2 = 1.0 / 3.0;
     for (int w = 0; w < 3; ++w) {
         a.c2w[w] = (float)(c2 * K.a0[w]);
@@ -81,7 +88,8 @@ int f32_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const d
     double *tmp = nullptr;
     LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
     LBG_CK(ctx, cudaMemcpyAsync(tmp, n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
-    LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->aa ? ctx->d_g[0] : ctx->d_g[1], s));
+    if (ctx->aa) LBG_CK(ctx, launch_to_dev_compact32(a, tmp, ctx->d_g[0], s));
+    else LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->d_g[1], s));
     LBG_CK(ctx, cudaFreeAsync(tmp, s));
     if (ctx->aa) {
         // AA: the populations are the natural-order state; the next launch collides them with
@@ -121,7 +129,13 @@ int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double 
         LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
         a.nout = tmp;
     }
-    if (ctx->aa) LBG_CK(ctx, launch_aa_finalize_f32(a, ctx->aa_phase == 1, s));
+    if (ctx->aa) {
+        // the AA kernels touch fluid nodes only: solid nodes report the reference's zeros
+        LBG_CK(ctx, cudaMemsetAsync(ctx->d_rho, 0, sizeof(double) * N, s));
+        for (int q = 0; q < 3; ++q) LBG_CK(ctx, cudaMemsetAsync(ctx->d_j[q], 0, sizeof(double) * N, s));
+        if (tmp) LBG_CK(ctx, cudaMemsetAsync(tmp, 0, sizeof(double) * Q * N, s));
+        LBG_CK(ctx, launch_aa_finalize_f32(a, ctx->aa_phase == 1, s));
+    }
     else LBG_CK(ctx, launch_finalize_f32(a, ctx->prev_kind == PREV_POST, s));
     if (n) LBG_CK(ctx, cudaMemcpyAsync(n, tmp, sizeof(double) * Q * N, cudaMemcpyDeviceToHost, s));
     if (density) LBG_CK(ctx, cudaMemcpyAsync(density, ctx->d_rho, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
@@ -133,6 +147,49 @@ int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double 
     return LBGPU_OK;
 }
 
+// Launch-bound tuner of the AA kernels: each variant (3..6 resident blocks per SM) of the even
+// and of the odd launch is timed on a scratch copy of the box's populations (the state is not
+// advanced), and the fastest is kept.  Small boxes (under 2^20 fluid nodes) keep the default;
+// LBGPU_AA_MINB=<even>,<odd> fixes the variants and skips the tuner.
+static int aa_tune(lbgpu_ctx *ctx)
+{
+    if (ctx->aa_tuned) return LBGPU_OK;
+    ctx->aa_tuned = true;
+    if (ctx->aa_minb_fixed || ctx->Nf < (1u << 20)) return LBGPU_OK;
+    cudaStream_t s = ctx->stream;
+    float *scratch = nullptr;
+    const size_t bytes = sizeof(float) * Q * (size_t)ctx->Nf;
+    if (cudaMallocAsync(&scratch, bytes, s) != cudaSuccess) {
+        cudaGetLastError();   // no room for the scratch copy: keep the default variants
+        return LBGPU_OK;
+    }
+    LBG_CK(ctx, cudaMemcpyAsync(scratch, ctx->d_g[0], bytes, cudaMemcpyDeviceToDevice, s));
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    a.g0 = scratch;
+    a.force_moment = a.force_collide = 1;
+    for (int odd = 0; odd < 2; ++odd) {
+        float best = 1e30f;
+        for (int minb = 3; minb <= 6; ++minb) {
+            a.minb_even = a.minb_odd = minb;
+            for (int k = 0; k < 2; ++k) LBG_CK(ctx, launch_aa_step_f32(a, odd, s));
+            LBG_CK(ctx, cudaEventRecord(ctx->ev0, s));
+            for (int k = 0; k < 6; ++k) LBG_CK(ctx, launch_aa_step_f32(a, odd, s));
+            LBG_CK(ctx, cudaEventRecord(ctx->ev1, s));
+            LBG_CK(ctx, cudaEventSynchronize(ctx->ev1));
+            float ms = 0.0f;
+            LBG_CK(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            if (ms < best) {
+                best = ms;
+                ctx->aa_minb[odd] = minb;
+            }
+        }
+    }
+    LBG_CK(ctx, cudaFreeAsync(scratch, s));
+    LBG_CK(ctx, cudaStreamSynchronize(s));
+    return LBGPU_OK;
+}
+
 // AA launches.  A launch computes the moments of the state it reads (force of the collision
 // that produced it: prev_force_moment) and performs the next collision (force_last_collide);
 // then the force of the following collision becomes force_on.  This reproduces the A/B
@@ -140,6 +197,8 @@ int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double 
 static int aa_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
 {
     cudaStream_t s = ctx->stream;
+    int rc0 = aa_tune(ctx);
+    if (rc0) return rc0;
     FlowArgs32 a;
     fill_args32(ctx, a);
     auto one = [&]() -> int {
