@@ -63,6 +63,16 @@ def args_():
     ap.add_argument("--batch-chunk", type=int, default=500, help="steps per call (one CUDA graph)")
     ap.add_argument("--one-at-a-time-sample", type=int, default=6,
                     help="cells (and a third as many tubes) timed one at a time")
+    # FP32 error statement (permeability, D_eff, adsorbed fraction, retention time) vs FP64
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--precision-size", type=int, default=64)
+    ap.add_argument("--precision-flow-steps", type=int, default=20000)
+    ap.add_argument("--precision-mp-steps", type=int, default=20000)
+    # charged solutes: Poisson-Nernst-Planck, then flow and tracer in the charged geometry
+    ap.add_argument("--no-charged", action="store_true")
+    ap.add_argument("--pnp-max-outer", type=int, default=200)
+    ap.add_argument("--charged-flow-steps", type=int, default=5000)
+    ap.add_argument("--charged-mp-steps", type=int, default=5000)
     # serving stream (Poisson arrivals, continuous batching)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-n", type=int, default=48)
@@ -184,6 +194,113 @@ def cpu_oracle_mlups(nature, seconds, threads):
         steps *= 2
     # subtract nothing: init_populations is part of every run but is one pass out of ~60 per step
     return nfluid * steps / dt / 1e6, steps, dt, time.perf_counter() - t0
+
+
+def precision_results(nature, precision, tau, f_ext, flow_steps, mp_steps, tracer):
+    """Flow then tracer propagation in one precision; the results the FP32 error is stated for.
+    permeability k = nu <u_x> / f_x (Darcy velocity over the whole box); D_eff = VACF(0)/2 +
+    sum VACF (Green-Kubo, unit step, flow axis x); adsorbed fraction = K n_if / (n_f + K n_if)
+    (the tracer's equilibrium time fraction on interfacial nodes); retention time = lx / v_tr
+    with v_tr = (1 - adsorbed fraction) <u_x>_fluid (mean tracer velocity)."""
+    from laboetie_gb300 import Box
+
+    with Box(nature, relaxation_time=tau, f_ext=f_ext, precision=precision) as box:
+        box.flow_init()
+        box.flow_steps(flow_steps, force_on=True)
+        _, rho, j = box.flow_get(populations=False)
+        v0 = box.mp_init(f_ext=f_ext, **tracer)
+        vac, _ = box.mp_propagate(mp_steps)
+        counts = box.node_counts()
+    nu = (tau - 0.5) / 3.0
+    fluid = nature == 0
+    ux_fluid = float(j[0][fluid].sum() / rho[fluid].sum())
+    k = nu * float(j[0].sum()) / nature.size / f_ext[0]
+    K = tracer["ka"] / tracer["kd"]
+    ads = K * counts["fluid_interfacial"] / (counts["fluid"] + K * counts["fluid_interfacial"])
+    return {"permeability": k, "d_eff": float(v0[0] / 2 + vac[:, 0].sum()),
+            "adsorbed_fraction": ads, "retention_time": nature.shape[2] / ((1 - ads) * ux_fluid),
+            "mp_steps": int(len(vac))}
+
+
+def bench_precision(a):
+    """FP32-deviation vs FP64 error of each result on a porous medium (spheres r=8, porosity
+    0.60, tau 0.8, f_ext 1e-6, tracer Db 0.01 with beta dF = -2)."""
+    from laboetie_gb300 import FP32_DEV, FP64
+    from laboetie_gb300 import geometry as geo
+
+    L = a.precision_size
+    nat = geo.porous_spheres(L, RADIUS, POROSITY, SEED)
+    tracer = dict(Db=0.01, ka=0.01 * math.exp(2.0), kd=0.01)
+    out = {}
+    t = time.perf_counter()
+    for name, prec in (("fp64", FP64), ("fp32", FP32_DEV)):
+        out[name] = precision_results(nat, prec, TAU, FEXT, a.precision_flow_steps, a.precision_mp_steps, tracer)
+    rel = {k: abs(out["fp32"][k] - out["fp64"][k]) / abs(out["fp64"][k])
+           for k in ("permeability", "d_eff", "adsorbed_fraction", "retention_time")}
+    return {"config": {"workload": f"porous {L}^3 spheres r=8 porosity 0.60 seed {SEED}, tau 0.8, f_ext (1e-6,0,0)",
+                       "flow_steps": a.precision_flow_steps, "mp_steps": a.precision_mp_steps,
+                       "tracer": "Db 0.01, K = e^2 (kd 0.01)"},
+            "fp64": out["fp64"], "fp32": out["fp32"], "relative_error": rel,
+            "seconds": round(time.perf_counter() - t, 1)}
+
+
+def bench_charged(a):
+    """Charged solutes (slit 1x1x64 and touching spheres 48^3, surface charge -0.01 e per
+    interfacial solid node, bjl 0.4, lambda_D 4, D+- 0.05): the Poisson-Nernst-Planck loop with
+    the reference's Jacobi solver (bit-identical to the oracle) and with the 4-colour SOR
+    (omega 1.8, tol 1e-10), the SOR error on potential and ion densities against the reference
+    solver, then FP32 vs FP64 flow (f_ext 1e-6) and tracer VACF in the charged geometry (the
+    tracer is neutral: the reference stops on a charged one, module_moment_propagation.f90:71-79)."""
+    from laboetie_gb300 import FP32_DEV, FP64, Box
+    from laboetie_gb300 import geometry as geo
+    from laboetie_gb300.lbgpu import POISSON_REFERENCE, POISSON_SOR4
+
+    cases = [("slit 1x1x64", geo.slit(1, 1, 64)), ("touching spheres 48^3", geo.cc(48, 48, 48))]
+    out = []
+    for name, nat in cases:
+        res = {"case": name}
+        with Box(nat) as box:
+            inter = box.interfacial()
+        sigma = -0.01 * int(((nat == 1) & (inter == 1)).sum())
+        sol = {}
+        for sname, solver in (("reference_jacobi", POISSON_REFERENCE), ("sor4", POISSON_SOR4)):
+            with Box(nat) as box:
+                box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
+                             solver=solver, omega=1.8, tol=1e-10)
+                t = time.perf_counter()
+                outer, sweeps, rc = box.poisson_nernst_planck(max_outer=a.pnp_max_outer, check=False)
+                dt = time.perf_counter() - t
+                cp, cm, phi, _ = box.pnp_get()
+            sol[sname] = (cp, cm, phi)
+            res[sname] = {"outer": outer, "sweeps": sweeps, "seconds": round(dt, 4), "status": rc,
+                          "sweeps_per_s": round(sweeps / dt, 1) if dt > 0 else None}
+            if solver == POISSON_SOR4 and any(d % 2 for d in nat.shape):
+                res[sname]["note"] = "odd box side: the 4-colour solver runs as Jacobi with omega 1.4 and tol 1e-10"
+        rel = lambda x, y: float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+        r, q = sol["reference_jacobi"], sol["sor4"]
+        res["sor4_vs_reference"] = {"phi": rel(q[2], r[2]), "c_plus": rel(q[0], r[0]),
+                                    "c_minus": rel(q[1], r[1])}
+        v = {}
+        for pname, prec in (("fp64", FP64), ("fp32", FP32_DEV)):
+            with Box(nat, relaxation_time=1.0, f_ext=(1e-6, 0.0, 0.0), precision=prec) as box:
+                box.flow_init()
+                box.flow_steps(a.charged_flow_steps, force_on=True)
+                v0 = box.mp_init(f_ext=(1e-6, 0.0, 0.0), Db=0.01, ka=0.01 * math.e, kd=0.01)
+                vac, _ = box.mp_propagate(a.charged_mp_steps)
+            v[pname] = (v0, vac)
+        scale = float(np.abs(v["fp64"][0]).max())
+        n = min(len(v["fp64"][1]), len(v["fp32"][1]))
+        res["vacf_fp32_vs_fp64"] = {
+            "max_abs_over_vacf0": float(np.max(np.abs(v["fp32"][1][:n] - v["fp64"][1][:n]))) / scale,
+            "d_eff_rel": float(abs((v["fp32"][0][0] / 2 + v["fp32"][1][:n, 0].sum()) -
+                                   (v["fp64"][0][0] / 2 + v["fp64"][1][:n, 0].sum())) /
+                               abs(v["fp64"][0][0] / 2 + v["fp64"][1][:n, 0].sum())),
+            "steps": n}
+        out.append(res)
+    return {"cases": out, "config": {"bjl": 0.4, "lambda_D": 4.0, "D_plus": 0.05, "D_minus": 0.05,
+                                     "surface_charge_per_interfacial_solid_node": -0.01,
+                                     "max_outer": a.pnp_max_outer, "flow_steps": a.charged_flow_steps,
+                                     "mp_steps": a.charged_mp_steps, "tracer": "neutral, Db 0.01, K = e"}}
 
 
 def bench_batched(a):
@@ -468,6 +585,10 @@ def main():
         "clocks": clocks_out,
         "cpu_baseline": cpu,
     }
+    if world == 1 and not a.no_precision:
+        line["precision"] = bench_precision(a)
+    if world == 1 and not a.no_charged:
+        line["charged"] = bench_charged(a)
     if world == 1 and not a.no_batch:
         line["batched"] = bench_batched(a)
     if world == 1 and not a.no_serve:
