@@ -61,7 +61,24 @@ struct MpArgs32 {
     int ads;
     float ka, kd, one_minus_kd;
     float a1[3], lwh[3];
+    int slab;                          // shared-memory slab step where the box allows it
 };
+
+// Shared-memory slab variant of the FP32 step (mp_f32.cu): 32 x 8 column tiles sweeping a chunk
+// of z planes.  Used when lx >= 32, ly >= 8 and lz >= 3.  Returns the grid (0: not eligible) and
+// the planes per block in *zc.
+constexpr int MPS_TX = 32, MPS_TY = 8;
+inline unsigned mp32_slab_grid(int lx, int ly, int lz, int *zc)
+{
+    if (lx < MPS_TX || ly < MPS_TY || lz < 3) return 0;
+    const int nxy = ((lx + MPS_TX - 1) / MPS_TX) * ((ly + MPS_TY - 1) / MPS_TY);
+    int nz = 2432 / nxy;
+    if (nz < 1) nz = 1;
+    if (nz > lz) nz = lz;
+    const int c = (lz + nz - 1) / nz;
+    *zc = c;
+    return (unsigned)(nxy * ((lz + c - 1) / c));
+}
 
 cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);

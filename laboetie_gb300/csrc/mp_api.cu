@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -144,7 +145,9 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
     a.q = tr->z;
     a.D = tr->Db;
     s->nblocks = (unsigned)((N + MP_BLOCK - 1) / MP_BLOCK);
-    if ((rc = alloc_zero(ctx, s, &a.partial, 3 * (size_t)s->nblocks))) return rc;
+    int zc = 0;
+    const unsigned slab = s->prec == LBGPU_FP64 ? 0u : mp32_slab_grid(a.lx, a.ly, a.lz, &zc);
+    if ((rc = alloc_zero(ctx, s, &a.partial, 3 * (size_t)std::max(s->nblocks, slab)))) return rc;
     if ((rc = alloc_zero(ctx, s, &a.ctl, 1))) return rc;
 
     if (s->prec == LBGPU_FP64) {
@@ -176,6 +179,9 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
         b.ly = a.ly;
         b.lz = a.lz;
         b.ads = s->ads;
+        // LBGPU_MP_SLAB=0: the grid-stride step everywhere (same per-node arithmetic)
+        const char *slab_env = std::getenv("LBGPU_MP_SLAB");
+        b.slab = !(slab_env && std::string(slab_env) == "0");
         b.ka = (float)tr->ka;
         b.kd = (float)tr->kd;
         b.one_minus_kd = (float)(1.0 - tr->kd);

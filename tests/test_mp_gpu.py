@@ -137,3 +137,25 @@ def test_mp_fp32_tracks_fp64(oracle_mod):
     d64 = v64[0] / 2 + v64[1].sum(axis=0)
     d32 = v32[0] / 2 + v32[1].sum(axis=0)
     assert abs(d32[0] - d64[0]) <= 1e-5 * abs(d64[0])
+
+
+def test_mp_fp32_slab_and_grid_stride_steps_agree(monkeypatch):
+    """The shared-memory slab step (boxes with lx >= 32, ly >= 8) and the grid-stride step do
+    the same per-node arithmetic: P and P_ads are bit-identical after any number of steps; the
+    VACF differs only in the order of its node sums (1e-12 of |VACF(0)|)."""
+    nat = geo.porous_spheres(L=40, radius=5.0, porosity=0.6, seed=3)
+    rng = np.random.default_rng(5)
+    rho = np.where(nat == 0, 1.0 + 1e-3 * rng.standard_normal(nat.shape), 0.0)
+    j = [np.where(nat == 0, 1e-3 * rng.standard_normal(nat.shape), 0.0) for _ in range(3)]
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("LBGPU_MP_SLAB", mode)
+        with Box(nat, precision=FP32_DEV) as box:
+            v0 = box.mp_init(moments=(rho, j), Db=0.01, ka=0.02, kd=0.01)
+            vac, _ = box.mp_propagate(37)
+            P, A = box.mp_get()
+        out[mode] = (v0, vac, P, A)
+    a, b = out["1"], out["0"]
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+    assert len(a[1]) == len(b[1]) == 37
+    assert np.max(np.abs(a[1] - b[1])) <= 1e-12 * np.abs(a[0]).max()
