@@ -11,12 +11,37 @@
 #include "batch.h"
 #include "collide32.cuh"
 #include "common.cuh"
+#include "compact.cuh"
 #include "lbgpu.h"
 
 namespace lbg {
 namespace {
 
-// One AA update of one fluid node of a box whose populations start at g (global or shared).
+// Moments and collision of one node's 19 deviations (the same operations in every layout).
+__device__ __forceinline__ void aa_collide(float (&f)[Q], const BatchInst &I)
+{
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
+    static_for<0, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        drho += f[l];
+        if constexpr (c.x > 0) jx += f[l];
+        if constexpr (c.x < 0) jx -= f[l];
+        if constexpr (c.y > 0) jy += f[l];
+        if constexpr (c.y < 0) jy -= f[l];
+        if constexpr (c.z > 0) jz += f[l];
+        if constexpr (c.z < 0) jz -= f[l];
+    });
+    if (I.force) {
+        jx = __fadd_rn(jx, __fmul_rn(0.5f, I.F[0]));
+        jy = __fadd_rn(jy, __fmul_rn(0.5f, I.F[1]));
+        jz = __fadd_rn(jz, __fmul_rn(0.5f, I.F[2]));
+    }
+    collide_dev<7>(f, drho, jx, jy, jz, I, I.force != 0);
+}
+
+// One AA update of one fluid node of a box in the lattice layout whose populations start at g
+// (global or shared).
 template <bool ODD>
 __device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uint32_t m,
                                         const BatchInst &I)
@@ -49,30 +74,41 @@ __device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uin
 #pragma unroll
         for (int l = 0; l < Q; ++l) f[l] = g[(unsigned)l * N + node];
     }
-    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
-    static_for<0, Q>([&](auto L) {
-        constexpr int l = decltype(L)::value;
-        constexpr Vel c = vel(l);
-        drho += f[l];
-        if constexpr (c.x > 0) jx += f[l];
-        if constexpr (c.x < 0) jx -= f[l];
-        if constexpr (c.y > 0) jy += f[l];
-        if constexpr (c.y < 0) jy -= f[l];
-        if constexpr (c.z > 0) jz += f[l];
-        if constexpr (c.z < 0) jz -= f[l];
-    });
-    if (I.force) {
-        jx = __fadd_rn(jx, __fmul_rn(0.5f, I.F[0]));
-        jy = __fadd_rn(jy, __fmul_rn(0.5f, I.F[1]));
-        jz = __fadd_rn(jz, __fmul_rn(0.5f, I.F[2]));
-    }
-    collide_dev<7>(f, drho, jx, jy, jz, I, I.force != 0);
+    aa_collide(f, I);
     if constexpr (ODD) {
 #pragma unroll
         for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
     } else {
 #pragma unroll
         for (int l = 0; l < Q; ++l) g[(unsigned)inv(l) * N + node] = f[l];
+    }
+}
+
+// One AA update of the compact node i of a box in the fluid-only layout (compact.cuh).  A thread
+// writes exactly the slots it read, so the read-only cache path is safe for the loads.
+template <bool ODD>
+__device__ __forceinline__ void aa_node_compact(const BatchInst &I, unsigned i)
+{
+    float *g = I.g;
+    const unsigned Nf = I.Nf;
+    float f[Q];
+    unsigned off[Q];
+    if constexpr (ODD) {
+        aa_gather_offsets(I, i, __ldg(I.cpos + i), __ldg(I.cmask + i), [&](int l, unsigned o) {
+            off[l] = o;
+            f[l] = __ldg(g + o);
+        });
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = __ldg(g + (unsigned)l * Nf + i);
+    }
+    aa_collide(f, I);
+    if constexpr (ODD) {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) g[(unsigned)inv(l) * Nf + i] = f[l];
     }
 }
 
@@ -94,13 +130,11 @@ __device__ __forceinline__ float cdot(const float4 &v)
 // vt receives the node's VACF term (before the 1/Pstat factor for INIT).
 template <bool INIT>
 __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float4 *Pnext,
-                                        const float4 *An, float4 *Anext, unsigned r, uint32_t m,
-                                        const BatchInst &I, double (&vt)[3], unsigned &bad)
+                                        const float4 *An, float4 *Anext, unsigned r, int x, int y,
+                                        int z, uint32_t m, const BatchInst &I, double (&vt)[3],
+                                        unsigned &bad)
 {
     const int lx = I.lx, ly = I.ly, lz = I.lz;
-    const int x = (int)(r % (unsigned)lx);
-    const unsigned yz = r / (unsigned)lx;
-    const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
     const int sy = lx, sz = lx * ly;
     // [c+1] = coordinate of (x + c), periodic
     const int X[3] = {wrap_minus(x, lx), x, wrap_plus(x, lx)};
@@ -165,6 +199,22 @@ __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float
     }
 }
 
+__device__ __forceinline__ void lattice_xyz(const BatchInst &I, unsigned r, int &x, int &y, int &z)
+{
+    x = (int)(r % (unsigned)I.lx);
+    const unsigned yz = r / (unsigned)I.lx;
+    y = (int)(yz % (unsigned)I.ly);
+    z = (int)(yz / (unsigned)I.ly);
+}
+
+__device__ __forceinline__ unsigned compact_xyz(const BatchInst &I, unsigned c, int &x, int &y, int &z)
+{
+    x = (int)(c & ((1u << I.xbits) - 1u));
+    y = (int)((c >> I.xbits) & ((1u << I.ybits) - 1u));
+    z = (int)(c >> (I.xbits + I.ybits));
+    return (unsigned)x + (unsigned)I.lx * ((unsigned)y + (unsigned)I.ly * (unsigned)z);
+}
+
 // Sum of 3 doubles over the block in a fixed order (lanes by shuffle tree, then warps in index
 // order); valid in thread 0.  Any block size that is a multiple of 32, up to 1024.
 __device__ __forceinline__ void block_sum3(double (&v)[3])
@@ -189,11 +239,11 @@ __device__ __forceinline__ void block_sum3(double (&v)[3])
 
 __device__ __forceinline__ unsigned *status_word(const BatchInst &I)
 {
-    const unsigned ntile = ((unsigned)I.N + BATCH_BLOCK - 1) / BATCH_BLOCK;
-    return reinterpret_cast<unsigned *>(I.tacc + (size_t)ntile * BATCH_TACC);
+    return reinterpret_cast<unsigned *>(I.tacc + (size_t)batch_ntile(I) * BATCH_TACC);
 }
 
-// Velocity u = j/rho of a node in natural order (after an even number of AA launches).
+// Velocity u = j/rho of a node in natural order (after an even number of AA launches); g holds
+// the populations with stride N (lattice) or Nf (compact), node is the index in that layout.
 __device__ __forceinline__ float3 node_velocity(const float *g, unsigned N, unsigned node,
                                                 const BatchInst &I)
 {
@@ -226,11 +276,11 @@ __device__ __forceinline__ float du_and_store(float4 *uprev, unsigned node, cons
     return fmaxf(fmaxf(fabsf(u.x - p.x), fabsf(u.y - p.y)), fabsf(u.z - p.z));
 }
 
-// FP64 density and flux of a node in natural order (solid nodes: zeros).
+// FP64 density and flux of a fluid node in natural order (index in the box's layout).
 __device__ __forceinline__ void node_moments64(const BatchInst &I, unsigned node, double &rho,
                                                double &X, double &Y, double &Z)
 {
-    const unsigned N = (unsigned)I.N;
+    const unsigned N = I.compact ? I.Nf : (unsigned)I.N;
     double d = 0.0;
     X = Y = Z = 0.0;
     static_for<0, Q>([&](auto L) {
@@ -256,8 +306,12 @@ __global__ void __launch_bounds__(BATCH_BLOCK, 3) k_batch_aa(const BatchInst *__
 {
     const BatchTile t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
-    const unsigned N = (unsigned)I.N;
     const unsigned node = (unsigned)t.start + threadIdx.x;
+    if (I.compact) {
+        if (node < I.Nf) aa_node_compact<ODD>(I, node);
+        return;
+    }
+    const unsigned N = (unsigned)I.N;
     if (node >= N) return;
     const uint32_t m = __ldg(I.mask + node);
     if (!(m & FLUID_BIT)) return;
@@ -275,15 +329,24 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
     if constexpr (INIT) t = BatchTile{inst, (int)blockIdx.x * BATCH_BLOCK};
     else t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
-    const unsigned N = (unsigned)I.N;
-    const unsigned node = (unsigned)t.start + threadIdx.x;
+    const unsigned k = (unsigned)t.start + threadIdx.x;   // node in the box's layout
     double vt[3] = {0.0, 0.0, 0.0};
     unsigned bad = 0;
-    if (node < N) {
-        const uint32_t m = __ldg(I.mask + node);
+    if (k < batch_units(I)) {
+        uint32_t m;
+        unsigned r;
+        int x, y, z;
+        if (I.compact) {
+            m = __ldg(I.cmask + k);
+            r = compact_xyz(I, __ldg(I.cpos + k), x, y, z);
+        } else {
+            m = __ldg(I.mask + k);
+            r = k;
+            lattice_xyz(I, r, x, y, z);
+        }
         if (m & FLUID_BIT) {
-            if constexpr (INIT) mp_node<true>(I.V, nullptr, I.P[0], nullptr, nullptr, node, m, I, vt, bad);
-            else mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], node, m, I, vt, bad);
+            if constexpr (INIT) mp_node<true>(I.V, nullptr, I.P[0], nullptr, nullptr, r, x, y, z, m, I, vt, bad);
+            else mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], r, x, y, z, m, I, vt, bad);
         }
     }
     block_sum3(vt);
@@ -310,18 +373,20 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
 // V = (j + f_ext)/rho of one box from its flow state (FP64 moments rounded once to FP32).
 __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_v(const BatchInst *__restrict__ insts, int inst)
 {
+    // compact boxes: V stays zero on solid nodes (the allocation is zeroed when the box is added)
     const BatchInst &I = insts[inst];
-    const unsigned node = blockIdx.x * BATCH_BLOCK + threadIdx.x;
-    if (node >= (unsigned)I.N) return;
-    if (!(I.mask[node] & FLUID_BIT)) {
-        I.V[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned k = blockIdx.x * BATCH_BLOCK + threadIdx.x;
+    if (k >= batch_units(I)) return;
+    const unsigned r = I.compact ? lattice_of(I, I.cpos[k]) : k;
+    if (!I.compact && !(I.mask[k] & FLUID_BIT)) {
+        I.V[r] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     double rho, J[3];
-    node_moments64(I, node, rho, J[0], J[1], J[2]);
+    node_moments64(I, k, rho, J[0], J[1], J[2]);
     float o[3];
     for (int d = 0; d < 3; ++d) o[d] = (float)((J[d] + I.tfext[d]) / rho);
-    I.V[node] = make_float4(o[0], o[1], o[2], 0.0f);
+    I.V[r] = make_float4(o[0], o[1], o[2], 0.0f);
 }
 
 // One block per small box, for all the steps of a call: load, nsteps steps of the box's phase
@@ -388,7 +453,11 @@ __global__ void __launch_bounds__(BATCH_SMEM_THREADS) k_batch_smem(const BatchIn
         double vt[3] = {0.0, 0.0, 0.0};
         for (unsigned node = threadIdx.x; node < N; node += T) {
             const uint32_t m = msk[node];
-            if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, node, m, I, vt, bad);
+            if (m & FLUID_BIT) {
+                int x, y, z;
+                lattice_xyz(I, node, x, y, z);
+                mp_node<false>(V, Pn, Px, An, Ax, node, x, y, z, m, I, vt, bad);
+            }
         }
         block_sum3(vt);  // its barriers also separate this step from the next
         if (threadIdx.x == 0)
@@ -416,11 +485,13 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_check(const BatchInst *__
 {
     const BatchTile t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
-    const unsigned N = (unsigned)I.N;
     const unsigned node = (unsigned)t.start + threadIdx.x;
     float du = 0.0f;
-    if (node < N && (I.mask[node] & FLUID_BIT))
-        du = du_and_store(I.uprev, node, node_velocity(I.g, N, node, I));
+    if (I.compact) {
+        if (node < I.Nf) du = du_and_store(I.uprev, node, node_velocity(I.g, I.Nf, node, I));
+    } else if (node < (unsigned)I.N && (I.mask[node] & FLUID_BIT)) {
+        du = du_and_store(I.uprev, node, node_velocity(I.g, (unsigned)I.N, node, I));
+    }
     for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
     if ((threadIdx.x & 31) == 0) atomicMax(du_out + t.inst, __float_as_uint(du));
 }
@@ -431,13 +502,18 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_moments(const BatchInst *
                                                                double *jz)
 {
     const BatchInst &I = insts[inst];
-    const unsigned node = blockIdx.x * BATCH_BLOCK + threadIdx.x;
-    if (node >= (unsigned)I.N) return;
-    if (!(I.mask[node] & FLUID_BIT)) {
-        rho[node] = jx[node] = jy[node] = jz[node] = 0.0;
+    const unsigned k = blockIdx.x * BATCH_BLOCK + threadIdx.x;
+    if (k >= batch_units(I)) return;
+    if (I.compact) {
+        const unsigned r = lattice_of(I, I.cpos[k]);
+        node_moments64(I, k, rho[r], jx[r], jy[r], jz[r]);
         return;
     }
-    node_moments64(I, node, rho[node], jx[node], jy[node], jz[node]);
+    if (!(I.mask[k] & FLUID_BIT)) {
+        rho[k] = jx[k] = jy[k] = jz[k] = 0.0;
+        return;
+    }
+    node_moments64(I, k, rho[k], jx[k], jy[k], jz[k]);
 }
 
 }  // namespace
@@ -464,9 +540,9 @@ cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, int N, cudaStream_t s)
+cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, unsigned units, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((N + BATCH_BLOCK - 1) / BATCH_BLOCK);
+    const unsigned grid = (units + BATCH_BLOCK - 1) / BATCH_BLOCK;
     k_batch_mp_v<<<grid, BATCH_BLOCK, 0, s>>>(insts, inst);
     k_batch_mp<true><<<grid, BATCH_BLOCK, 0, s>>>(insts, nullptr, inst, 0);
     return cudaGetLastError();
@@ -488,10 +564,10 @@ cudaError_t launch_batch_check(const BatchInst *insts, const BatchTile *tiles, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_moments(const BatchInst *insts, int inst, int N, double *rho, double *jx,
+cudaError_t launch_batch_moments(const BatchInst *insts, int inst, unsigned units, double *rho, double *jx,
                                  double *jy, double *jz, cudaStream_t s)
 {
-    k_batch_moments<<<(N + BATCH_BLOCK - 1) / BATCH_BLOCK, BATCH_BLOCK, 0, s>>>(insts, inst, rho, jx, jy, jz);
+    k_batch_moments<<<(units + BATCH_BLOCK - 1) / BATCH_BLOCK, BATCH_BLOCK, 0, s>>>(insts, inst, rho, jx, jy, jz);
     return cudaGetLastError();
 }
 

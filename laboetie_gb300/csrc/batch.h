@@ -41,7 +41,18 @@ struct BatchInst {
     float a1[3], lwh[3], ka, kd, one_minus_kd;
     float bw;               // 1 / (fluid + K * interfacial fluid) nodes, rounded to FP32
     double tfext[3];        // tracer f_ext added to j in V
+    // Tiled boxes use the fluid-only AA layout of compact.cuh: g[l*Nf + i], uprev[i], tiles of
+    // compact indices.  Shared-memory boxes keep the lattice layout g[l*N + node].
+    int compact;
+    unsigned Nf;
+    int nw, xbits, ybits;
+    const uint32_t *cpos, *cmask;
+    const uint2 *rowtab;
 };
+
+// Nodes a box's kernels iterate (compact fluid nodes or lattice nodes) and its 256-node tiles.
+__host__ __device__ inline unsigned batch_units(const BatchInst &I) { return I.compact ? I.Nf : (unsigned)I.N; }
+__host__ __device__ inline unsigned batch_ntile(const BatchInst &I) { return (batch_units(I) + BATCH_BLOCK - 1) / BATCH_BLOCK; }
 
 struct BatchTile {
     int inst;   // index into the descriptor array
@@ -59,10 +70,13 @@ cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist
                               cudaStream_t s);
 cudaError_t launch_batch_check(const BatchInst *insts, const BatchTile *tiles, int ntiles,
                                unsigned *du, cudaStream_t s);
-cudaError_t launch_batch_moments(const BatchInst *insts, int inst, int N, double *rho, double *jx,
+// density and flux of one box at every lattice node (compact boxes: the caller zeroes the
+// outputs first, solid nodes stay zero)
+cudaError_t launch_batch_moments(const BatchInst *insts, int inst, unsigned units, double *rho, double *jx,
                                  double *jy, double *jz, cudaStream_t s);
-// start of the tracer phase of one box: V from the flow state, P(t=1) and VACF(0) per tile
-cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, int N, cudaStream_t s);
+// start of the tracer phase of one box (units = batch_units): V from the flow state, P(t=1) and
+// VACF(0) per tile
+cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, unsigned units, cudaStream_t s);
 cudaError_t batch_configure(int max_smem_bytes);
 
 }  // namespace lbg

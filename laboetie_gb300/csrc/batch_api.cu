@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "batch.h"
+#include "compact.cuh"
 #include "ctx.h"
 #include "flow.h"
 #include "lbgpu.h"
@@ -37,9 +38,9 @@ struct Slot {
     void *mem = nullptr;      // the slot's one device allocation
     long long fluid = 0;
     size_t bytes = 0;
-    bool smem = false;        // stepped with the whole box in shared memory
+    bool smem = false;        // stepped with the whole box in shared memory (lattice layout)
     bool tracer = false;
-    int ntile = 0;
+    int ntile = 0;            // 256-node tiles of the box's layout
     int mp_steps = 0;
 };
 
@@ -57,19 +58,27 @@ bool tracer_ads(const lbgpu_tracer &t)
     return std::fabs(K) > EPS;
 }
 
-// Byte layout of a slot's allocation: g, mask, uprev, nature, then the tracer buffers.
+// Byte layout of a slot's allocation: populations (g, over `units` nodes: lattice nodes, or
+// fluid nodes in the compact layout), lattice flags, previous velocity per unit, nature, the
+// compact tables (positions, flags, row table of `tab` entries) and the tracer buffers
+// (lattice-ordered V, P, A and per-tile VACF accumulators).
 struct Layout {
-    size_t g, mask, uprev, nature, V, P0, P1, A0, A1, tacc, total;
+    size_t g, mask, uprev, nature, cpos, cmask, rowtab, V, P0, P1, A0, A1, tacc, total;
 };
 
-Layout layout(long long N, bool tracer, bool ads)
+Layout layout(long long N, long long units, long long tab, bool compact, bool tracer, bool ads)
 {
     Layout L{};
     size_t o = 0;
-    L.g = o;      o += up(sizeof(float) * Q * (size_t)N);
+    L.g = o;      o += up(sizeof(float) * Q * (size_t)units);
     L.mask = o;   o += up(sizeof(uint32_t) * (size_t)N);
-    L.uprev = o;  o += up(sizeof(float4) * (size_t)N);
+    L.uprev = o;  o += up(sizeof(float4) * (size_t)units);
     L.nature = o; o += up((size_t)N);
+    if (compact) {
+        L.cpos = o;   o += up(sizeof(uint32_t) * (size_t)units);
+        L.cmask = o;  o += up(sizeof(uint32_t) * (size_t)units);
+        L.rowtab = o; o += up(sizeof(uint2) * (size_t)tab);
+    }
     if (tracer) {
         const size_t f4 = up(sizeof(float4) * (size_t)N);
         L.V = o;  o += f4;
@@ -79,11 +88,19 @@ Layout layout(long long N, bool tracer, bool ads)
             L.A0 = o; o += f4;
             L.A1 = o; o += f4;
         }
-        const size_t ntile = ((size_t)N + BATCH_BLOCK - 1) / BATCH_BLOCK;
+        const size_t ntile = ((size_t)units + BATCH_BLOCK - 1) / BATCH_BLOCK;
         L.tacc = o; o += up(sizeof(double) * (ntile * BATCH_TACC + 1));
     }
     L.total = o;
     return L;
+}
+
+// Upper bound of a box's footprint over both layouts (the fluid count is not known before the
+// geometry is read): the lattice layout plus the compact tables for every node.
+size_t footprint_bound(long long N, int lx, int ly, int lz, bool tracer, bool ads)
+{
+    const long long tab = (long long)ly * lz * ((lx + 31) / 32);
+    return layout(N, N, tab, true, tracer, ads).total;
 }
 
 }  // namespace
@@ -196,7 +213,8 @@ int rebuild(lbgpu_batch *b)
                                                                        : batch_smem_mp(sl.d.N, sl.d.ads));
         } else {
             auto &list = sl.d.phase == BATCH_FLOW ? flow : mp;
-            for (int st = 0; st < sl.d.N; st += BATCH_BLOCK) list.push_back({id, st});
+            const int units = (int)batch_units(sl.d);
+            for (int st = 0; st < units; st += BATCH_BLOCK) list.push_back({id, st});
         }
     }
     std::vector<BatchTile> tiles(flow);
@@ -313,7 +331,7 @@ size_t lbgpu_batch_footprint(const lbgpu_cell *c)
     if (!c || c->lx <= 0 || c->ly <= 0 || c->lz <= 0) return 0;
     const long long N = (long long)c->lx * c->ly * c->lz;
     const bool tracer = c->tracer.Db != 0.0;
-    return layout(N, tracer, tracer && tracer_ads(c->tracer)).total;
+    return footprint_bound(N, c->lx, c->ly, c->lz, tracer, tracer && tracer_ads(c->tracer));
 }
 
 int lbgpu_batch_create(int device, size_t memory_budget, lbgpu_batch **out)
@@ -392,19 +410,28 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
     const long long N = (long long)c->lx * c->ly * c->lz;
     if ((unsigned long long)Q * N >= (1ULL << 32)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: box too large");
     const bool ads = tracer && tracer_ads(t);
-    const Layout L = layout(N, tracer, ads);
+    for (long long i = 0; i < N; ++i)
+        if (nature[i] != 0 && nature[i] != 1) return bfail(LBGPU_ERR_INVALID, "nature must be 0 or 1");
+    Slot sl;
+    sl.active = true;
+    sl.tracer = tracer;
+    sl.smem = batch_smem_flow((int)N) <= b->smem_max && (!tracer || batch_smem_mp((int)N, ads) <= b->smem_max);
+    // tiled boxes: fluid-only layout (compact.cuh) built from the geometry on the host
+    std::vector<uint2> tab;
+    std::vector<uint32_t> pos;
+    int nw = 0, xbits = 0, ybits = 0;
+    const bool compact = !sl.smem;
+    if (compact && !build_compact_tables(c->lx, c->ly, c->lz, nature, tab, pos, nw, xbits, ybits))
+        return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: box shape beyond the packed-position limits");
+    if (compact && pos.empty()) return bfail(LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
+    const long long units = compact ? (long long)pos.size() : N;
+    const Layout L = layout(N, units, (long long)tab.size(), compact, tracer, ads);
     if (b->used + L.total > b->budget)
         return bfail(LBGPU_ERR_OOM, "lbgpu_batch_add: box needs " + std::to_string(L.total >> 20) +
                                         " MiB beyond the batch memory budget");
-    for (long long i = 0; i < N; ++i)
-        if (nature[i] != 0 && nature[i] != 1) return bfail(LBGPU_ERR_INVALID, "nature must be 0 or 1");
     cudaStream_t s = b->stream;
-    Slot sl;
-    sl.active = true;
     sl.bytes = L.total;
-    sl.tracer = tracer;
-    sl.ntile = (int)((N + BATCH_BLOCK - 1) / BATCH_BLOCK);
-    sl.smem = batch_smem_flow((int)N) <= b->smem_max && (!tracer || batch_smem_mp((int)N, ads) <= b->smem_max);
+    sl.ntile = (int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK);
     LBB_CK(cudaMallocAsync(&sl.mem, L.total, s));
     char *base = static_cast<char *>(sl.mem);
     BatchInst &d = sl.d;
@@ -421,6 +448,16 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
     d.mask = mask;
     d.uprev = reinterpret_cast<float4 *>(base + L.uprev);
     int8_t *d_nature = reinterpret_cast<int8_t *>(base + L.nature);
+    if (compact) {
+        d.compact = 1;
+        d.Nf = (unsigned)units;
+        d.nw = nw;
+        d.xbits = xbits;
+        d.ybits = ybits;
+        d.cpos = reinterpret_cast<uint32_t *>(base + L.cpos);
+        d.cmask = reinterpret_cast<uint32_t *>(base + L.cmask);
+        d.rowtab = reinterpret_cast<uint2 *>(base + L.rowtab);
+    }
     if (tracer) {
         d.V = reinterpret_cast<float4 *>(base + L.V);
         d.P[0] = reinterpret_cast<float4 *>(base + L.P0);
@@ -431,14 +468,28 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
         }
         d.tacc = reinterpret_cast<double *>(base + L.tacc);
     }
-    LBB_CK(cudaMemsetAsync(sl.mem, 0, L.total, s));   // rest state rho = rho0, j = 0; P = A = 0
+    LBB_CK(cudaMemsetAsync(sl.mem, 0, L.total, s));   // rest state rho = rho0, j = 0; P = A = V = 0
     LBB_CK(cudaMemcpyAsync(d_nature, nature, N, cudaMemcpyHostToDevice, s));
     LBB_CK(launch_node_flags(d_nature, mask, c->lx, c->ly, c->lz, s));
+    if (compact) {
+        LBB_CK(cudaMemcpyAsync((void *)d.cpos, pos.data(), sizeof(uint32_t) * pos.size(), cudaMemcpyHostToDevice, s));
+        LBB_CK(cudaMemcpyAsync((void *)d.rowtab, tab.data(), sizeof(uint2) * tab.size(), cudaMemcpyHostToDevice, s));
+        FlowArgs32 fa;
+        std::memset(&fa, 0, sizeof(fa));
+        fa.mask = mask;
+        fa.Nf = d.Nf;
+        fa.cpos = d.cpos;
+        fa.lx = d.lx;
+        fa.ly = d.ly;
+        fa.xbits = xbits;
+        fa.ybits = ybits;
+        LBB_CK(launch_compact_mask(fa, const_cast<uint32_t *>(d.cmask), s));
+    }
     LBB_CK(cudaMemsetAsync(b->d_counts, 0, 4 * sizeof(unsigned long long), s));
     LBB_CK(launch_count_nodes(mask, N, b->d_counts, s));
     unsigned long long counts[4];
     LBB_CK(cudaMemcpyAsync(counts, b->d_counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
-    LBB_CK(cudaStreamSynchronize(s));   // the caller may reuse nature
+    LBB_CK(cudaStreamSynchronize(s));   // the caller may reuse nature; host tables go out of scope
     if (!counts[0]) {
         cudaFreeAsync(sl.mem, s);
         return bfail(LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
@@ -514,11 +565,14 @@ int lbgpu_batch_moments(lbgpu_batch *b, int id, double *rho, double *jx, double 
     int rc = rebuild(b);
     if (rc) return rc;
     const int desc = desc_of(b, id);
-    const int N = b->slots[id].d.N;
+    const BatchInst &d = b->slots[id].d;
+    const int N = d.N;
     cudaStream_t s = b->stream;
     double *tmp = nullptr;
     LBB_CK(cudaMallocAsync((void **)&tmp, sizeof(double) * 4 * (size_t)N, s));
-    LBB_CK(launch_batch_moments(b->d_insts, desc, N, tmp, tmp + N, tmp + 2 * (size_t)N, tmp + 3 * (size_t)N, s));
+    if (d.compact) LBB_CK(cudaMemsetAsync(tmp, 0, sizeof(double) * 4 * (size_t)N, s));   // solid nodes: zeros
+    LBB_CK(launch_batch_moments(b->d_insts, desc, batch_units(d), tmp, tmp + N, tmp + 2 * (size_t)N,
+                                tmp + 3 * (size_t)N, s));
     double *out[4] = {rho, jx, jy, jz};
     for (int q = 0; q < 4; ++q)
         LBB_CK(cudaMemcpyAsync(out[q], tmp + q * (size_t)N, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
@@ -536,7 +590,7 @@ int lbgpu_batch_mp_start(lbgpu_batch *b, int id)
     int rc = rebuild(b);
     if (rc) return rc;
     cudaStream_t s = b->stream;
-    LBB_CK(launch_batch_mp_start(b->d_insts, desc_of(b, id), sl.d.N, s));
+    LBB_CK(launch_batch_mp_start(b->d_insts, desc_of(b, id), batch_units(sl.d), s));
     unsigned st = 0;
     LBB_CK(cudaMemcpyAsync(&st, sl.d.tacc + (size_t)sl.ntile * BATCH_TACC, sizeof(st), cudaMemcpyDeviceToHost, s));
     LBB_CK(cudaStreamSynchronize(s));

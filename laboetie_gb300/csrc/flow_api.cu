@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "compact.cuh"
 #include "ctx.h"
 #include "flow.h"
 #include "lbgpu.h"
@@ -39,39 +40,15 @@ void free_op(lbgpu_ctx *ctx)
 // row bitmask table built on the host from nature; flag words gathered on the device.
 int build_compact_layout(lbgpu_ctx *ctx, const int8_t *nature)
 {
-    const int lx = ctx->p.lx, ly = ctx->p.ly, lz = ctx->p.lz, rows = ly * lz;
-    const int nw = (lx + 31) / 32;
-    auto bits = [](int n) {
-        int b = 1;
-        while ((1 << b) < n) ++b;
-        return b;
-    };
-    const int xbits = bits(lx), ybits = bits(ly), zbits = bits(lz);
-    if (xbits + ybits + zbits > 32 || (unsigned long long)rows * nw >= (1ULL << 32))
+    const int lx = ctx->p.lx, ly = ctx->p.ly, lz = ctx->p.lz;
+    std::vector<uint2> tab;
+    std::vector<uint32_t> pos;
+    int nw = 0, xbits = 0, ybits = 0;
+    if (!build_compact_tables(lx, ly, lz, nature, tab, pos, nw, xbits, ybits))
         return ctx_fail(ctx, LBGPU_ERR_INVALID,
                         "FP32 in-place streaming: box shape beyond the packed-position limits "
                         "(use LBGPU_FP32_STREAMING=ab)");
-    std::vector<uint2> tab((size_t)rows * nw);
-    std::vector<uint32_t> pos;
-    pos.reserve((size_t)ctx->counts[0]);
-    uint32_t c = 0;
-    for (int z = 0; z < lz; ++z)
-        for (int y = 0; y < ly; ++y) {
-            const size_t r = (size_t)y + (size_t)ly * z;
-            for (int w = 0; w < nw; ++w) {
-                uint32_t bm = 0;
-                const uint32_t base = c;
-                for (int b = 0; b < 32; ++b) {
-                    const int x = w * 32 + b;
-                    if (x < lx && nature[r * lx + x] == 0) {
-                        bm |= 1u << b;
-                        pos.push_back((uint32_t)x | ((uint32_t)y << xbits) | ((uint32_t)z << (xbits + ybits)));
-                        ++c;
-                    }
-                }
-                tab[r * nw + w] = make_uint2(bm, base);
-            }
-        }
+    const uint32_t c = (uint32_t)pos.size();
     ctx->Nf = c;
     ctx->nw = nw;
     ctx->xbits = xbits;

@@ -15,6 +15,7 @@
 
 #include "collide32.cuh"
 #include "common.cuh"
+#include "compact.cuh"
 #include "flow.h"
 #include "lbgpu.h"
 
@@ -38,79 +39,6 @@ __device__ __forceinline__ Coords32 coords32(unsigned node, int lx, int ly, int 
     k.Y[0] = wrap_plus(y, ly) * sy;  k.Y[1] = y * sy;  k.Y[2] = wrap_minus(y, ly) * sy;
     k.Z[0] = wrap_plus(z, lz) * sz;  k.Z[1] = z * sz;  k.Z[2] = wrap_minus(z, lz) * sz;
     return k;
-}
-
-// AA layout over the fluid nodes: compact index of the fluid node x of the lattice row whose
-// table entries start at rb, from the row's fluid bitmask word and the compact index of its
-// first fluid node.
-__device__ __forceinline__ unsigned compact_in_row(const uint2 *__restrict__ rowtab, unsigned rb, int x)
-{
-    const uint2 e = __ldg(rowtab + rb + (x >> 5));
-    return e.y + (unsigned)__popc(e.x & ((1u << (x & 31)) - 1u));
-}
-
-// Compact node position: x | y << xbits | z << (xbits + ybits) (no division to decode).
-__device__ __forceinline__ unsigned lattice_of(const FlowArgs32 &a, unsigned c)
-{
-    const unsigned x = c & ((1u << a.xbits) - 1u);
-    const unsigned y = (c >> a.xbits) & ((1u << a.ybits) - 1u);
-    const unsigned z = c >> (a.xbits + a.ybits);
-    return x + (unsigned)a.lx * (y + (unsigned)a.ly * z);
-}
-
-// Element index of the slot read for each direction by the gather of an odd AA launch at the
-// compact node i (packed position c, flag word m): slot l of the node itself across a bounce-back
-// link, else slot inv(l) of the fluid node x - c_l.  f(l, o) is called for every l.
-// Within a lattice row the fluid nodes are consecutive compact indices, so one table lookup per
-// neighbouring row gives cnt = the compact index the node x would have in that row (fluid nodes
-// before x); its neighbours x -+ 1 in the row are then cnt - 1 and cnt + fluid(x) (x - 1 and
-// x + 1 fluid), and the node's own row needs no lookup (cnt = i).  Only a wrap across the
-// periodic x boundary takes a second lookup.
-template <typename Fn>
-__device__ __forceinline__ void aa_gather_offsets(const FlowArgs32 &a, unsigned i, unsigned c,
-                                                  uint32_t m, Fn &&f)
-{
-    const int lx = a.lx, ly = a.ly, lz = a.lz, nw = a.nw;
-    const int x = (int)(c & ((1u << a.xbits) - 1u));
-    const int y = (int)((c >> a.xbits) & ((1u << a.ybits) - 1u));
-    const int z = (int)(c >> (a.xbits + a.ybits));
-    const unsigned row = (unsigned)(y + ly * z);
-    // [c+1] = row coordinate of (y - c), (z - c)
-    const int R[3] = {wrap_plus(y, ly), y, wrap_minus(y, ly)};
-    const int Z[3] = {wrap_plus(z, lz) * ly, z * ly, wrap_minus(z, lz) * ly};
-    const unsigned Nf = a.Nf;
-    const int w = x >> 5, b = x & 31;
-    const uint32_t below = (1u << b) - 1u;
-    const uint2 *__restrict__ tab = a.rowtab;
-    static_for<0, Q>([&](auto L) {
-        constexpr int l = decltype(L)::value;
-        constexpr Vel v = vel(l);
-        if constexpr (l == 0) {
-            f(0, i);
-        } else {
-            unsigned o;
-            if ((m >> l) & 1u) {
-                o = (unsigned)l * Nf + i;
-            } else {
-                unsigned s;
-                if constexpr (v.y == 0 && v.z == 0) {
-                    // own row: the fluid neighbour x - c.x is the previous / next compact node
-                    const unsigned rb = row * (unsigned)nw;
-                    if constexpr (v.x > 0) s = x > 0 ? i - 1u : compact_in_row(tab, rb, lx - 1);
-                    else s = x < lx - 1 ? i + 1u : compact_in_row(tab, rb, 0);
-                } else {
-                    const unsigned rb = (unsigned)(R[v.y + 1] + Z[v.z + 1]) * (unsigned)nw;
-                    const uint2 e = __ldg(tab + rb + w);
-                    const unsigned cnt = e.y + (unsigned)__popc(e.x & below);
-                    if constexpr (v.x == 0) s = cnt;
-                    else if constexpr (v.x > 0) s = x > 0 ? cnt - 1u : compact_in_row(tab, rb, lx - 1);
-                    else s = x < lx - 1 ? cnt + ((e.x >> b) & 1u) : compact_in_row(tab, rb, 0);
-                }
-                o = (unsigned)inv(l) * Nf + s;
-            }
-            f(l, o);
-        }
-    });
 }
 
 __device__ __forceinline__ void pull19f(float (&g)[Q], const float *__restrict__ src,

@@ -73,15 +73,16 @@ def test_no_gpu_means_a_loud_failure_not_a_cpu_fallback():
 
 
 def test_batch_footprint_and_struct_layout():
-    """lbgpu_batch_footprint is host logic: populations, flags, previous velocity and the
-    nature byte per node (256-byte aligned parts), plus the tracer buffers when Db > 0 (two more
-    float4 records per node with adsorption)."""
+    """lbgpu_batch_footprint is host logic, an upper bound over both layouts: populations, flags,
+    previous velocity and the nature byte per node, the compact-layout positions, flags and row
+    table (256-byte aligned parts), plus the tracer buffers when Db > 0 (two more float4 records
+    per node with adsorption)."""
     from laboetie_gb300.lbgpu import Cell, Request, RequestResult, footprint, make_cell
 
     assert (ctypes.sizeof(Cell), ctypes.sizeof(Request), ctypes.sizeof(RequestResult)) == (144, 200, 88)
     up = lambda x: (x + 255) // 256 * 256
     N = 1 * 50 * 50
-    base = up(76 * N) + up(4 * N) + up(16 * N) + up(N)
+    base = up(76 * N) + up(4 * N) + up(16 * N) + up(N) + 2 * up(4 * N) + up(8 * 50 * 50)
     assert footprint(make_cell((1, 50, 50))) == base
     tiles = (N + 255) // 256
     mp = 3 * up(16 * N) + up(8 * (9 * tiles + 1))
