@@ -13,6 +13,7 @@
 #include "common.cuh"
 #include "compact.cuh"
 #include "lbgpu.h"
+#include "mp_slab.cuh"
 
 namespace lbg {
 namespace {
@@ -239,7 +240,7 @@ __device__ __forceinline__ void block_sum3(double (&v)[3])
 
 __device__ __forceinline__ unsigned *status_word(const BatchInst &I)
 {
-    return reinterpret_cast<unsigned *>(I.tacc + (size_t)batch_ntile(I) * BATCH_TACC);
+    return reinterpret_cast<unsigned *>(I.tacc + (size_t)I.ntacc * BATCH_TACC);
 }
 
 // Velocity u = j/rho of a node in natural order (after an even number of AA launches); g holds
@@ -367,6 +368,32 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
     }
     if constexpr (INIT) {
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status_word(I), (unsigned)LBGPU_ERR_FRACTION);
+    }
+}
+
+// One tracer step of the slab tiles of boxes in the tracer phase (mp_slab.cuh); each tile keeps
+// its own running sums.
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_slab(const BatchInst *__restrict__ insts,
+                                                               const BatchTile *__restrict__ tiles, int par)
+{
+    extern __shared__ float4 sm4[];
+    const BatchTile t = tiles[blockIdx.x];
+    const BatchInst &I = insts[t.inst];
+    const int tiles_x = (I.lx + MPS_TX - 1) / MPS_TX, tiles_y = (I.ly + MPS_TY - 1) / MPS_TY;
+    const int nxy = tiles_x * tiles_y;
+    const int tile = t.start % nxy, chunk = t.start / nxy;
+    const int z0 = chunk * I.zc;
+    float vt[3] = {0.0f, 0.0f, 0.0f};
+    mp_slab_sweep(I, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + I.zc, I.lz),
+                  sm4, vt);
+    double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
+    block_sum3(v);
+    if (threadIdx.x == 0) {
+        double *acc = I.tacc + (size_t)t.start * BATCH_TACC;
+        for (int d = 0; d < 3; ++d) {
+            acc[3 + d] += v[d];
+            acc[6 + d] = v[d];
+        }
     }
 }
 
@@ -537,6 +564,14 @@ cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int 
 {
     if (ntiles <= 0) return cudaSuccess;
     k_batch_mp<false><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles, 0, par);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_mp_slab(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
+                                 cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    k_batch_mp_slab<<<ntiles, BATCH_BLOCK, MPS_SMEM, s>>>(insts, tiles, par);
     return cudaGetLastError();
 }
 

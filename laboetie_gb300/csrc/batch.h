@@ -48,6 +48,10 @@ struct BatchInst {
     int nw, xbits, ybits;
     const uint32_t *cpos, *cmask;
     const uint2 *rowtab;
+    // tracer phase of a tiled box with lx >= 32, ly >= 8, lz >= 3: shared-memory slab tiles of
+    // 32 x 8 columns and zc planes (mp_slab.cuh); 0 otherwise
+    int zc;
+    int ntacc;              // tiles with VACF accumulators in tacc (the status word follows)
 };
 
 // Nodes a box's kernels iterate (compact fluid nodes or lattice nodes) and its 256-node tiles.
@@ -64,6 +68,16 @@ cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int 
 // one tracer step of the tiled boxes: P[par] -> P[par^1]
 cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
                             cudaStream_t s);
+// the same for boxes with slab tiles (tile start = slab tile index within the box)
+cudaError_t launch_batch_mp_slab(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
+                                 cudaStream_t s);
+constexpr int BATCH_SLAB_ZC = 16;   // planes per slab tile
+// slab tiles of a box (0: not eligible)
+__host__ __device__ inline int batch_slab_tiles(int lx, int ly, int lz)
+{
+    if (lx < 32 || ly < 8 || lz < 3) return 0;
+    return ((lx + 31) / 32) * ((ly + 7) / 8) * ((lz + BATCH_SLAB_ZC - 1) / BATCH_SLAB_ZC);
+}
 // du: one word per descriptor, max |u - u_prev| of the check as IEEE bits (non-negative)
 cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist, int nsteps,
                               bool check, unsigned *du, int smem_bytes, int threads,

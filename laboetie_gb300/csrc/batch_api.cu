@@ -40,7 +40,7 @@ struct Slot {
     size_t bytes = 0;
     bool smem = false;        // stepped with the whole box in shared memory (lattice layout)
     bool tracer = false;
-    int ntile = 0;            // 256-node tiles of the box's layout
+    int ntile = 0;            // tiles with VACF accumulators (256-node tiles or slab tiles)
     int mp_steps = 0;
 };
 
@@ -66,7 +66,8 @@ struct Layout {
     size_t g, mask, uprev, nature, cpos, cmask, rowtab, V, P0, P1, A0, A1, tacc, total;
 };
 
-Layout layout(long long N, long long units, long long tab, bool compact, bool tracer, bool ads)
+Layout layout(long long N, long long units, long long tab, long long ntacc, bool compact, bool tracer,
+              bool ads)
 {
     Layout L{};
     size_t o = 0;
@@ -88,8 +89,7 @@ Layout layout(long long N, long long units, long long tab, bool compact, bool tr
             L.A0 = o; o += f4;
             L.A1 = o; o += f4;
         }
-        const size_t ntile = ((size_t)units + BATCH_BLOCK - 1) / BATCH_BLOCK;
-        L.tacc = o; o += up(sizeof(double) * (ntile * BATCH_TACC + 1));
+        L.tacc = o; o += up(sizeof(double) * ((size_t)ntacc * BATCH_TACC + 1));
     }
     L.total = o;
     return L;
@@ -100,7 +100,8 @@ Layout layout(long long N, long long units, long long tab, bool compact, bool tr
 size_t footprint_bound(long long N, int lx, int ly, int lz, bool tracer, bool ads)
 {
     const long long tab = (long long)ly * lz * ((lx + 31) / 32);
-    return layout(N, N, tab, true, tracer, ads).total;
+    const long long ntacc = std::max<long long>((N + BATCH_BLOCK - 1) / BATCH_BLOCK, batch_slab_tiles(lx, ly, lz));
+    return layout(N, N, tab, ntacc, true, tracer, ads).total;
 }
 
 }  // namespace
@@ -117,8 +118,8 @@ struct lbgpu_batch {
     bool dirty = true;
     BatchInst *d_insts = nullptr;
     int cap_insts = 0;
-    BatchTile *d_tiles = nullptr;   // flow tiles, then tracer tiles
-    int cap_tiles = 0, nflow = 0, nmp = 0;
+    BatchTile *d_tiles = nullptr;   // flow tiles, then tracer tiles, then tracer slab tiles
+    int cap_tiles = 0, nflow = 0, nmp = 0, nslab = 0;
     int *d_smem = nullptr;
     int cap_smem = 0, nsmem = 0, smem_bytes = 0, smem_threads = BATCH_SMEM_THREADS;
     unsigned *d_du = nullptr;
@@ -197,7 +198,7 @@ int rebuild(lbgpu_batch *b)
     cudaStream_t s = b->stream;
     drop_graphs(b);
     std::vector<BatchInst> descs;
-    std::vector<BatchTile> flow, mp;
+    std::vector<BatchTile> flow, mp, slab;
     std::vector<int> smem;
     b->desc_slot.clear();
     int smem_bytes = 0;
@@ -211,6 +212,9 @@ int rebuild(lbgpu_batch *b)
             smem.push_back(id);
             smem_bytes = std::max(smem_bytes, sl.d.phase == BATCH_FLOW ? batch_smem_flow(sl.d.N)
                                                                        : batch_smem_mp(sl.d.N, sl.d.ads));
+        } else if (sl.d.phase == BATCH_MP && sl.d.zc > 0) {
+            const int n = batch_slab_tiles(sl.d.lx, sl.d.ly, sl.d.lz);
+            for (int k = 0; k < n; ++k) slab.push_back({id, k});
         } else {
             auto &list = sl.d.phase == BATCH_FLOW ? flow : mp;
             const int units = (int)batch_units(sl.d);
@@ -219,6 +223,7 @@ int rebuild(lbgpu_batch *b)
     }
     std::vector<BatchTile> tiles(flow);
     tiles.insert(tiles.end(), mp.begin(), mp.end());
+    tiles.insert(tiles.end(), slab.begin(), slab.end());
     int rc;
     if ((rc = grow(&b->d_insts, b->cap_insts, (int)descs.size(), s))) return rc;
     if ((rc = grow(&b->d_tiles, b->cap_tiles, (int)tiles.size(), s))) return rc;
@@ -233,6 +238,7 @@ int rebuild(lbgpu_batch *b)
     LBB_CK(cudaStreamSynchronize(s));  // host vectors above go out of scope
     b->nflow = (int)flow.size();
     b->nmp = (int)mp.size();
+    b->nslab = (int)slab.size();
     b->nsmem = (int)smem.size();
     b->smem_bytes = smem_bytes;
     b->dirty = false;
@@ -255,6 +261,7 @@ int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
     for (int t = 0; t < nsteps; ++t) {
         LBB_CK(launch_batch_aa(b->d_insts, b->d_tiles, b->nflow, t & 1, s));
         LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
+        LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, s));
     }
     if (check) LBB_CK(launch_batch_check(b->d_insts, b->d_tiles, b->nflow, b->d_du, s));
     if (b->nsmem) LBB_CK(cudaStreamWaitEvent(s, b->join, 0));
@@ -425,13 +432,15 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
         return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: box shape beyond the packed-position limits");
     if (compact && pos.empty()) return bfail(LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
     const long long units = compact ? (long long)pos.size() : N;
-    const Layout L = layout(N, units, (long long)tab.size(), compact, tracer, ads);
+    const int nslab = compact && tracer ? batch_slab_tiles(c->lx, c->ly, c->lz) : 0;
+    const int ntacc = std::max((int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK), nslab);
+    const Layout L = layout(N, units, (long long)tab.size(), ntacc, compact, tracer, ads);
     if (b->used + L.total > b->budget)
         return bfail(LBGPU_ERR_OOM, "lbgpu_batch_add: box needs " + std::to_string(L.total >> 20) +
                                         " MiB beyond the batch memory budget");
     cudaStream_t s = b->stream;
     sl.bytes = L.total;
-    sl.ntile = (int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK);
+    sl.ntile = ntacc;
     LBB_CK(cudaMallocAsync(&sl.mem, L.total, s));
     char *base = static_cast<char *>(sl.mem);
     BatchInst &d = sl.d;
@@ -442,6 +451,8 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
     d.N = (int)N;
     d.phase = BATCH_FLOW;
     d.ads = ads ? 1 : 0;
+    d.zc = nslab ? BATCH_SLAB_ZC : 0;
+    d.ntacc = ntacc;
     fill_consts(d, *c);
     d.g = reinterpret_cast<float *>(base + L.g);
     uint32_t *mask = reinterpret_cast<uint32_t *>(base + L.mask);

@@ -1,0 +1,17 @@
+// cpasync.cuh -- 16-byte asynchronous global -> shared copies (cp.async, cached in L2 only) and
+// their group fences.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace lbg {
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+}  // namespace lbg

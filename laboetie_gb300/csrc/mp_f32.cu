@@ -10,8 +10,10 @@
 // Solid neighbours hold V = 0 and P = 0 and their links are masked to zero, so the gathers are
 // branch-free and can all be in flight at once.
 #include "common.cuh"
+#include "cpasync.cuh"
 #include "lbgpu.h"
 #include "mp.h"
+#include "mp_slab.cuh"
 #include "reduce.cuh"
 
 namespace lbg {
@@ -131,108 +133,20 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
     }
 }
 
-// 16-byte asynchronous global -> shared copies (cp.async, L2 only) and their group fences.
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-constexpr int SHX = MPS_TX + 2, SHY = MPS_TY + 2, SPL = SHX * SHY;  // a plane with its halo
-constexpr size_t MPS_SMEM = sizeof(float4) * 8 * SPL;                // 4 planes of V and of P
-
-// One tracer step (the flux form of k_mp32, same operations in the same order, so P is
-// bit-identical) with V and P staged in shared memory: a block owns a 32 x 8 column tile and a
-// chunk of zc planes; a ring of 4 planes (z-1, z, z+1 and the one being fetched) is filled by
-// asynchronous copies one plane ahead, so the 36 neighbour reads per node are shared-memory
-// reads and every V and P value is fetched from L2/HBM about 1.3 times (halo) per step.  One
-// block barrier per plane: after it, plane z+1 is in shared memory and every thread is done with
-// plane z-1's iteration, so the fetch of plane z+2 may overwrite the slot of plane z-2.
+// One tracer step of a box with V and P staged in shared memory (mp_slab.cuh): a block owns a
+// 32 x 8 column tile and a chunk of zc planes.
 __global__ void __launch_bounds__(MP_BLOCK) k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc)
 {
     const volatile MpCtl *vc = a.ctl;
     if (vc->done) return;
     const int par = vc->parity;
     extern __shared__ float4 sm4[];
-    float4 *sV = sm4, *sP = sm4 + 4 * SPL;
-    const int lx = a.lx, ly = a.ly, lz = a.lz;
     const int nxy = tiles_x * tiles_y;
     const int tile = (int)blockIdx.x % nxy, chunk = (int)blockIdx.x / nxy;
-    const int x0 = (tile % tiles_x) * MPS_TX, y0 = (tile / tiles_x) * MPS_TY;
-    const int z0 = chunk * zc, z1 = min(z0 + zc, lz);
-    const float4 *__restrict__ Vg = a.V;
-    const float4 *__restrict__ Pg = a.P[par];
-    auto load_plane = [&](int zz) {
-        const int gz = zz < 0 ? zz + lz : (zz >= lz ? zz - lz : zz);
-        float4 *dv = sV + ((zz - z0 + 1) & 3) * SPL, *dp = sP + ((zz - z0 + 1) & 3) * SPL;
-        for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
-            const int hx = k % SHX, hy = k / SHX;
-            int gx = x0 + hx - 1, gy = y0 + hy - 1;
-            gx = gx < 0 ? gx + lx : (gx >= lx ? gx - lx : gx);   // lx >= 32: one wrap at most
-            gy = gy < 0 ? gy + ly : (gy >= ly ? gy - ly : gy);   // ly >= 8
-            const size_t idx = (size_t)gx + (size_t)lx * ((size_t)gy + (size_t)ly * gz);
-            cp_async16(dv + k, Vg + idx);
-            cp_async16(dp + k, Pg + idx);
-        }
-        cp_async_commit();
-    };
-    const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool col = x < lx && y < ly;
+    const int z0 = chunk * zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    load_plane(z0 - 1);
-    load_plane(z0);
-    load_plane(z0 + 1);
-    for (int z = z0; z < z1; ++z) {
-        cp_async_wait0();
-        __syncthreads();
-        if (z + 2 <= z1) load_plane(z + 2);
-        const size_t r = (size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z);
-        const uint32_t m = col ? __ldg(a.mask + r) : 0u;
-        if (m & FLUID_BIT) {
-            const int c0 = (ty + 1) * SHX + (tx + 1);
-            const int s0 = (z - z0 + 1) & 3;
-            const float4 vr = sV[s0 * SPL + c0];
-            const float4 p = sP[s0 * SPL + c0];
-            float ux = 0.0f, uy = 0.0f, uz = 0.0f;
-            float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
-            static_for<1, Q>([&](auto L) {
-                constexpr int l = decltype(L)::value;
-                constexpr Vel c = vel(l);
-                constexpr int w = wclass(l);
-                const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
-                const int q = ((z + c.z - z0 + 1) & 3) * SPL + c0 + c.y * SHX + c.x;
-                const float4 vn = sV[q];
-                const float sp = on * (a.a1[w] * cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
-                const float spp = on * (a.a1[w] * cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
-                ux += c.x * sp;
-                uy += c.y * sp;
-                uz += c.z * sp;
-                const float4 pn = sP[q];
-                n0 += pn.x * spp - p.x * sp;
-                n1 += pn.y * spp - p.y * sp;
-                n2 += pn.z * spp - p.z * sp;
-            });
-            vt[0] += p.x * ux;
-            vt[1] += p.y * uy;
-            vt[2] += p.z * uz;
-            n0 += p.x;
-            n1 += p.y;
-            n2 += p.z;
-            if (a.ads && (m & INTERFACIAL_BIT)) {
-                const float4 qa = a.A[par][r];
-                n0 += qa.x * a.kd - a.ka * p.x;
-                n1 += qa.y * a.kd - a.ka * p.y;
-                n2 += qa.z * a.kd - a.ka * p.z;
-                a.A[par ^ 1][r] = make_float4(qa.x * a.one_minus_kd + p.x * a.ka,
-                                              qa.y * a.one_minus_kd + p.y * a.ka,
-                                              qa.z * a.one_minus_kd + p.z * a.ka, 0.0f);
-            }
-            __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
-        }
-    }
+    mp_slab_sweep(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
+                  sm4, vt);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     grid_sum3(v, a.partial, &a.ctl->blocks_done,
               [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });

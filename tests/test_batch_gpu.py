@@ -19,12 +19,14 @@ TR = dict(Db=0.01, ka=0.01 * math.e, kd=0.01)
 
 
 def _cells():
-    """Two shared-memory-sized chromatography cells, a slit and a tiled tube."""
+    """Two shared-memory-sized chromatography cells, a slit, a tiled tube and a tiled tube wide
+    enough for the tracer's shared-memory slab tiles."""
     return [
         (geo.chromatography_cell(seed=3), (0.0, 0.0, 1e-5)),
         (geo.chromatography_cell(seed=8), (0.0, 0.0, 1e-5)),
         (geo.slit(4, 4, 34), (1e-5, 0.0, 0.0)),
         (geo.modulated_tube(40, n=16, r_mean=5.0, r_amp=2.0), (0.0, 0.0, 1e-5)),
+        (geo.modulated_tube(36, n=32, r_mean=9.0, r_amp=3.0), (0.0, 0.0, 1e-5)),
     ]
 
 
@@ -102,12 +104,17 @@ def test_batch_flow_reaches_the_fp64_steady_state(oracle_mod):
     assert np.max(np.abs(rho[fl] - ref["rho"][fl])) < 1e-5
 
 
-def test_batch_tracer_matches_single_box_fp32():
+@pytest.mark.parametrize("make,fe", [
+    (lambda: geo.slit(4, 4, 34), (1e-5, 0.0, 0.0)),                                   # shared memory
+    (lambda: geo.modulated_tube(48, n=32, r_mean=10.0, r_amp=4.0), (0.0, 0.0, 1e-5)),  # slab tiles
+])
+def test_batch_tracer_matches_single_box_fp32(make, fe):
     """Given the batch's own flow moments, the single-box FP32 propagation computes the same V
-    and P step for step; VACF(0) and the Green-Kubo sum agree to 1e-12 relative (they differ
-    only in the order of the FP64 node sums)."""
-    nat = geo.slit(4, 4, 34)
-    fe = (1e-5, 0.0, 0.0)
+    and P step for step.  VACF(0) agrees to 1e-12 relative (FP64 sums of the same per-node
+    terms in another order); the per-step VACF is summed per thread in FP32 over a few nodes
+    before the FP64 sums, and the kernels group the nodes differently, so the VACF sums agree to
+    1e-6 of the summed magnitudes."""
+    nat = make()
     K = 400
     with Batch() as b:
         box = b.add(nat, f_ext=fe, tracer=dict(TR, f_ext=fe))
@@ -123,8 +130,8 @@ def test_batch_tracer_matches_single_box_fp32():
     assert len(vac) == K
     scale = np.abs(s0).max()
     assert np.max(np.abs(v0 - s0)) <= 1e-12 * scale
-    assert np.max(np.abs(vs - vac.sum(axis=0))) <= 1e-12 * scale * 10
-    assert np.max(np.abs(vl - vac[-1])) <= 1e-12 * scale
+    assert np.all(np.abs(vs - vac.sum(axis=0)) <= 1e-6 * np.abs(vac).sum(axis=0))
+    assert np.all(np.abs(vl - vac[-1]) <= 1e-6 * np.abs(vac[-1]) + 1e-18)
 
 
 def test_batch_refusals():
