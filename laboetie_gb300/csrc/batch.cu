@@ -86,17 +86,18 @@ __device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uin
 }
 
 // One AA update of the compact node i of a box in the fluid-only layout (compact.cuh).  A thread
-// writes exactly the slots it read, so the read-only cache path is safe for the loads.
+// writes exactly the slots it read, so the read-only cache path is safe for the loads.  Odd
+// launches park the slot of each direction in shared memory ([l][thread], conflict-free) so that
+// it does not occupy registers across the collision.
 template <bool ODD>
-__device__ __forceinline__ void aa_node_compact(const BatchInst &I, unsigned i)
+__device__ __forceinline__ void aa_node_compact(const BatchInst &I, unsigned i, unsigned (*soff)[BATCH_BLOCK])
 {
     float *g = I.g;
     const unsigned Nf = I.Nf;
     float f[Q];
-    unsigned off[Q];
     if constexpr (ODD) {
         aa_gather_offsets(I, i, __ldg(I.cpos + i), __ldg(I.cmask + i), [&](int l, unsigned o) {
-            off[l] = o;
+            soff[l][threadIdx.x] = o;
             f[l] = __ldg(g + o);
         });
     } else {
@@ -106,7 +107,7 @@ __device__ __forceinline__ void aa_node_compact(const BatchInst &I, unsigned i)
     aa_collide(f, I);
     if constexpr (ODD) {
 #pragma unroll
-        for (int l = 0; l < Q; ++l) g[off[inv(l)]] = f[l];
+        for (int l = 0; l < Q; ++l) g[soff[inv(l)][threadIdx.x]] = f[l];
     } else {
 #pragma unroll
         for (int l = 0; l < Q; ++l) g[(unsigned)inv(l) * Nf + i] = f[l];
@@ -301,22 +302,17 @@ __device__ __forceinline__ void node_moments64(const BatchInst &I, unsigned node
     rho = (double)I.rho0 + d;
 }
 
-template <bool ODD>
-__global__ void __launch_bounds__(BATCH_BLOCK, 3) k_batch_aa(const BatchInst *__restrict__ insts,
-                                                             const BatchTile *__restrict__ tiles)
+// One AA launch over the tiles of the tiled boxes (always in the compact layout); MINB resident
+// blocks per SM (3..6, picked by the tuner in batch_api.cu).
+template <bool ODD, int MINB>
+__global__ void __launch_bounds__(BATCH_BLOCK, MINB) k_batch_aa(const BatchInst *__restrict__ insts,
+                                                                const BatchTile *__restrict__ tiles)
 {
+    __shared__ unsigned soff[ODD ? Q : 1][BATCH_BLOCK];
     const BatchTile t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
-    const unsigned node = (unsigned)t.start + threadIdx.x;
-    if (I.compact) {
-        if (node < I.Nf) aa_node_compact<ODD>(I, node);
-        return;
-    }
-    const unsigned N = (unsigned)I.N;
-    if (node >= N) return;
-    const uint32_t m = __ldg(I.mask + node);
-    if (!(m & FLUID_BIT)) return;
-    aa_node<ODD>(I.g, N, node, m, I);
+    const unsigned i = (unsigned)t.start + threadIdx.x;
+    if (i < I.Nf) aa_node_compact<ODD>(I, i, soff);
 }
 
 // One tracer step of every tiled box in the tracer phase; with INIT (one box, the tiles of
@@ -513,12 +509,8 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_check(const BatchInst *__
     const BatchTile t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
     const unsigned node = (unsigned)t.start + threadIdx.x;
-    float du = 0.0f;
-    if (I.compact) {
-        if (node < I.Nf) du = du_and_store(I.uprev, node, node_velocity(I.g, I.Nf, node, I));
-    } else if (node < (unsigned)I.N && (I.mask[node] & FLUID_BIT)) {
-        du = du_and_store(I.uprev, node, node_velocity(I.g, (unsigned)I.N, node, I));
-    }
+    float du = 0.0f;   // tiled boxes are in the compact layout: every node is fluid
+    if (node < I.Nf) du = du_and_store(I.uprev, node, node_velocity(I.g, I.Nf, node, I));
     for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
     if ((threadIdx.x & 31) == 0) atomicMax(du_out + t.inst, __float_as_uint(du));
 }
@@ -550,12 +542,21 @@ cudaError_t batch_configure(int max_smem_bytes)
     return cudaFuncSetAttribute(k_batch_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
 }
 
-cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd,
+template <int MINB>
+static void batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, cudaStream_t s)
+{
+    if (odd) k_batch_aa<true, MINB><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
+    else k_batch_aa<false, MINB><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
+}
+
+cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int minb,
                             cudaStream_t s)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (odd) k_batch_aa<true><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
-    else k_batch_aa<false><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles);
+    if (minb <= 3) batch_aa<3>(insts, tiles, ntiles, odd, s);
+    else if (minb == 4) batch_aa<4>(insts, tiles, ntiles, odd, s);
+    else if (minb == 5) batch_aa<5>(insts, tiles, ntiles, odd, s);
+    else batch_aa<6>(insts, tiles, ntiles, odd, s);
     return cudaGetLastError();
 }
 

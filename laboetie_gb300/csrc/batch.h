@@ -63,7 +63,8 @@ struct BatchTile {
     int start;  // first node of the tile
 };
 
-cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd,
+// one AA launch over the tiles of the tiled boxes (compact layout); minb: 3..6 resident blocks
+cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int minb,
                             cudaStream_t s);
 // one tracer step of the tiled boxes: P[par] -> P[par^1]
 cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,

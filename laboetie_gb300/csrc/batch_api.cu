@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
@@ -124,6 +125,8 @@ struct lbgpu_batch {
     int cap_smem = 0, nsmem = 0, smem_bytes = 0, smem_threads = BATCH_SMEM_THREADS;
     unsigned *d_du = nullptr;
     int cap_du = 0;
+    int aa_minb[2] = {4, 5};      // resident blocks per SM of the even / odd AA launches
+    bool aa_tuned = false;
     std::vector<int> desc_slot;   // descriptor index -> slot
     std::vector<GraphEntry> graphs;
 };
@@ -259,7 +262,7 @@ int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
         LBB_CK(cudaEventRecord(b->join, b->side));
     }
     for (int t = 0; t < nsteps; ++t) {
-        LBB_CK(launch_batch_aa(b->d_insts, b->d_tiles, b->nflow, t & 1, s));
+        LBB_CK(launch_batch_aa(b->d_insts, b->d_tiles, b->nflow, t & 1, b->aa_minb[t & 1], s));
         LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
         LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, s));
     }
@@ -300,8 +303,73 @@ int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
     return LBGPU_OK;
 }
 
+// Launch-bound tuner of the tiled AA launches: the first time a batch holds at least 1024 flow
+// tiles, every variant (3..6 resident blocks per SM) of the even and of the odd launch is timed
+// on scratch copies of the tiled boxes' populations (a second descriptor table points at them;
+// the boxes' state is not advanced) and the fastest is kept for the batch's lifetime.
+// LBGPU_BATCH_AA_MINB=<even>,<odd> fixes the variants instead.
+int tune_aa(lbgpu_batch *b)
+{
+    if (b->aa_tuned || b->nflow < 1024) return LBGPU_OK;
+    b->aa_tuned = true;
+    if (const char *e = std::getenv("LBGPU_BATCH_AA_MINB")) {
+        int ev = 0, od = 0;
+        if (std::sscanf(e, "%d,%d", &ev, &od) == 2) {
+            b->aa_minb[0] = ev;
+            b->aa_minb[1] = od;
+            return LBGPU_OK;
+        }
+    }
+    cudaStream_t s = b->stream;
+    std::vector<BatchInst> descs(b->desc_slot.size());
+    size_t total = 0;
+    for (size_t i = 0; i < descs.size(); ++i) {
+        descs[i] = b->slots[b->desc_slot[i]].d;
+        if (!descs[i].compact || descs[i].phase != BATCH_FLOW) continue;
+        total += (size_t)Q * descs[i].Nf;
+    }
+    float *scratch = nullptr;
+    BatchInst *d_tmp = nullptr;
+    if (cudaMallocAsync(&scratch, sizeof(float) * total, s) != cudaSuccess ||
+        cudaMallocAsync(&d_tmp, sizeof(BatchInst) * descs.size(), s) != cudaSuccess) {
+        cudaGetLastError();   // no room: keep the default variants
+        if (scratch) cudaFreeAsync(scratch, s);
+        return LBGPU_OK;
+    }
+    size_t off = 0;
+    for (auto &d : descs) {
+        if (!d.compact || d.phase != BATCH_FLOW) continue;
+        LBB_CK(cudaMemcpyAsync(scratch + off, d.g, sizeof(float) * Q * d.Nf, cudaMemcpyDeviceToDevice, s));
+        d.g = scratch + off;
+        off += (size_t)Q * d.Nf;
+    }
+    LBB_CK(cudaMemcpyAsync(d_tmp, descs.data(), sizeof(BatchInst) * descs.size(), cudaMemcpyHostToDevice, s));
+    for (int odd = 0; odd < 2; ++odd) {
+        float best = 1e30f;
+        for (int minb = 3; minb <= 6; ++minb) {
+            for (int k = 0; k < 2; ++k) LBB_CK(launch_batch_aa(d_tmp, b->d_tiles, b->nflow, odd, minb, s));
+            LBB_CK(cudaEventRecord(b->ev0, s));
+            for (int k = 0; k < 6; ++k) LBB_CK(launch_batch_aa(d_tmp, b->d_tiles, b->nflow, odd, minb, s));
+            LBB_CK(cudaEventRecord(b->ev1, s));
+            LBB_CK(cudaEventSynchronize(b->ev1));
+            float ms = 0.0f;
+            LBB_CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            if (ms < best) {
+                best = ms;
+                b->aa_minb[odd] = minb;
+            }
+        }
+    }
+    LBB_CK(cudaFreeAsync(scratch, s));
+    LBB_CK(cudaFreeAsync(d_tmp, s));
+    LBB_CK(cudaStreamSynchronize(s));   // descs go out of scope
+    drop_graphs(b);                     // graphs captured with the previous variants
+    return LBGPU_OK;
+}
+
 int run_steps(lbgpu_batch *b, int nsteps, bool check)
 {
+    if (int rc = tune_aa(b)) return rc;
     cudaGraphExec_t exec = nullptr;
     int rc = graph_of(b, nsteps, check, &exec);
     if (rc) return rc;
@@ -560,7 +628,8 @@ int lbgpu_batch_time_steps(lbgpu_batch *b, int nsteps, float *ms)
     if (rc) return rc;
     const bool work = !b->desc_slot.empty() && nsteps > 0;
     cudaGraphExec_t exec = nullptr;
-    if (work && (rc = graph_of(b, nsteps, false, &exec))) return rc;   // outside the timed region
+    if ((rc = tune_aa(b))) return rc;                                    // outside the timed region
+    if (work && (rc = graph_of(b, nsteps, false, &exec))) return rc;
     LBB_CK(cudaEventRecord(b->ev0, b->stream));
     if (work && (rc = run_steps(b, nsteps, false))) return rc;
     LBB_CK(cudaEventRecord(b->ev1, b->stream));
