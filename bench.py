@@ -339,7 +339,7 @@ def bench_batched(a):
     # one at a time through the single-box API: a sample of each family, extrapolated
     fam = {"cell": [], "tube": []}
     ns = a.one_at_a_time_sample
-    sample = [c for c in cells if c[2] == "cell"][:ns] + [c for c in cells if c[2] == "tube"][:max(1, ns // 3)]
+    sample = [c for c in cells if c[2] == "cell"][:ns] + [c for c in cells if c[2] == "tube"][:(max(1, ns // 3) if ns else 0)]
     for n, fe, f in sample:
         nf = int((n == 0).sum())
         t = time.perf_counter()
@@ -357,6 +357,13 @@ def bench_batched(a):
         rate = sum(x[1] for x in fam[f]) / sum(x[0] for x in fam[f])   # fluid nodes per second
         t_one += tot_nf / rate
     n_solves = len(cells)
+    one = None
+    if t_one > 0:
+        one = {"value": round(n_solves / t_one, 3), "unit": "solves/s",
+               "sample": f"{len(fam['cell'])} cells + {len(fam['tube'])} tubes timed through "
+                         "lbgpu_flow_steps/lbgpu_mp_propagate one box at a time, "
+                         "extrapolated per family by fluid nodes",
+               "seconds_extrapolated": round(t_one, 2)}
     return {
         "metric": "batched solves/s", "value": round(n_solves / dt, 3), "unit": "solves/s",
         "seconds": round(dt, 3), "solves": n_solves,
@@ -367,12 +374,8 @@ def bench_batched(a):
                    "flow_steps": KF, "mp_steps": KM, "steps_per_graph": CH,
                    "tracer": "Db 0.01, K = e (kd 0.01)", "fluid_nodes": info["fluid_nodes"],
                    "smem_boxes": info["smem_boxes"], "bytes": info["bytes"]},
-        "one_at_a_time": {"value": round(n_solves / t_one, 3), "unit": "solves/s",
-                          "sample": f"{len(fam['cell'])} cells + {len(fam['tube'])} tubes timed through "
-                                    "lbgpu_flow_steps/lbgpu_mp_propagate one box at a time, "
-                                    "extrapolated per family by fluid nodes",
-                          "seconds_extrapolated": round(t_one, 2)},
-        "speedup_vs_one_at_a_time": round(t_one / dt, 2),
+        "one_at_a_time": one,
+        "speedup_vs_one_at_a_time": round(t_one / dt, 2) if one else None,
         "d_eff_cell0": deff_cell0,
     }
 

@@ -41,19 +41,16 @@ __device__ __forceinline__ void aa_collide(float (&f)[Q], const BatchInst &I)
     collide_dev<7>(f, drho, jx, jy, jz, I, I.force != 0);
 }
 
-// One AA update of one fluid node of a box in the lattice layout whose populations start at g
-// (global or shared).
+// One AA update of one fluid node (x, y, z) of a box in the lattice layout whose populations
+// start at g (global or shared).
 template <bool ODD>
-__device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uint32_t m,
-                                        const BatchInst &I)
+__device__ __forceinline__ void aa_node(float *g, unsigned N, unsigned node, uint32_t m, int x, int y,
+                                        int z, const BatchInst &I)
 {
     float f[Q];
     unsigned off[Q];
     if constexpr (ODD) {
         const int lx = I.lx, ly = I.ly, lz = I.lz;
-        const int x = (int)(node % (unsigned)lx);
-        const unsigned yz = node / (unsigned)lx;
-        const int y = (int)(yz % (unsigned)ly), z = (int)(yz / (unsigned)ly);
         const int sy = lx, sz = lx * ly;
         // [c+1] = coordinate of (x - c)
         const int X[3] = {wrap_plus(x, lx), x, wrap_minus(x, lx)};
@@ -216,6 +213,34 @@ __device__ __forceinline__ unsigned compact_xyz(const BatchInst &I, unsigned c, 
     z = (int)(c >> (I.xbits + I.ybits));
     return (unsigned)x + (unsigned)I.lx * ((unsigned)y + (unsigned)I.ly * (unsigned)z);
 }
+
+// Coordinates of the nodes threadIdx.x, threadIdx.x + T, threadIdx.x + 2T, ... of a box, advanced
+// by additions (one division per walk instead of two per node).
+struct NodeWalk {
+    int x, y, z, dx, dy, dz, lx, ly;
+    __device__ __forceinline__ NodeWalk(const BatchInst &I, unsigned T) : lx(I.lx), ly(I.ly)
+    {
+        lattice_xyz(I, threadIdx.x, x, y, z);
+        dx = (int)(T % (unsigned)lx);
+        const unsigned q = T / (unsigned)lx;
+        dy = (int)(q % (unsigned)ly);
+        dz = (int)(q / (unsigned)ly);
+    }
+    __device__ __forceinline__ void next()
+    {
+        x += dx;
+        y += dy;
+        z += dz;
+        if (x >= lx) {
+            x -= lx;
+            ++y;
+        }
+        if (y >= ly) {
+            y -= ly;
+            ++z;
+        }
+    }
+};
 
 // Sum of 3 doubles over the block in a fixed order (lanes by shuffle tree, then warps in index
 // order); valid in thread 0.  Any block size that is a multiple of 32, up to 1024.
@@ -432,11 +457,12 @@ __global__ void __launch_bounds__(BATCH_SMEM_THREADS) k_batch_smem(const BatchIn
         for (unsigned i = threadIdx.x; i < N; i += T) msk[i] = I.mask[i];
         __syncthreads();
         for (int s = 0; s < nsteps; ++s) {
-            for (unsigned node = threadIdx.x; node < N; node += T) {
+            NodeWalk w(I, T);
+            for (unsigned node = threadIdx.x; node < N; node += T, w.next()) {
                 const uint32_t m = msk[node];
                 if (!(m & FLUID_BIT)) continue;
-                if (s & 1) aa_node<true>(g, N, node, m, I);
-                else aa_node<false>(g, N, node, m, I);
+                if (s & 1) aa_node<true>(g, N, node, m, w.x, w.y, w.z, I);
+                else aa_node<false>(g, N, node, m, w.x, w.y, w.z, I);
             }
             __syncthreads();
         }
@@ -474,13 +500,10 @@ __global__ void __launch_bounds__(BATCH_SMEM_THREADS) k_batch_smem(const BatchIn
         const float4 *Pn = odd ? P1 : P0, *An = odd ? A1 : A0;
         float4 *Px = odd ? P0 : P1, *Ax = odd ? A0 : A1;
         double vt[3] = {0.0, 0.0, 0.0};
-        for (unsigned node = threadIdx.x; node < N; node += T) {
+        NodeWalk w(I, T);
+        for (unsigned node = threadIdx.x; node < N; node += T, w.next()) {
             const uint32_t m = msk[node];
-            if (m & FLUID_BIT) {
-                int x, y, z;
-                lattice_xyz(I, node, x, y, z);
-                mp_node<false>(V, Pn, Px, An, Ax, node, x, y, z, m, I, vt, bad);
-            }
+            if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, node, w.x, w.y, w.z, m, I, vt, bad);
         }
         block_sum3(vt);  // its barriers also separate this step from the next
         if (threadIdx.x == 0)
