@@ -156,6 +156,13 @@ int lbgpu_compensated_force_field(lbgpu_ctx *ctx, int particle_diameter,
  * uniform f_ext on fluid nodes (FP64 contexts).  All three NULL: back to the uniform f_ext. */
 int lbgpu_set_force_field(lbgpu_ctx *ctx, const double *fx, const double *fy, const double *fz);
 
+/* The reference's profile output (equilibration.f90:154-176 every print_files_frequency steps,
+ * 499-516 at exit), reduced on the device from the current flow state: for each plane normal to
+ * axis (0 = x, 1 = y, 2 = z; L = lx, ly or lz planes), flux[3k..3k+2] = SUM of jx, jy, jz over
+ * the plane and mean_density[k] = SUM(density)/MAX(COUNT(density > epsilon), 1), summed in the
+ * Fortran SUM order (bit-identical to the reference on the same state). */
+int lbgpu_profiles(lbgpu_ctx *ctx, int axis, double *flux, double *mean_density);
+
 /* Fixed-step flow: nsteps fused steps with the force of the given phase (0 = no force,
  * 1 = f_ext on fluid nodes), no convergence test (the timing mode). */
 int lbgpu_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on);

@@ -120,6 +120,7 @@ def library():
         ("lbgpu_moments_noalloc", [i, i, i] + [vp] * 8 + [C.POINTER(d), vp]),
         ("lbgpu_compensated_force_field", [vp, i, vp, i, vp, vp, vp]),
         ("lbgpu_set_force_field", [vp, vp, vp, vp]),
+        ("lbgpu_profiles", [vp, i, vp, vp]),
     ):
         if hasattr(L, name):
             getattr(L, name).argtypes = args
@@ -404,6 +405,19 @@ def _compensated_force_field(self, particle_diameter=1, particle_coords=(0, 0, 0
                                               *(_ptr(x) for x in f))
     self._chk(rc, "compensated_force_field")
     return f
+
+
+def _profiles(self, axis):
+    """equilibration.f90:154-176: (flux (L, 3), mean density (L,)) per plane normal to axis
+    (0 = x, 1 = y, 2 = z), reduced on the device."""
+    L = self.shape[2 - axis]
+    flux = np.zeros((L, 3))
+    dens = np.zeros(L)
+    self._chk(self.L.lbgpu_profiles(self.ctx, axis, _ptr(flux), _ptr(dens)), "profiles")
+    return flux, dens
+
+
+Box.profiles = _profiles
 
 
 def _set_force_field(self, f):

@@ -106,6 +106,8 @@ def lib():
         L.orc_charge_test.argtypes = [_int, _i8, _dp, _dp, _d, _pd, _pd]
         L.orc_pnp.argtypes = [_int, _int, _int, _i8, _d, _d, _d, _d, _d, _int, _dp, _dp, _dp,
                               _pd, _int, _pi, _pi]
+        L.orc_profiles.argtypes = [_int, _int, _int] + [_dp] * 4 + [_int, _dp, _dp]
+        L.orc_profiles.restype = None
         _lib = L
     return _lib
 
@@ -317,3 +319,14 @@ def pnp(nature, bjl, sigma, D_plus, D_minus, rho_ch, cp, cm, phi, anormf0, loop_
         _chk(rc, "pnp")
     return dict(c_plus=cp, c_minus=cm, phi=phi, anormf0=an.value, outer=outer.value,
                 sor_iters=tot.value, status=rc)
+
+
+def profiles(nature, rho, j, axis):
+    """equilibration.f90:159-175: (flux (L, 3), mean density (L,)) per plane normal to axis."""
+    lx, ly, lz = _dims(nature)
+    L = (lx, ly, lz)[axis]
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (rho, *j)]
+    flux = np.zeros((L, 3))
+    dens = np.zeros(L)
+    lib().orc_profiles(lx, ly, lz, *arrs, axis, flux, dens)
+    return flux, dens

@@ -835,3 +835,36 @@ int orc_pnp(int lx, int ly, int lz, const int8_t *nature, double bjl, double sig
     free(cmo);
     return rc;
 }
+
+/* equilibration.f90:159-175 (and 504-516 at exit): per plane normal to `axis` (0 = x, 1 = y,
+ * 2 = z), SUM(jx), SUM(jy), SUM(jz) and SUM(density)/MAX(COUNT(density > eps), 1), each SUM a
+ * single accumulator over the plane in array element order (first remaining index fastest). */
+void orc_profiles(int lx, int ly, int lz, const double *density, const double *jx,
+                  const double *jy, const double *jz, int axis, double *flux, double *mean_density)
+{
+    const double eps = 2.220446049250313e-16; /* EPSILON(1._dp) */
+    const int n[3] = {lx, ly, lz};
+    const int L = n[axis];
+    const int a = axis == 0 ? 1 : 0, b = axis == 2 ? 1 : 2; /* remaining axes, a fastest */
+    for (int k = 0; k < L; ++k) {
+        double sx = 0.0, sy = 0.0, sz = 0.0, sd = 0.0;
+        long cnt = 0;
+        for (int q = 0; q < n[b]; ++q)
+            for (int p = 0; p < n[a]; ++p) {
+                int c[3];
+                c[axis] = k;
+                c[a] = p;
+                c[b] = q;
+                const long r = nid(c[0], c[1], c[2], lx, ly);
+                sx = sx + jx[r];
+                sy = sy + jy[r];
+                sz = sz + jz[r];
+                sd = sd + density[r];
+                cnt += density[r] > eps;
+            }
+        flux[3 * k] = sx;
+        flux[3 * k + 1] = sy;
+        flux[3 * k + 2] = sz;
+        mean_density[k] = sd / (double)(cnt > 0 ? cnt : 1);   /* MAX(COUNT(...), 1) */
+    }
+}

@@ -151,6 +151,10 @@ int orc_pnp(int lx, int ly, int lz, const int8_t *nature, double bjl, double sig
             double *c_minus, double *phi, double *anormf0, int max_outer, int *outer_out,
             int *sor_iters_total);
 
+/* equilibration.f90:159-175, 504-516: mass-flux and mean-density profiles along an axis. */
+void orc_profiles(int lx, int ly, int lz, const double *density, const double *jx,
+                  const double *jy, const double *jz, int axis, double *flux, double *mean_density);
+
 #ifdef __cplusplus
 }
 #endif

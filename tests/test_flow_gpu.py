@@ -275,3 +275,19 @@ def test_equilibration_compensated_force_bit_exact(oracle_mod, label, make):
     assert np.array_equal(n, ref["n"])
     for d in range(3):
         assert np.array_equal(j[d], ref["j"][d])
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32_DEV])
+def test_device_profiles_equal_the_reference_profiles(oracle_mod, prec):
+    """lbgpu_profiles reduces the reference's profile output (equilibration.f90:154-176) on the
+    device in the Fortran SUM order: bit-identical to the oracle's restatement applied to the
+    same flow state, along every axis."""
+    nat = geo.porous_spheres(L=12, radius=3.0, porosity=0.7, seed=2)
+    with Box(nat, relaxation_time=0.9, f_ext=(1e-5, 2e-6, 0.0), precision=prec) as box:
+        box.flow_init()
+        box.flow_steps(15, force_on=True)
+        _, rho, j = box.flow_get(populations=False)
+        for axis in range(3):
+            flux, dens = box.profiles(axis)
+            rf, rd = oracle_mod.profiles(nat, rho, j, axis)
+            assert np.array_equal(flux, rf) and np.array_equal(dens, rd)

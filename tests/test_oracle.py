@@ -179,3 +179,20 @@ def test_golden_fixtures(oracle_mod, c1_flow):
         vac = [mp.vacf0] + [mp.propagate(it)[0] for it in range(1, 201)]
         mp.close()
         assert np.array_equal(np.array(vac), m[f"vacf_{tag}"])
+
+
+def test_profiles_restatement_matches_plane_sums(oracle_mod):
+    """equilibration.f90:159-175: per-plane sums of j and the mean density over nodes with
+    density > epsilon; integer-valued fields make every sum exact, so any summation order agrees
+    bit for bit."""
+    rng = np.random.default_rng(4)
+    lz, ly, lx = 5, 4, 7
+    nat = np.zeros((lz, ly, lx), dtype=np.int8)
+    rho = rng.integers(0, 3, size=(lz, ly, lx)).astype(np.float64)
+    j = [rng.integers(-5, 6, size=(lz, ly, lx)).astype(np.float64) for _ in range(3)]
+    for axis, red in ((0, (0, 1)), (1, (0, 2)), (2, (1, 2))):
+        flux, dens = oracle_mod.profiles(nat, rho, j, axis)
+        for d in range(3):
+            assert np.array_equal(flux[:, d], j[d].sum(axis=red))
+        cnt = np.maximum((rho > np.finfo(float).eps).sum(axis=red), 1)
+        assert np.array_equal(dens, rho.sum(axis=red) / cnt)
