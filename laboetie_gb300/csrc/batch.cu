@@ -328,13 +328,14 @@ __device__ __forceinline__ void node_moments64(const BatchInst &I, unsigned node
 }
 
 // One AA launch over the tiles of the tiled boxes (always in the compact layout); MINB resident
-// blocks per SM (3..6, picked by the tuner in batch_api.cu).
+// blocks per SM (3..6, picked by the tuner in batch_api.cu).  Odd launches take the tiles in
+// reverse order, starting on the tiles the even launch wrote last (still in L2).
 template <bool ODD, int MINB>
 __global__ void __launch_bounds__(BATCH_BLOCK, MINB) k_batch_aa(const BatchInst *__restrict__ insts,
                                                                 const BatchTile *__restrict__ tiles)
 {
     __shared__ unsigned soff[ODD ? Q : 1][BATCH_BLOCK];
-    const BatchTile t = tiles[blockIdx.x];
+    const BatchTile t = tiles[ODD ? gridDim.x - 1 - blockIdx.x : blockIdx.x];
     const BatchInst &I = insts[t.inst];
     const unsigned i = (unsigned)t.start + threadIdx.x;
     if (i < I.Nf) aa_node_compact<ODD>(I, i, soff);
