@@ -441,7 +441,8 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_v(const BatchInst *__r
 // One block per small box, for all the steps of a call: load, nsteps steps of the box's phase
 // in shared memory, optional convergence check (flow), store.  nsteps is even, so a flow box
 // ends in natural order and a tracer box with P(now) in P[0].
-__global__ void __launch_bounds__(BATCH_SMEM_THREADS) k_batch_smem(const BatchInst *__restrict__ insts,
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT) k_batch_smem(const BatchInst *__restrict__ insts,
                                                                    const int *__restrict__ list,
                                                                    int nsteps, int check,
                                                                    unsigned *du_out)
@@ -563,7 +564,9 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_moments(const BatchInst *
 
 cudaError_t batch_configure(int max_smem_bytes)
 {
-    return cudaFuncSetAttribute(k_batch_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_batch_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_batch_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
 }
 
 template <int MINB>
@@ -612,7 +615,9 @@ cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist
                               bool check, unsigned *du, int smem_bytes, int threads, cudaStream_t s)
 {
     if (nlist <= 0) return cudaSuccess;
-    k_batch_smem<<<nlist, threads, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
+    // up to 512 threads: the variant with up to 128 registers per thread; 1024: at most 64
+    if (threads <= 512) k_batch_smem<512><<<nlist, threads, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
+    else k_batch_smem<1024><<<nlist, 1024, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
     return cudaGetLastError();
 }
 

@@ -10,7 +10,8 @@
 namespace lbg {
 
 constexpr int BATCH_BLOCK = 256;        // threads per tile of the HBM kernels
-constexpr int BATCH_SMEM_THREADS = 512; // threads of a shared-memory-resident box
+constexpr int BATCH_SMEM_THREADS = 512; // default threads of a shared-memory-resident box (256, 512
+                                        // or 1024, picked by the tuner in batch_api.cu)
 constexpr int BATCH_SMEM_BYTES_MAX = 227 * 1024;
 constexpr int BATCH_TACC = 9;           // doubles per tile: VACF(0) part, sum over steps, last step
 

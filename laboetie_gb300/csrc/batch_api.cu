@@ -127,6 +127,7 @@ struct lbgpu_batch {
     int cap_du = 0;
     int aa_minb[2] = {4, 5};      // resident blocks per SM of the even / odd AA launches
     bool aa_tuned = false;
+    bool smem_tuned = false;
     std::vector<int> desc_slot;   // descriptor index -> slot
     std::vector<GraphEntry> graphs;
 };
@@ -367,9 +368,73 @@ int tune_aa(lbgpu_batch *b)
     return LBGPU_OK;
 }
 
+// Block-size tuner of the shared-memory kernel: the first time a batch holds at least 64
+// shared-memory boxes, all in the flow phase, 20 steps are timed twice with 256 and with 512
+// threads per box on scratch copies of their populations (the boxes' state does not advance) and
+// the fastest is kept.  (1024 threads, at most 64 registers each, spill and lose in the tracer
+// phase, which cannot be timed before the flow has run; LBGPU_BATCH_SMEM_THREADS=1024 still
+// selects them.)  LBGPU_BATCH_SMEM_THREADS fixes the size instead.
+int tune_smem(lbgpu_batch *b)
+{
+    if (b->smem_tuned || b->nsmem < 64) return LBGPU_OK;
+    b->smem_tuned = true;
+    if (const char *e = std::getenv("LBGPU_BATCH_SMEM_THREADS")) {
+        const int t = std::atoi(e);
+        if (t == 256 || t == 512 || t == 1024) b->smem_threads = t;
+        return LBGPU_OK;
+    }
+    std::vector<BatchInst> descs(b->desc_slot.size());
+    size_t total = 0;
+    for (size_t i = 0; i < descs.size(); ++i) {
+        const Slot &sl = b->slots[b->desc_slot[i]];
+        descs[i] = sl.d;
+        if (!sl.smem) continue;
+        if (sl.d.phase != BATCH_FLOW) return LBGPU_OK;
+        total += (size_t)Q * sl.d.N;
+    }
+    cudaStream_t s = b->stream;
+    float *scratch = nullptr;
+    BatchInst *d_tmp = nullptr;
+    if (cudaMallocAsync(&scratch, sizeof(float) * total, s) != cudaSuccess ||
+        cudaMallocAsync(&d_tmp, sizeof(BatchInst) * descs.size(), s) != cudaSuccess) {
+        cudaGetLastError();   // no room: keep the default
+        if (scratch) cudaFreeAsync(scratch, s);
+        return LBGPU_OK;
+    }
+    size_t off = 0;
+    for (size_t i = 0; i < descs.size(); ++i) {
+        if (!b->slots[b->desc_slot[i]].smem) continue;
+        BatchInst &d = descs[i];
+        LBB_CK(cudaMemcpyAsync(scratch + off, d.g, sizeof(float) * Q * d.N, cudaMemcpyDeviceToDevice, s));
+        d.g = scratch + off;
+        off += (size_t)Q * d.N;
+    }
+    LBB_CK(cudaMemcpyAsync(d_tmp, descs.data(), sizeof(BatchInst) * descs.size(), cudaMemcpyHostToDevice, s));
+    const int cand[2] = {256, 512};
+    float best[2] = {1e30f, 1e30f};
+    for (int rep = 0; rep < 2; ++rep)
+        for (int k = 0; k < 2; ++k) {
+            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 2, false, nullptr, b->smem_bytes, cand[k], s));
+            LBB_CK(cudaEventRecord(b->ev0, s));
+            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 20, false, nullptr, b->smem_bytes, cand[k], s));
+            LBB_CK(cudaEventRecord(b->ev1, s));
+            LBB_CK(cudaEventSynchronize(b->ev1));
+            float ms = 0.0f;
+            LBB_CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            best[k] = std::min(best[k], ms);
+        }
+    b->smem_threads = best[0] < best[1] ? cand[0] : cand[1];
+    LBB_CK(cudaFreeAsync(scratch, s));
+    LBB_CK(cudaFreeAsync(d_tmp, s));
+    LBB_CK(cudaStreamSynchronize(s));   // descs go out of scope
+    drop_graphs(b);
+    return LBGPU_OK;
+}
+
 int run_steps(lbgpu_batch *b, int nsteps, bool check)
 {
     if (int rc = tune_aa(b)) return rc;
+    if (int rc = tune_smem(b)) return rc;
     cudaGraphExec_t exec = nullptr;
     int rc = graph_of(b, nsteps, check, &exec);
     if (rc) return rc;
@@ -628,7 +693,7 @@ int lbgpu_batch_time_steps(lbgpu_batch *b, int nsteps, float *ms)
     if (rc) return rc;
     const bool work = !b->desc_slot.empty() && nsteps > 0;
     cudaGraphExec_t exec = nullptr;
-    if ((rc = tune_aa(b))) return rc;                                    // outside the timed region
+    if ((rc = tune_aa(b)) || (rc = tune_smem(b))) return rc;             // outside the timed region
     if (work && (rc = graph_of(b, nsteps, false, &exec))) return rc;
     LBB_CK(cudaEventRecord(b->ev0, b->stream));
     if (work && (rc = run_steps(b, nsteps, false))) return rc;
