@@ -51,12 +51,17 @@ struct PnpState {
     double anormf0 = 0.0, rho_ch = 0.0;
     bool charged = false;
     std::vector<void *> allocs;
+    // CUDA graphs of 8 and of 64 sweeps, captured at the first solve and replayed by every later
+    // one (their arguments are fixed until the state is released)
+    cudaGraphExec_t sor_exec[2] = {nullptr, nullptr};
 };
 
 void pnp_release(lbgpu_ctx *ctx)
 {
     if (!ctx->pnp) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cudaGraphExec_t g : ctx->pnp->sor_exec)
+        if (g) cudaGraphExecDestroy(g);
     for (void *p : ctx->pnp->allocs) cudaFree(p);
     delete ctx->pnp;
     ctx->pnp = nullptr;
@@ -538,32 +543,40 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
     a.one_minus_omega = 1.0 - a.omega;
     LBG_CK(ctx, cudaMemcpyAsync(s->ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
     const unsigned grid = grid_for(ctx->N);
-    const int G = 64;
-    cudaGraph_t g;
-    cudaGraphExec_t exec;
-    LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < G; ++k) {
-        if (four) {
-            for (int col = 0; col < 4; ++col) {
-                PnpArgs b = a;
-                b.color = col;
-                k_sor_color<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
+    // sweeps after the exit are no-ops (the control block is done): a graph of 8 sweeps first,
+    // then graphs of 64 until the solve converges or reaches its cap
+    for (int k = 0; k < 2; ++k) {
+        if (s->sor_exec[k]) continue;
+        const int G = k == 0 ? 8 : 64;
+        cudaGraph_t g;
+        LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < G; ++q) {
+            if (four) {
+                for (int col = 0; col < 4; ++col) {
+                    PnpArgs b = a;
+                    b.color = col;
+                    k_sor_color<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
+                }
+            } else {
+                k_sor_jacobi<<<grid, PB, 0, st>>>(a, s->phi[0], s->phi[1]);
             }
-        } else {
-            k_sor_jacobi<<<grid, PB, 0, st>>>(a, s->phi[0], s->phi[1]);
+        }
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (ce != cudaSuccess) return ctx_cuda(ctx, ce, "capture sor");
+        ce = cudaGraphInstantiate(&s->sor_exec[k], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            s->sor_exec[k] = nullptr;
+            return ctx_cuda(ctx, ce, "instantiate sor");
         }
     }
-    cudaError_t e = cudaStreamEndCapture(st, &g);
-    if (e != cudaSuccess) return ctx_cuda(ctx, e, "capture sor");
-    LBG_CK(ctx, cudaGraphInstantiate(&exec, g, 0));
-    cudaGraphDestroy(g);
-    for (;;) {
-        e = cudaGraphLaunch(exec, st);
+    cudaError_t e = cudaSuccess;
+    for (int round = 0;; ++round) {
+        e = cudaGraphLaunch(s->sor_exec[round == 0 ? 0 : 1], st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&c, s->ctl, sizeof(c), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess || c.done) break;
     }
-    cudaGraphExecDestroy(exec);
     if (e != cudaSuccess) return ctx_cuda(ctx, e, "lbgpu_sor");
     if (!four) s->par = c.parity;
     if (iters) *iters = s->p.solver == LBGPU_POISSON_REFERENCE ? c.iter - 1 : c.iter;  // sor.f90:87
