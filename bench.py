@@ -199,9 +199,10 @@ def cpu_oracle_mlups(nature, seconds, threads):
 def precision_results(nature, precision, tau, f_ext, flow_steps, mp_steps, tracer):
     """Flow then tracer propagation in one precision; the results the FP32 error is stated for.
     permeability k = nu <u_x> / f_x (Darcy velocity over the whole box); D_eff = VACF(0)/2 +
-    sum VACF (Green-Kubo, unit step, flow axis x); adsorbed fraction = K n_if / (n_f + K n_if)
-    (the tracer's equilibrium time fraction on interfacial nodes); retention time = lx / v_tr
-    with v_tr = (1 - adsorbed fraction) <u_x>_fluid (mean tracer velocity)."""
+    sum VACF (Green-Kubo, unit step, flow axis x); adsorbed fraction = sum P_ads,x / sum
+    (P_x + P_ads,x) at the last tracer step (the adsorbed share of the propagated quantity); the
+    equilibrium adsorbed fraction K n_if / (n_f + K n_if) (node counts: exact in both); retention
+    time = lx / v_tr with v_tr = (1 - equilibrium fraction) <u_x>_fluid."""
     from laboetie_gb300 import Box
 
     with Box(nature, relaxation_time=tau, f_ext=f_ext, precision=precision) as box:
@@ -210,6 +211,7 @@ def precision_results(nature, precision, tau, f_ext, flow_steps, mp_steps, trace
         _, rho, j = box.flow_get(populations=False)
         v0 = box.mp_init(f_ext=f_ext, **tracer)
         vac, _ = box.mp_propagate(mp_steps)
+        P, A = box.mp_get()
         counts = box.node_counts()
     nu = (tau - 0.5) / 3.0
     fluid = nature == 0
@@ -218,8 +220,9 @@ def precision_results(nature, precision, tau, f_ext, flow_steps, mp_steps, trace
     K = tracer["ka"] / tracer["kd"]
     ads = K * counts["fluid_interfacial"] / (counts["fluid"] + K * counts["fluid_interfacial"])
     return {"permeability": k, "d_eff": float(v0[0] / 2 + vac[:, 0].sum()),
-            "adsorbed_fraction": ads, "retention_time": nature.shape[2] / ((1 - ads) * ux_fluid),
-            "mp_steps": int(len(vac))}
+            "adsorbed_fraction": float(A[..., 0].sum() / (P[..., 0].sum() + A[..., 0].sum())),
+            "equilibrium_adsorbed_fraction": ads,
+            "retention_time": nature.shape[2] / ((1 - ads) * ux_fluid), "mp_steps": int(len(vac))}
 
 
 def bench_precision(a):
@@ -236,7 +239,8 @@ def bench_precision(a):
     for name, prec in (("fp64", FP64), ("fp32", FP32_DEV)):
         out[name] = precision_results(nat, prec, TAU, FEXT, a.precision_flow_steps, a.precision_mp_steps, tracer)
     rel = {k: abs(out["fp32"][k] - out["fp64"][k]) / abs(out["fp64"][k])
-           for k in ("permeability", "d_eff", "adsorbed_fraction", "retention_time")}
+           for k in ("permeability", "d_eff", "adsorbed_fraction", "equilibrium_adsorbed_fraction",
+                     "retention_time")}
     return {"config": {"workload": f"porous {L}^3 spheres r=8 porosity 0.60 seed {SEED}, tau 0.8, f_ext (1e-6,0,0)",
                        "flow_steps": a.precision_flow_steps, "mp_steps": a.precision_mp_steps,
                        "tracer": "Db 0.01, K = e^2 (kd 0.01)"},
