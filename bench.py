@@ -403,7 +403,7 @@ def bench_serving(a):
             res = b.serve(reqs, du_tol=1e-8, check_every=100)
             wall = time.perf_counter() - t
         lat = np.array([r["finished"] - q["arrival"] for r, q in zip(res, reqs)])
-        ok = [r for r in res if r["status"] == 0]
+        ok = [r for r in res if r["status"] in (0, 1 << 5)]   # served; 1 << 5: flow capped
         out.append({"rate_per_s": rate, "n": len(reqs), "ok": len(ok),
                     "converged": sum(1 for r in ok if r["converged"]),
                     "solves_per_s": round(len(ok) / wall, 3), "seconds": round(wall, 2),

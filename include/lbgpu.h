@@ -294,6 +294,10 @@ typedef struct {
     double vacf0[3], vacf_sum[3];
 } lbgpu_request_result;
 
+/* result status: 0, or LBGPU_ERR_STEP_CAP (flow capped before converging; its tracer steps still
+ * ran), LBGPU_ERR_NONFINITE (its flow produced a non-finite velocity; it left at once),
+ * LBGPU_ERR_FRACTION (tracer start refused), LBGPU_ERR_OOM (can never fit the budget),
+ * LBGPU_ERR_INVALID / LBGPU_ERR_UNSUPPORTED (refused cell).  Other requests are unaffected. */
 /* Request server (continuous batching) on an empty batch: a request is admitted once it has
  * arrived and its buffers fit the batch's memory budget (in arrival order), is stepped with all
  * resident boxes in rounds of check_every steps, ends its flow when du < du_tol at a check

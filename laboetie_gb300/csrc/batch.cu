@@ -8,6 +8,8 @@
 // and writes it back: HBM is touched twice per call instead of twice per step.  Every box is
 // updated by its own threads only and its arithmetic does not depend on which other boxes
 // share the launch, so a box gives the same result alone and in any mix.
+#include <cfloat>
+
 #include "batch.h"
 #include "collide32.cuh"
 #include "common.cuh"
@@ -296,11 +298,16 @@ __device__ __forceinline__ float3 node_velocity(const float *g, unsigned N, unsi
     return make_float3(jx * ir, jy * ir, jz * ir);
 }
 
-__device__ __forceinline__ float du_and_store(float4 *uprev, unsigned node, const float3 u)
+// max |u - u_prev| of a node as the bits of a non-negative float (a non-finite velocity gives
+// the bits of a NaN, 0x7fffffff, which exceed those of every finite value and of infinity), so
+// that maxima of the bits, unlike fmaxf, keep a NaN; u_prev := u.
+__device__ __forceinline__ unsigned du_and_store(float4 *uprev, unsigned node, const float3 u)
 {
     const float4 p = uprev[node];
     uprev[node] = make_float4(u.x, u.y, u.z, 0.0f);
-    return fmaxf(fmaxf(fabsf(u.x - p.x), fabsf(u.y - p.y)), fabsf(u.z - p.z));
+    const float d = fmaxf(fmaxf(fabsf(u.x - p.x), fabsf(u.y - p.y)), fabsf(u.z - p.z));
+    const bool finite = fabsf(u.x) <= FLT_MAX && fabsf(u.y) <= FLT_MAX && fabsf(u.z) <= FLT_MAX;
+    return finite ? __float_as_uint(d) : 0x7fffffffu;
 }
 
 // FP64 density and flux of a fluid node in natural order (index in the box's layout).
@@ -469,11 +476,11 @@ __global__ void __launch_bounds__(MAXT) k_batch_smem(const BatchInst *__restrict
             __syncthreads();
         }
         if (check) {
-            float du = 0.0f;
+            unsigned du = 0u;
             for (unsigned node = threadIdx.x; node < N; node += T)
-                if (msk[node] & FLUID_BIT) du = fmaxf(du, du_and_store(I.uprev, node, node_velocity(g, N, node, I)));
-            for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
-            if ((threadIdx.x & 31) == 0) atomicMax(du_out + id, __float_as_uint(du));
+                if (msk[node] & FLUID_BIT) du = max(du, du_and_store(I.uprev, node, node_velocity(g, N, node, I)));
+            for (int o = 16; o > 0; o >>= 1) du = max(du, __shfl_xor_sync(0xffffffffu, du, o));
+            if ((threadIdx.x & 31) == 0) atomicMax(du_out + id, du);
         }
         for (unsigned i = threadIdx.x; i < (unsigned)Q * N; i += T) I.g[i] = g[i];
         return;
@@ -534,10 +541,10 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_check(const BatchInst *__
     const BatchTile t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
     const unsigned node = (unsigned)t.start + threadIdx.x;
-    float du = 0.0f;   // tiled boxes are in the compact layout: every node is fluid
+    unsigned du = 0u;   // tiled boxes are in the compact layout: every node is fluid
     if (node < I.Nf) du = du_and_store(I.uprev, node, node_velocity(I.g, I.Nf, node, I));
-    for (int o = 16; o > 0; o >>= 1) du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(du_out + t.inst, __float_as_uint(du));
+    for (int o = 16; o > 0; o >>= 1) du = max(du, __shfl_xor_sync(0xffffffffu, du, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(du_out + t.inst, du);
 }
 
 // Density and flux (FP64) of one box in natural order; solid nodes report zeros.

@@ -25,6 +25,7 @@
 #include "ctx.h"
 #include "flow.h"
 #include "lbgpu.h"
+#include "trace.h"
 
 using namespace lbg;
 
@@ -535,6 +536,7 @@ void lbgpu_batch_destroy(lbgpu_batch *b)
 
 int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, int *id)
 {
+    TraceRange trace_("lbgpu_batch_add");
     if (!b || !c || !nature || !id) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: null argument");
     if (c->lx <= 0 || c->ly <= 0 || c->lz <= 0) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: bad size");
     if (!(c->relaxation_time > 0.5)) return bfail(LBGPU_ERR_INVALID, "relaxation_time must be > 0.5");
@@ -666,6 +668,7 @@ int lbgpu_batch_remove(lbgpu_batch *b, int id)
 
 int lbgpu_batch_steps(lbgpu_batch *b, int nsteps, int check, float *du)
 {
+    TraceRange trace_("lbgpu_batch_steps");
     if (!b || nsteps < 0 || (nsteps & 1)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_steps: nsteps must be even and >= 0");
     int rc = rebuild(b);
     if (rc) return rc;
@@ -728,6 +731,7 @@ int lbgpu_batch_moments(lbgpu_batch *b, int id, double *rho, double *jx, double 
 
 int lbgpu_batch_mp_start(lbgpu_batch *b, int id)
 {
+    TraceRange trace_("lbgpu_batch_mp_start");
     if (!valid_slot(b, id)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_start: no such box");
     Slot &sl = b->slots[id];
     if (!sl.tracer) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_start: the box has no tracer (tracer.Db = 0)");
@@ -791,6 +795,7 @@ int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *s
 int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *req, int n, double du_tol, int check_every,
                 lbgpu_request_result *out)
 {
+    TraceRange trace_("lbgpu_serve");
     if (!b || n < 0 || (n > 0 && (!req || !out)) || check_every <= 0 || (check_every & 1))
         return bfail(LBGPU_ERR_INVALID, "lbgpu_serve: bad argument (check_every must be even and > 0)");
     for (auto &sl : b->slots)
@@ -880,6 +885,7 @@ int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *req, int n, double du_tol, 
             const bool cap = q.max_steps > 0 && out[r].steps >= q.max_steps;
             if (!(conv || cap || bad)) continue;
             out[r].converged = conv ? 1 : 0;
+            if (!conv) out[r].status |= LBGPU_ERR_STEP_CAP;   // flagged; its tracer steps still run
             if (bad) {
                 out[r].status = LBGPU_ERR_NONFINITE;
                 if ((rc = finish((int)k, r, t))) return rc;
@@ -892,7 +898,7 @@ int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *req, int n, double du_tol, 
                 rc = lbgpu_batch_mp_start(b, (int)k);
                 if (rc == LBGPU_OK) continue;
                 if (rc != LBGPU_ERR_FRACTION) return rc;
-                out[r].status = rc;
+                out[r].status |= rc;
             }
             if ((rc = finish((int)k, r, now_s() - t0))) return rc;
         }

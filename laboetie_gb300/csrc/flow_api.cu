@@ -13,6 +13,7 @@
 #include "ctx.h"
 #include "flow.h"
 #include "lbgpu.h"
+#include "trace.h"
 
 using namespace lbg;
 
@@ -412,6 +413,7 @@ int lbgpu_moments(lbgpu_ctx *ctx, const double *n, const double *f_ext_x, const 
 int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap,
                         int *steps_out)
 {
+    TraceRange trace_("lbgpu_equilibration");
     if (!ctx) return LBGPU_ERR_INVALID;
     if (ctx->p.precision != LBGPU_FP64)
         return ctx_fail(ctx, LBGPU_ERR_INVALID,
@@ -499,6 +501,7 @@ int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int h
 
 int lbgpu_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on)
 {
+    TraceRange trace_("lbgpu_flow_steps");
     if (!ctx || nsteps < 0) return LBGPU_ERR_INVALID;
     if (ctx->prev_kind == PREV_NONE)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_flow_steps: call lbgpu_flow_init first");

@@ -12,6 +12,7 @@
 #include "ctx.h"
 #include "flow.h"
 #include "lbgpu.h"
+#include "trace.h"
 #include "mp.h"
 
 namespace lbg {
@@ -69,6 +70,7 @@ extern "C" {
 int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, const double *jx,
                   const double *jy, const double *jz, double vacf0[3])
 {
+    TraceRange trace_("lbgpu_mp_init");
     if (!ctx || !tr) return LBGPU_ERR_INVALID;
     if ((density == nullptr) != (jx == nullptr) || (jx == nullptr) != (jy == nullptr) ||
         (jy == nullptr) != (jz == nullptr))
@@ -210,6 +212,7 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
 static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done, int *is_converged,
                   bool timing, float *ms)
 {
+    TraceRange trace_("moment propagation");
     MpState *s = ctx->mp;
     if (!s) return ctx_fail(ctx, LBGPU_ERR_INVALID, "moment propagation: call lbgpu_mp_init first");
     if (s->pending)

@@ -22,6 +22,7 @@
 #include "common.cuh"
 #include "ctx.h"
 #include "lbgpu.h"
+#include "trace.h"
 #include "reduce.cuh"
 
 namespace lbg {
@@ -514,6 +515,7 @@ int lbgpu_pnp_get(lbgpu_ctx *ctx, double *c_plus, double *c_minus, double *phi, 
 
 int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
 {
+    TraceRange trace_("lbgpu_sor");
     if (!ctx) return LBGPU_ERR_INVALID;
     int rc = need_pnp(ctx, "lbgpu_sor");
     if (rc) return rc;
@@ -588,6 +590,7 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
 
 int lbgpu_just_eq_smolu(lbgpu_ctx *ctx, int *iters)
 {
+    TraceRange trace_("lbgpu_just_eq_smolu");
     if (!ctx) return LBGPU_ERR_INVALID;
     int rc = need_pnp(ctx, "lbgpu_just_eq_smolu");
     if (rc) return rc;
@@ -641,6 +644,7 @@ int lbgpu_charge_test(lbgpu_ctx *ctx, double *solid_charge, double *fluid_charge
 
 int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *sor_iters_total)
 {
+    TraceRange trace_("lbgpu_poisson_nernst_planck");
     if (!ctx) return LBGPU_ERR_INVALID;
     int rc = need_pnp(ctx, "lbgpu_poisson_nernst_planck");
     if (rc) return rc;

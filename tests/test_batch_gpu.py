@@ -178,7 +178,8 @@ def test_serve_result_alone_equals_result_in_the_stream():
     reqs = _requests(seed=7, n=9, rate=200.0)
     with Batch() as b:
         mix = b.serve(reqs, du_tol=1e-9, check_every=100)
-    assert all(r["status"] == 0 and r["finished"] >= r["admitted"] >= 0 for r in mix)
+    # status 0, or 1 << 5 for a flow capped before converging (its tracer steps still ran)
+    assert all(r["status"] in (0, 1 << 5) and r["finished"] >= r["admitted"] >= 0 for r in mix)
     overlap = sum(1 for r in mix for q in mix if q is not r and q["admitted"] < r["finished"] and
                   r["admitted"] < q["finished"])
     assert overlap > 0   # the stream really shared the device
@@ -209,5 +210,5 @@ def test_serve_admission_by_footprint():
         res = b.serve(reqs, du_tol=0.0, check_every=100)
     assert res[1]["status"] == 1 << 6 and res[1]["admitted"] < 0
     ok = [res[i] for i in (0, 2, 3)]
-    assert all(r["status"] == 0 and r["steps"] == 400 for r in ok)
+    assert all(r["status"] == 1 << 5 and not r["converged"] and r["steps"] == 400 for r in ok)  # capped
     assert ok[2]["admitted"] >= min(ok[0]["finished"], ok[1]["finished"])
