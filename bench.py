@@ -73,6 +73,9 @@ def args_():
     ap.add_argument("--pnp-max-outer", type=int, default=200)
     ap.add_argument("--charged-flow-steps", type=int, default=5000)
     ap.add_argument("--charged-mp-steps", type=int, default=5000)
+    ap.add_argument("--poisson-size", type=int, default=192)
+    ap.add_argument("--poisson-sweeps", type=int, default=512)
+    ap.add_argument("--poisson-only", action="store_true", help="charged section: the sweep timing only")
     # serving stream (Poisson arrivals, continuous batching)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-n", type=int, default=48)
@@ -261,7 +264,7 @@ def bench_charged(a):
 
     cases = [("slit 1x1x64", geo.slit(1, 1, 64)), ("touching spheres 48^3", geo.cc(48, 48, 48))]
     out = []
-    for name, nat in cases:
+    for name, nat in ([] if a.poisson_only else cases):
         res = {"case": name}
         with Box(nat) as box:
             inter = box.interfacial()
@@ -301,6 +304,33 @@ def bench_charged(a):
                                abs(v["fp64"][0][0] / 2 + v["fp64"][1][:n, 0].sum())),
             "steps": n}
         out.append(res)
+    # Poisson sweep roofline on a large charged box: 4 x 8 B per node and sweep (phi read and
+    # written, c+ and c- read).  Tolerance 0, so every solve runs exactly its sweep cap; an odd box
+    # side selects the Jacobi kernel, an even one the 4-colour kernel.
+    hbm, _ = peaks()
+    sweeps = {}
+    for sname, L in (("jacobi", a.poisson_size - 1), ("sor4", a.poisson_size)):
+        nat = geo.cc(L, L, L)
+        with Box(nat) as box:
+            inter = box.interfacial()
+        sigma = -0.01 * int(((nat == 1) & (inter == 1)).sum())
+        with Box(nat) as box:
+            box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
+                         solver=POISSON_SOR4, omega=1.8, tol=0.0, max_iter=a.poisson_sweeps)
+            for k in range(2):            # warm-up solve (captures the sweep graphs), timed solve
+                t = time.perf_counter()
+                try:
+                    box.sor()
+                except Exception:
+                    pass                  # LBGPU_ERR_STEP_CAP after exactly max_iter sweeps
+                dt = time.perf_counter() - t
+        gbs = 32.0 * nat.size * a.poisson_sweeps / dt / 1e9
+        sweeps[sname] = {"box": f"touching spheres {L}^3", "sweeps": a.poisson_sweeps,
+                         "ms_per_sweep": round(dt / a.poisson_sweeps * 1e3, 4),
+                         "roofline": {"bound": "fp64 pipe", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                                      "frac": round(gbs / hbm, 4), "algorithmic_bytes_per_node": 32,
+                                      "note": "FP64-pipe bound (83 % of its peak under ncu); frac is of HBM"}}
+    out.append({"case": "Poisson sweeps (wall clock of one solve, host checks every 64 sweeps)", **sweeps})
     return {"cases": out, "config": {"bjl": 0.4, "lambda_D": 4.0, "D_plus": 0.05, "D_minus": 0.05,
                                      "surface_charge_per_interfacial_solid_node": -0.01,
                                      "max_outer": a.pnp_max_outer, "flow_steps": a.charged_flow_steps,

@@ -184,17 +184,22 @@ __global__ void __launch_bounds__(PB) k_sor_jacobi(const PnpArgs a, double *phi0
 }
 
 // One colour of the 4-colour SOR: phi <- (1-omega) phi + omega * 1.5 (sum_{l>0} w_l phi(x-c_l) + b).
-// The sum of |change| over the four colours is the stopping measure; colour 3 decides.
+// The sum of |change| over the four colours is the stopping measure; colour 3 decides.  The
+// threads walk only the colour's N/4 nodes (even lx and ly): in plane z the colour holds the rows
+// y = 2j + (c1 ^ z&1) and in them the nodes x = 2i + (c0 ^ z&1), c0 and c1 the colour's bits.
 __global__ void __launch_bounds__(PB) k_sor_color(const PnpArgs a, double *phi)
 {
     const volatile PnpCtl *vc = a.ctl;
     if (vc->done) return;
     double t[3] = {0.0, 0.0, 0.0};
-    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
-        int x, y, z;
-        coords(r, a.lx, a.ly, x, y, z);
-        const int col = ((x + z) & 1) | (((y + z) & 1) << 1);
-        if (col != a.color) continue;
+    const int hx = a.lx >> 1, hy = a.ly >> 1;
+    const long long Nc = (long long)hx * hy * a.lz;
+    for (long long k = (long long)blockIdx.x * PB + threadIdx.x; k < Nc; k += (long long)gridDim.x * PB) {
+        const long long q = k / hx;
+        const int z = (int)(q / hy), zp = z & 1;
+        const int x = 2 * (int)(k - q * hx) + ((a.color & 1) ^ zp);
+        const int y = 2 * (int)(q - (long long)z * hy) + (((a.color >> 1) & 1) ^ zp);
+        const long long r = x + (long long)a.lx * (y + (long long)a.ly * z);
         double s = 0.0;
         static_for<1, Q>([&](auto L) {
             constexpr int l = decltype(L)::value;
