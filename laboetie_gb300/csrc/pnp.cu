@@ -200,15 +200,17 @@ __global__ void __launch_bounds__(PB) k_sor_color(const PnpArgs a, double *phi)
         const int x = 2 * (int)(k - q * hx) + ((a.color & 1) ^ zp);
         const int y = 2 * (int)(q - (long long)z * hy) + (((a.color >> 1) & 1) ^ zp);
         const long long r = x + (long long)a.lx * (y + (long long)a.ly * z);
+        // this solver is not the reference's, so it may fuse: explicit multiply-adds (the file is
+        // built without contraction for the reference sweeps) halve its FP64 instructions
         double s = 0.0;
         static_for<1, Q>([&](auto L) {
             constexpr int l = decltype(L)::value;
             constexpr Vel c = vel(l);
-            s = s + a.a0[wclass(l)] * phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)];
+            s = __fma_rn(a.a0[wclass(l)], phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)], s);
         });
-        const double target = 1.5 * (s + a.factor * (a.cp[r] - a.cm[r]));
+        const double target = 1.5 * __fma_rn(a.factor, a.cp[r] - a.cm[r], s);
         const double old = phi[r];
-        const double nw = a.one_minus_omega * old + a.omega * target;
+        const double nw = __fma_rn(a.one_minus_omega, old, a.omega * target);
         phi[r] = nw;
         t[0] = t[0] + fabs(nw - old);
     }
