@@ -1,13 +1,15 @@
 // batch.cu -- kernels stepping many independent boxes together (FP32 deviations, in-place AA;
 // FP32 tracer moment propagation).
 //
-// Large boxes are cut into tiles of BATCH_BLOCK consecutive nodes; one launch steps every tile
-// of every large box in a phase (a tile never straddles two boxes, so a block reads one
-// descriptor).  Small boxes are stepped by a persistent block each that loads the whole box
-// into shared memory, runs all the steps of a call there with a block barrier between steps,
-// and writes it back: HBM is touched twice per call instead of twice per step.  Every box is
-// updated by its own threads only and its arithmetic does not depend on which other boxes
-// share the launch, so a box gives the same result alone and in any mix.
+// Large boxes are stored in the fluid-only layout of compact.cuh and cut into tiles of
+// BATCH_BLOCK consecutive fluid nodes; one launch steps every tile of every large box in a phase
+// (a tile never straddles two boxes, so a block reads one descriptor).  In the tracer phase,
+// large boxes at least 32 x 8 wide run shared-memory slab tiles (mp_slab.cuh).  Small boxes are
+// stepped by a persistent block each that loads the whole box (lattice layout) into shared
+// memory, runs all the steps of a call there with a block barrier between steps, and writes it
+// back: HBM is touched twice per call instead of twice per step.  Every box is updated by its
+// own threads only and its arithmetic does not depend on which other boxes share the launch,
+// so a box gives the same result alone and in any mix, and in either path.
 #include <cfloat>
 
 #include "batch.h"

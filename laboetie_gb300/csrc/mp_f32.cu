@@ -4,11 +4,12 @@
 //   n_l/rho - w_l + lambda w_l/2 = a1_l (c_l . V(r)) + lambda w_l / 2,   V = (j + f_ext)/rho
 // (drop_tracers.f90:97-100 divided by rho), so every probability of a step follows from V at
 // the node and at its neighbours.  V and the propagated quantity P are stored as float4
-// records (x, y, z, unused): a link costs two 16-byte gathers.  A step moves 52 bytes per fluid
-// node (V and P read, P written, the flag word); the VACF node sum is formed per thread in FP32
-// over a few nodes and in FP64 across threads and blocks.
-// Solid neighbours hold V = 0 and P = 0 and their links are masked to zero, so the gathers are
-// branch-free and can all be in flight at once.
+// records (x, y, z, unused).  Boxes at least 32 x 8 wide are stepped by k_mp32_slab, which
+// stages planes of V and P in shared memory (mp_slab.cuh); others by k_mp32, where a link costs
+// two 16-byte gathers.  A step moves 40 algorithmic bytes per fluid node (V and P read, P
+// written, the flag word); the VACF node sum is formed per thread in FP32 over a few nodes and
+// in FP64 across threads and blocks.  Solid neighbours hold V = 0 and P = 0 and their links are
+// masked to zero, so the gathers are branch-free and can all be in flight at once.
 #include "common.cuh"
 #include "cpasync.cuh"
 #include "lbgpu.h"
