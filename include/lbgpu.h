@@ -138,7 +138,10 @@ enum lbgpu_flow_mode {
  * the first convergence, exit at the second) evaluated on the device between steps.
  * Stops at convergence or after max_steps (LBGPU_ERR_STEP_CAP).  l2err_hist (optional,
  * capacity hist_cap) receives l2err(t) for t = 1..steps (the output/l2err.dat series).
- * *steps_out = the exit step t. */
+ * *steps_out = the exit step t.  FP64 contexts: bit-identical to the reference.  FP32-deviation
+ * contexts: the same loop in FP32 (a check after each in-place step, l2err from FP64 moments);
+ * l2err cannot fall below the FP32 resolution of j (about 1e-7 of |j|), so a target_error under
+ * that is never met and the loop ends at max_steps. */
 int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap,
                         int *steps_out);
 

@@ -101,6 +101,10 @@ struct FlowCtl {
     double last_l2err;
     int hist_cap;
     int exit_force_moment;  // force_moment of the exit step (its moments include F/2)
+    // FP32 in-place loop (a check launch after every AA launch): the moment force of the state
+    // the next check reads, and the moment / collision forces of the next AA launch
+    int check_fm, aa_fm, aa_fc;
+    int exit_phase;         // AA phase of the state the loop exited on
 };
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v)

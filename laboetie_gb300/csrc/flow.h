@@ -57,6 +57,9 @@ struct FlowArgs32 {
     const uint32_t *cpos, *cmask;
     const uint2 *rowtab;
     int xbits, ybits;            // cpos = x | y << xbits | z << (xbits + ybits)
+    // reference loop (lbgpu_equilibration): control block read by the AA launches, l2err history
+    FlowCtl *ctl;
+    double *hist;
 };
 
 // FP64 strict ---------------------------------------------------------------------------
@@ -85,6 +88,9 @@ cudaError_t launch_to_dev_compact32(const FlowArgs32 &a, const double *n, float 
 cudaError_t launch_finalize_f32(const FlowArgs32 &a, bool pull, cudaStream_t s);
 cudaError_t launch_collide_f32(const FlowArgs32 &a, cudaStream_t s);
 cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s);
+// reference loop: FP64 moments, l2err, n<0 / non-finite checks of the AA state (swapped after an
+// even launch) and the phase decision in the control block a.ctl
+cudaError_t launch_aa_check_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s);
 cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s);
 cudaError_t launch_to_dev32(const FlowArgs32 &a, const double *n, float *out, cudaStream_t s);
 

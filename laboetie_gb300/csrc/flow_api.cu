@@ -223,6 +223,7 @@ int f32_flow_init(lbgpu_ctx *ctx);
 int f32_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const double *jx,
                  const double *jy, const double *jz);
 int f32_flow_get(lbgpu_ctx *ctx, double *n, double *density, double *jx, double *jy, double *jz);
+int f32_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap, int *steps_out);
 int f32_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms);
 }  // namespace lbg
 
@@ -415,12 +416,15 @@ int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int h
 {
     TraceRange trace_("lbgpu_equilibration");
     if (!ctx) return LBGPU_ERR_INVALID;
-    if (ctx->p.precision != LBGPU_FP64)
-        return ctx_fail(ctx, LBGPU_ERR_INVALID,
-                        "lbgpu_equilibration: the reference loop runs on an FP64 context");
     if (ctx->prev_kind == PREV_NONE)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_equilibration: call lbgpu_flow_init first");
     if (hist_cap < 0 || (hist_cap > 0 && !l2err_hist)) return LBGPU_ERR_INVALID;
+    if (ctx->p.precision == LBGPU_FP32_DEV) {
+        if (ctx->d_F[0])
+            return ctx_fail(ctx, LBGPU_ERR_UNSUPPORTED,
+                            "lbgpu_equilibration: a per-node force field needs an FP64 context");
+        return f32_equilibration(ctx, max_steps, l2err_hist, hist_cap, steps_out);
+    }
     cudaStream_t s = ctx->stream;
     double *d_hist = nullptr;
     if (hist_cap > 0) {

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
 // One AA update of the compact node i; odd launches take its flag word m and lattice index p.
 template <bool ODD, int FMASK>
 __device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint32_t m, unsigned p,
-                                          unsigned (*soff)[BLOCK])
+                                          unsigned (*soff)[BLOCK], int fm, int fc)
 {
     // Each thread writes only the slots it has read, and every value it writes depends on all
     // of them: no store can overtake a load, so the two views of the buffer may be restricted.
@@ -144,12 +144,12 @@ __device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint3
         if constexpr (c.z > 0) jz += f[l];
         if constexpr (c.z < 0) jz -= f[l];
     });
-    if (FMASK && a.force_moment) {
+    if (FMASK && fm) {
         jx = __fadd_rn(jx, __fmul_rn(0.5f, a.F[0]));
         jy = __fadd_rn(jy, __fmul_rn(0.5f, a.F[1]));
         jz = __fadd_rn(jz, __fmul_rn(0.5f, a.F[2]));
     }
-    collide_dev<FMASK>(f, drho, jx, jy, jz, a, a.force_collide != 0);
+    collide_dev<FMASK>(f, drho, jx, jy, jz, a, fc != 0);
     if constexpr (ODD) {
         // the population leaving along l goes to the slot the opposite direction was read from
 #pragma unroll
@@ -166,17 +166,137 @@ __device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint3
 // launches walk the nodes in reverse block order, so each launch starts on the nodes the
 // previous one wrote last, which are still in L2 (about 55 MB of the 323 MB of populations of the
 // 192^3 benchmark box).
-template <bool ODD, int FMASK, int MINB>
+template <bool ODD, int FMASK, int MINB, bool LOOP>
 __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
 {
     // odd launches: element index of the slot read for direction l, parked in shared memory
     // ([l][thread], conflict-free) so that it does not occupy registers across the collision
     __shared__ unsigned soff[ODD ? Q : 1][BLOCK];
+    int fm = a.force_moment, fc = a.force_collide;
+    if constexpr (LOOP) {   // reference loop: forces decided on the device; no-op after the exit
+        const volatile FlowCtl *c = a.ctl;
+        if (c->done) return;
+        fm = c->aa_fm;
+        fc = c->aa_fc;
+    }
     const unsigned blk = ODD ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const unsigned i = blk * BLOCK + threadIdx.x;   // compact (fluid) node
     if (i >= a.Nf) return;
-    if constexpr (!ODD) aa_update<false, FMASK>(a, i, 0u, 0u, soff);
-    else aa_update<true, FMASK>(a, i, __ldg(a.cmask + i), __ldg(a.cpos + i), soff);
+    if constexpr (!ODD) aa_update<false, FMASK>(a, i, 0u, 0u, soff, fm, fc);
+    else aa_update<true, FMASK>(a, i, __ldg(a.cmask + i), __ldg(a.cpos + i), soff, fm, fc);
+}
+
+// Control step of the FP32 reference loop, run by the last block of a check launch: the
+// equilibration.f90:339-489 decisions (l2err history, convergence at l2err <= target_error and
+// t > 2, f_ext from the next collision on at the first convergence, exit at the second) for the
+// state S_t of step t.  Unlike the FP64 fused step no step is repeated: the decision is taken
+// before the AA launch of step t+1 collides S_t.
+__device__ void control_step32(FlowCtl *c, double *hist, int phase)
+{
+    const unsigned long long eb = atomicExch(&c->err_bits, 0ull);
+    const double l2 = __longlong_as_double((long long)eb);
+    c->blocks_done = 0;
+    const unsigned st = atomicOr(&c->status, 0u);
+    const int t = c->t;
+    const int fm = c->check_fm;   // moment force of S_t
+    bool finish = false;
+    if (st & (LBGPU_ERR_NEGATIVE_POPULATION | LBGPU_ERR_NONFINITE)) {
+        finish = true;
+    } else {
+        if (hist && t - 1 < c->hist_cap) hist[t - 1] = l2;
+        c->last_l2err = l2;
+        if (l2 <= c->target_error && t > 2) {
+            if (!c->conv_without) {
+                c->conv_without = 1;
+                c->aa_fc = 1;          // f_ext acts from the collision of step t+1 on
+            } else {
+                c->conv_with = 1;
+                finish = true;
+            }
+        }
+    }
+    c->exit_force_moment = fm;
+    c->exit_step = t;
+    c->exit_phase = phase;
+    c->aa_fm = fm;
+    c->check_fm = c->aa_fc;        // S_{t+1} = collide(S_t) with aa_fc: its moments carry it
+    c->t = t + 1;
+    if (!finish && c->max_steps > 0 && t >= c->max_steps) {
+        finish = true;
+        atomicOr(&c->status, (unsigned)LBGPU_ERR_STEP_CAP);
+    }
+    if (finish) c->done = 1;
+}
+
+// Check launch of the FP32 reference loop: FP64 moments of the AA state (natural order after
+// an odd launch, SWAPPED after an even one) with the state's moment force, max |j - j_old| over
+// the fluid nodes, n = d + w rho0 < 0 and non-finite tests, j stored for the next check; the
+// last block runs the control step.  A no-op once the loop has exited.
+template <bool SWAPPED>
+__global__ void __launch_bounds__(BLOCK) k_aa_check32(const FlowArgs32 a)
+{
+    const volatile FlowCtl *vc = a.ctl;
+    if (vc->done) return;
+    const int fm = vc->check_fm;
+    const unsigned i = blockIdx.x * BLOCK + threadIdx.x;
+    double err = 0.0;
+    unsigned bad = 0;
+    if (i < a.Nf) {
+        const unsigned c = a.cpos[i];
+        const unsigned p = lattice_of(a, c);
+        const float *g = a.g0;
+        float f[Q];
+        if constexpr (SWAPPED) {
+            aa_gather_offsets(a, i, c, a.cmask[i], [&](int l, unsigned o) { f[l] = g[o]; });
+        } else {
+#pragma unroll
+            for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * a.Nf + i];
+        }
+        double drho = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+        static_for<0, Q>([&](auto L) {
+            constexpr int l = decltype(L)::value;
+            constexpr Vel v = vel(l);
+            const double d = (double)f[l];
+            drho += d;
+            jx += v.x * d;
+            jy += v.y * d;
+            jz += v.z * d;
+            const double n = d + a.w64[wclass(l)] * a.rho0d;
+            if (n < 0.0) bad |= LBGPU_ERR_NEGATIVE_POPULATION;
+            if (!(fabs(n) <= DBL_MAX)) bad |= LBGPU_ERR_NONFINITE;
+        });
+        if (fm) {
+            jx += 0.5 * (double)a.F[0];
+            jy += 0.5 * (double)a.F[1];
+            jz += 0.5 * (double)a.F[2];
+        }
+        err = fmax(fmax(fabs(jx - a.jx[p]), fabs(jy - a.jy[p])), fabs(jz - a.jz[p]));
+        a.jx[p] = jx;
+        a.jy[p] = jy;
+        a.jz[p] = jz;
+        a.rho[p] = a.rho0d + drho;
+    }
+    // block max of err (IEEE order of non-negative doubles = order of their bits) and OR of bad
+    __shared__ unsigned long long smax;
+    __shared__ unsigned sbad;
+    if (threadIdx.x == 0) {
+        smax = 0ull;
+        sbad = 0u;
+    }
+    __syncthreads();
+    if (err > 0.0 || !(err == err)) atomicMax(&smax, (unsigned long long)__double_as_longlong(err == err ? err : INFINITY));
+    if (bad) atomicOr(&sbad, bad);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        FlowCtl *c = a.ctl;
+        if (smax) atomicMax(&c->err_bits, smax);
+        if (sbad) atomicOr(&c->status, sbad);
+        __threadfence();
+        if (atomicAdd(&c->blocks_done, 1u) == gridDim.x - 1) {
+            __threadfence();
+            control_step32(c, a.hist, SWAPPED ? 1 : 0);
+        }
+    }
 }
 
 // Moments (FP64) of an AA buffer: natural order after an odd launch (SWAPPED = false), or
@@ -365,8 +485,15 @@ cudaError_t launch_flow_step_f32(const FlowArgs32 &a, unsigned grid, cudaStream_
 template <int FM, int MINB>
 static void aa_launch(const FlowArgs32 &a, bool odd, unsigned grid, cudaStream_t s)
 {
-    if (odd) k_aa32<true, FM, MINB><<<grid, BLOCK, 0, s>>>(a);
-    else k_aa32<false, FM, MINB><<<grid, BLOCK, 0, s>>>(a);
+    // the loop variant is a separate instantiation: the control-block read costs the hot
+    // fixed-step kernel ~2 % when it is only a run-time branch
+    if (a.ctl) {
+        if (odd) k_aa32<true, FM, MINB, true><<<grid, BLOCK, 0, s>>>(a);
+        else k_aa32<false, FM, MINB, true><<<grid, BLOCK, 0, s>>>(a);
+    } else {
+        if (odd) k_aa32<true, FM, MINB, false><<<grid, BLOCK, 0, s>>>(a);
+        else k_aa32<false, FM, MINB, false><<<grid, BLOCK, 0, s>>>(a);
+    }
 }
 
 template <int FM>
@@ -384,6 +511,14 @@ cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s)
     // one instantiation: with the force switched off (force_collide = 0) the force terms are
     // skipped at run time
     aa_launch_minb<7>(a, odd, odd ? a.minb_odd : a.minb_even, grid, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aa_check_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s)
+{
+    const unsigned grid = (a.Nf + BLOCK - 1) / BLOCK;
+    if (swapped) k_aa_check32<true><<<grid, BLOCK, 0, s>>>(a);
+    else k_aa_check32<false><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
 

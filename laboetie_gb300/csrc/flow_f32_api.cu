@@ -1,6 +1,7 @@
 // flow_f32_api.cu -- host side of the FP32-deviation flow path (same C ABI as FP64).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -247,6 +248,90 @@ static int aa_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms)
     LBG_CK(ctx, cudaEventRecord(ctx->ev1, s));
     LBG_CK(ctx, cudaEventSynchronize(ctx->ev1));
     LBG_CK(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    return LBGPU_OK;
+}
+
+// The reference loop of equilibration.f90:143-491 on an FP32 in-place context: graphs of
+// (AA launch of step t, check launch of S_t) pairs; each check decides the forces of the next AA
+// launch on the device, launches after the exit return at once, and the host only reads the
+// control block between graphs.
+int f32_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap, int *steps_out)
+{
+    if (!ctx->aa)
+        return ctx_fail(ctx, LBGPU_ERR_UNSUPPORTED,
+                        "lbgpu_equilibration: the FP32 reference loop runs in the in-place layout");
+    int rc = aa_tune(ctx);
+    if (rc) return rc;
+    // j_old of the first check: the moments of the current state
+    if ((rc = f32_flow_get(ctx, nullptr, nullptr, nullptr, nullptr, nullptr))) return rc;
+    cudaStream_t s = ctx->stream;
+    double *d_hist = nullptr;
+    if (hist_cap > 0) {
+        LBG_CK(ctx, cudaMallocAsync(&d_hist, sizeof(double) * hist_cap, s));
+        LBG_CK(ctx, cudaMemsetAsync(d_hist, 0, sizeof(double) * hist_cap, s));
+    }
+    FlowCtl c;
+    std::memset(&c, 0, sizeof(c));
+    c.t = 1;
+    c.max_steps = max_steps;
+    c.target_error = ctx->p.target_error;
+    c.hist_cap = hist_cap;
+    c.aa_fm = ctx->prev_force_moment;   // moments of the current state
+    c.aa_fc = 0;                        // phase A: no force (equilibration.f90:143-190)
+    c.check_fm = 0;
+    c.exit_phase = ctx->aa_phase;
+    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+    FlowArgs32 a;
+    fill_args32(ctx, a);
+    a.ctl = ctx->d_ctl;
+    a.hist = d_hist;
+    // an even number of (AA, check) pairs per graph, so every replay starts at the same phase
+    const int G = 2 * (int)std::min<long long>(128, std::max<long long>(4, (1LL << 23) / std::max<unsigned>(ctx->Nf, 1u)));
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    LBG_CK(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < G; ++k) {
+        const bool odd = ((ctx->aa_phase + k) & 1) != 0;   // an even launch leaves the state swapped
+        cudaError_t e = launch_aa_step_f32(a, odd, s);
+        if (e == cudaSuccess) e = launch_aa_check_f32(a, !odd, s);
+        if (e != cudaSuccess) {
+            cudaStreamEndCapture(s, &graph);
+            return ctx_cuda(ctx, e, "capture FP32 reference loop");
+        }
+    }
+    LBG_CK(ctx, cudaStreamEndCapture(s, &graph));
+    LBG_CK(ctx, cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    FlowCtl h;
+    rc = LBGPU_OK;
+    for (;;) {
+        cudaError_t e = cudaGraphLaunch(exec, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, ctx->d_ctl, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            rc = ctx_cuda(ctx, e, "lbgpu_equilibration (FP32)");
+            break;
+        }
+        if (h.done) break;
+    }
+    cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    ctx->aa_phase = h.exit_phase;
+    ctx->prev_force_moment = h.exit_force_moment;
+    ctx->force_last_collide = h.aa_fc;
+    ctx->prev_kind = PREV_POST;
+    if (steps_out) *steps_out = h.exit_step;
+    if (d_hist) {
+        LBG_CK(ctx, cudaMemcpyAsync(l2err_hist, d_hist, sizeof(double) * hist_cap, cudaMemcpyDeviceToHost, s));
+        LBG_CK(ctx, cudaFreeAsync(d_hist, s));
+    }
+    LBG_CK(ctx, cudaStreamSynchronize(s));
+    if (h.status & LBGPU_ERR_NEGATIVE_POPULATION)
+        return ctx_fail(ctx, LBGPU_ERR_NEGATIVE_POPULATION, "In equilibration, the population n(x,y,z,vel) < 0");
+    if (h.status & LBGPU_ERR_NONFINITE)
+        return ctx_fail(ctx, LBGPU_ERR_NONFINITE, "equilibration: non-finite population");
+    if (h.status & LBGPU_ERR_STEP_CAP)
+        return ctx_fail(ctx, LBGPU_ERR_STEP_CAP, "equilibration: step cap reached before the second convergence");
     return LBGPU_OK;
 }
 

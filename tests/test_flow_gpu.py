@@ -291,3 +291,41 @@ def test_device_profiles_equal_the_reference_profiles(oracle_mod, prec):
             flux, dens = box.profiles(axis)
             rf, rd = oracle_mod.profiles(nat, rho, j, axis)
             assert np.array_equal(flux, rf) and np.array_equal(dens, rd)
+
+
+def test_fp32_reference_loop_tracks_fp64():
+    """The reference loop (equilibration.f90:143-491) on an FP32-deviation context: the same
+    phase machine, decided on the device before each in-place step.  On the C1 slit with a
+    target above the FP32 resolution of j (1e-8; FP32 deviations of ~1e-3 resolve ~1e-10, the
+    reference's default target) both precisions converge twice and stop at nearly the same step;
+    the l2err history of the first 200 steps and the final velocity profile agree with FP64 to
+    1e-4 relative."""
+    nat = geo.slit(4, 4, 34)
+    out = {}
+    for prec in (FP64, FP32_DEV):
+        with Box(nat, relaxation_time=1.0, f_ext=(1e-5, 0, 0), target_error=1e-8, precision=prec) as box:
+            box.flow_init()
+            steps, hist = box.equilibration(max_steps=100000, hist_cap=100000)
+            _, rho, j = box.flow_get(populations=False)
+        out[prec] = (steps, hist, rho, j)
+    s64, h64, r64, j64 = out[FP64]
+    s32, h32, r32, j32 = out[FP32_DEV]
+    assert abs(s32 - s64) <= 0.05 * s64, (s32, s64)
+    assert np.allclose(h32[:200], h64[:200], rtol=1e-4, atol=0)
+    assert np.max(np.abs(j32[0] - j64[0])) <= 1e-4 * np.abs(j64[0]).max()
+    assert np.max(np.abs(r32 - r64)) < 1e-6
+
+
+def test_fp32_reference_loop_errors():
+    nat = geo.slit(4, 4, 12)
+    with Box(nat, relaxation_time=1.0, f_ext=(1e-5, 0, 0), target_error=1e-10, precision=FP32_DEV) as box:
+        box.flow_init()
+        with pytest.raises(LbgpuError) as e:
+            box.equilibration(max_steps=7, hist_cap=7)
+        assert e.value.status & (1 << 5)
+        n, rho, j = box.flow_get()
+        n[2, 4, 1, 1] = np.inf
+        box.flow_set(n, rho, j)
+        with pytest.raises(LbgpuError) as e:
+            box.equilibration(max_steps=100, hist_cap=100)
+        assert e.value.status & (1 << 3)
