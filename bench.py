@@ -591,7 +591,8 @@ def main():
         "config": {"workload": WORKLOAD, "boxes": world,
                    "parallelism": "replicas" if world > 1 else "single",
                    "fluid_nodes": nfluid, "nodes": int(nature.size),
-                   "l2": "inputs larger than L2 (538 MB of FP32 populations per buffer)"},
+                   "l2": f"inputs larger than L2: {round(BYTES_F32 / 2 * nfluid / 1e6)} MB of FP32 populations "
+                         "(fluid nodes only) against the 129 MB L2; no flush between steps"},
         "roofline": {"bound": "hbm", "achieved": round(achieved32, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved32 / hbm, 4), "peak_kind": peak_kind,
                      "traffic": (round(tr * nfluid) if tr else None),
