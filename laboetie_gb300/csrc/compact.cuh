@@ -41,8 +41,10 @@ __device__ __forceinline__ unsigned lattice_of(const A &a, unsigned c)
 // Within a lattice row the fluid nodes are consecutive compact indices, so one table lookup per
 // neighbouring row gives cnt = the compact index the node x would have in that row (fluid nodes
 // before x); its neighbours x -+ 1 in the row are then cnt - 1 and cnt + fluid(x) (x - 1 and
-// x + 1 fluid), and the node's own row needs no lookup (cnt = i).  Only a wrap across the
-// periodic x boundary takes a second lookup.
+// x + 1 fluid), and the node's own row needs no lookup (cnt = i).  The eight lookups are made
+// up front, independent of the bounce-back bits, so that they are in flight together and each
+// serves every direction into its row; only a wrap across the periodic x boundary takes a second
+// lookup.
 template <typename A, typename Fn>
 __device__ __forceinline__ void aa_gather_offsets(const A &a, unsigned i, unsigned c,
                                                   uint32_t m, Fn &&f)
@@ -59,33 +61,36 @@ __device__ __forceinline__ void aa_gather_offsets(const A &a, unsigned i, unsign
     const int w = x >> 5, b = x & 31;
     const uint32_t below = (1u << b) - 1u;
     const uint2 *__restrict__ tab = a.rowtab;
+    // neighbouring rows, slot k = 3 (c.y + 1) + (c.z + 1) (k = 4: the node's own row)
+    uint2 e[9];
+    static_for<0, 9>([&](auto K) {
+        constexpr int k = decltype(K)::value;
+        if constexpr (k != 4) e[k] = __ldg(tab + (unsigned)(R[k / 3] + Z[k % 3]) * (unsigned)nw + w);
+    });
     static_for<0, Q>([&](auto L) {
         constexpr int l = decltype(L)::value;
         constexpr Vel v = vel(l);
         if constexpr (l == 0) {
             f(0, i);
         } else {
-            unsigned o;
-            if ((m >> l) & 1u) {
-                o = (unsigned)l * Nf + i;
+            constexpr int k = 3 * (v.y + 1) + (v.z + 1);
+            unsigned s;
+            if constexpr (k == 4) {
+                // own row: the fluid neighbour x - c.x is the previous / next compact node
+                const unsigned rb = row * (unsigned)nw;
+                if constexpr (v.x > 0) s = x > 0 ? i - 1u : compact_in_row(tab, rb, lx - 1);
+                else s = x < lx - 1 ? i + 1u : compact_in_row(tab, rb, 0);
             } else {
-                unsigned s;
-                if constexpr (v.y == 0 && v.z == 0) {
-                    // own row: the fluid neighbour x - c.x is the previous / next compact node
-                    const unsigned rb = row * (unsigned)nw;
-                    if constexpr (v.x > 0) s = x > 0 ? i - 1u : compact_in_row(tab, rb, lx - 1);
-                    else s = x < lx - 1 ? i + 1u : compact_in_row(tab, rb, 0);
+                const unsigned cnt = e[k].y + (unsigned)__popc(e[k].x & below);
+                if constexpr (v.x == 0) {
+                    s = cnt;
                 } else {
                     const unsigned rb = (unsigned)(R[v.y + 1] + Z[v.z + 1]) * (unsigned)nw;
-                    const uint2 e = __ldg(tab + rb + w);
-                    const unsigned cnt = e.y + (unsigned)__popc(e.x & below);
-                    if constexpr (v.x == 0) s = cnt;
-                    else if constexpr (v.x > 0) s = x > 0 ? cnt - 1u : compact_in_row(tab, rb, lx - 1);
-                    else s = x < lx - 1 ? cnt + ((e.x >> b) & 1u) : compact_in_row(tab, rb, 0);
+                    if constexpr (v.x > 0) s = x > 0 ? cnt - 1u : compact_in_row(tab, rb, lx - 1);
+                    else s = x < lx - 1 ? cnt + ((e[k].x >> b) & 1u) : compact_in_row(tab, rb, 0);
                 }
-                o = (unsigned)inv(l) * Nf + s;
             }
-            f(l, o);
+            f(l, ((m >> l) & 1u) ? (unsigned)l * Nf + i : (unsigned)inv(l) * Nf + s);
         }
     });
 }
