@@ -92,6 +92,24 @@ int lbgpu_interfacial(lbgpu_ctx *ctx, uint8_t *out);
 /* counts[0..3] = fluid, solid, fluid&interfacial, solid&interfacial node counts. */
 int lbgpu_node_counts(lbgpu_ctx *ctx, long long counts[4]);
 
+/* ---------------------------------------------------------------- geometry on the device
+ * The builders of module_geometry.f90 selected by geometryLabel (supercell_definition.f90:52-80)
+ * evaluated on the GPU: -1 no solid, 1 slit, 2 cylinder, 3 cc, 4 disc, 5 sinusoidal walls,
+ * 6 planes with two radii, 7 tube with varying diameter (params = {lw_o_lx, a_o_R}, the two
+ * numbers of tube.in), 8 spherical cavity, 9 sphere, 10 cylinders between walls; the others take
+ * params = NULL.  Distances are gfortran's NORM2 with separately rounded operations, so every
+ * node falls on the reference's side of each threshold.  Labels 0 (geom.in) and 11 (geom.pbm)
+ * read files: the host parses them and passes nature to lbgpu_create.
+ * The reference's STOP conditions (e.g. label 2 with lx /= ly) and a box without fluid node
+ * ("All nodes are solid: no fluid, no fluid dynamics!", supercell_definition.f90:92-94) return
+ * LBGPU_ERR_INVALID with the reference's message in lbgpu_last_error(NULL, ...); they are
+ * checked before any device work, so they are reported without a GPU too.
+ * lbgpu_geometry writes nature(lx,ly,lz) (0 fluid, 1 solid, x fastest) to the host array
+ * nature; lbgpu_create_label is lbgpu_create on the box built on the device (p->lx, ly, lz). */
+int lbgpu_geometry(int device, int label, int lx, int ly, int lz, const double *params,
+                   int8_t *nature);
+int lbgpu_create_label(const lbgpu_params *p, int label, const double *params, lbgpu_ctx **out);
+
 /* ---------------------------------------------------------------- flow: state transfer */
 
 /* init_simu.f90:283-291 on the device: density = rho0 on fluid, 0 on solid; n_l = w_l*density;

@@ -108,6 +108,12 @@ int force_mask(const double f[3])
 
 }  // namespace lbg
 
+namespace lbg {
+int geometry_build(int label, int lx, int ly, int lz, const double *params, int8_t *d_nature,
+                   long long *nfluid, cudaStream_t s, std::string &err);
+int geometry_check(int label, int lx, int ly, int lz, const double *params, std::string &err);
+}  // namespace lbg
+
 extern "C" {
 
 void lbgpu_default_params(lbgpu_params *p, int lx, int ly, int lz)
@@ -164,6 +170,60 @@ int lbgpu_create(const lbgpu_params *p, const int8_t *nature, lbgpu_ctx **out)
     }
     *out = ctx;
     return LBGPU_OK;
+}
+
+int lbgpu_geometry(int device, int label, int lx, int ly, int lz, const double *params, int8_t *nature)
+{
+    if (!nature) return fail_global(LBGPU_ERR_INVALID, "lbgpu_geometry: null nature");
+    if (lx <= 0 || ly <= 0 || lz <= 0)
+        return fail_global(LBGPU_ERR_INVALID, "lbgpu_geometry: lx, ly, lz must be > 0");
+    const long long N = (long long)lx * ly * lz;
+    if (N >= (1LL << 31)) return fail_global(LBGPU_ERR_INVALID, "lbgpu_geometry: more than 2^31 nodes");
+    std::string err;
+    if (geometry_check(label, lx, ly, lz, params, err)) return fail_global(LBGPU_ERR_INVALID, err);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail_global(LBGPU_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail_global(LBGPU_ERR_INVALID, "bad device ordinal");
+    if ((e = cudaSetDevice(device)) != cudaSuccess)
+        return fail_global(LBGPU_ERR_CUDA, std::string("lbgpu_geometry: ") + cudaGetErrorString(e));
+    cudaStream_t s = nullptr;
+    int8_t *d = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMallocAsync(&d, (size_t)N, s)) != cudaSuccess) {
+        if (s) cudaStreamDestroy(s);
+        return fail_global(LBGPU_ERR_CUDA, std::string("lbgpu_geometry: ") + cudaGetErrorString(e));
+    }
+    long long nfluid = 0;
+    int rc = geometry_build(label, lx, ly, lz, params, d, &nfluid, s, err);
+    if (rc == LBGPU_OK) {
+        e = cudaMemcpyAsync(nature, d, (size_t)N, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            rc = LBGPU_ERR_CUDA;
+            err = std::string("lbgpu_geometry: ") + cudaGetErrorString(e);
+        }
+    }
+    cudaFreeAsync(d, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc ? fail_global(rc, err) : LBGPU_OK;
+}
+
+int lbgpu_create_label(const lbgpu_params *p, int label, const double *params, lbgpu_ctx **out)
+{
+    if (!p || !out) return fail_global(LBGPU_ERR_INVALID, "lbgpu_create_label: null argument");
+    *out = nullptr;
+    if (p->lx <= 0 || p->ly <= 0 || p->lz <= 0)
+        return fail_global(LBGPU_ERR_INVALID, "lbgpu_create_label: lx, ly, lz must be > 0");
+    const long long N = (long long)p->lx * p->ly * p->lz;
+    if (N >= (1LL << 31)) return fail_global(LBGPU_ERR_INVALID, "lbgpu_create_label: more than 2^31 nodes");
+    // the compact layout of FP32 boxes is planned on the host, so the box comes back once
+    std::vector<int8_t> nature((size_t)N);
+    const int rc = lbgpu_geometry(p->device, label, p->lx, p->ly, p->lz, params, nature.data());
+    if (rc) return rc;
+    return lbgpu_create(p, nature.data(), out);
 }
 
 void lbgpu_destroy(lbgpu_ctx *ctx)

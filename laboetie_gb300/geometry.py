@@ -105,6 +105,87 @@ def tube_varying_diameter(lx, ly, lz, lw_o_lx=0.5, a_o_R=0.5):
     return np.where(fluid, FLUID, SOLID).astype(np.int8)
 
 
+def disc_benichou(lx, ly, lz):
+    """geometryLabel = 4: a disc of radius (lx-1)/2 with four exits, along z
+    (module_geometry.f90:336-378); lx == ly, odd."""
+    if lx != ly or lx % 2 == 0:
+        raise ValueError("disc needs lx == ly, odd")
+    i, j, _ = _grid(lx, ly, lz)
+    ox, oy = (lx + 1) / 2.0, (ly + 1) / 2.0
+    radius = float(norm2(1.0 - ox, float((lx + 1) // 2) - oy))
+    return np.where(norm2(i - ox, j - oy) > radius, SOLID, FLUID).astype(np.int8)
+
+
+def sinusoidal_walls(lx, ly, lz):
+    """geometryLabel = 5: a channel along x between walls y = +-(a sin(2 pi (i-1)/lx) + b) about
+    the middle row (module_geometry.f90:122-153); ly odd."""
+    if ly % 2 == 0:
+        raise ValueError("sinusoidal walls need an odd ly")
+    midly = (ly + 1) // 2
+    b = float(np.float32(np.float32(2.0) / np.float32(3.0)) * np.float32(midly))   # 2./3.*midly, REAL
+    a = float(midly) - b - 1.0
+    if a <= 0.0 or b <= 0.0:
+        raise ValueError("sinusoidal walls: amplitude or offset not positive")
+    nat = np.zeros((lz, ly, lx), dtype=np.int8)
+    for i in range(1, lx + 1):
+        yi = a * math.sin(2.0 * math.pi * float(i - 1) / float(lx)) + b + float(midly)
+        ay = abs(yi)
+        ninty = (int(math.floor(ay)) + (1 if ay - math.floor(ay) >= 0.5 else 0)) * (1 if yi >= 0 else -1)   # NINT
+        for jj in range(midly, ly + 1):
+            v = FLUID if jj < ninty else SOLID
+            nat[:, jj - 1, i - 1] = v
+            nat[:, 2 * midly - jj - 1, i - 1] = v
+    return nat
+
+
+def planes_two_radii(lx, ly, lz):
+    """geometryLabel = 6: walls at y = 1 and y = ly, narrowed by (ly-2)/4 rows on each side for
+    x > lx/2 (module_geometry.f90:96-119)."""
+    nat = np.zeros((lz, ly, lx), dtype=np.int8)
+    nat[:, 0, :] = SOLID
+    nat[:, ly - 1, :] = SOLID
+    q = (ly - 2) // 4 if ly >= 2 else 0
+    for i in range(1, lx + 1):
+        if i > lx // 2:
+            for jj in range(2, 1 + q + 1):
+                nat[:, jj - 1, i - 1] = SOLID
+            for jj in range(ly - q, ly):
+                nat[:, jj - 1, i - 1] = SOLID
+    return nat
+
+
+def sphere_benichou(lx, ly, lz):
+    """geometryLabel = 9: a spherical cavity with six exits (module_geometry.f90:287-331);
+    cubic box, odd side."""
+    if not (lx == ly == lz) or lx % 2 == 0:
+        raise ValueError("sphere needs a cubic box with odd side")
+    i, j, k = _grid(lx, ly, lz)
+    o = (lx + 1) / 2.0
+    radius = float(norm2(1.0 - o, float((ly + 1) // 2) - o, float((lz + 1) // 2) - o))
+    return np.where(norm2(i - o, j - o, k - o) > radius, SOLID, FLUID).astype(np.int8)
+
+
+def cylinders_between_walls(lx, ly, lz):
+    """geometryLabel = 10: four cylinders of radius 0.2 lx centred on the edges of an lx x ly
+    cell (ly = lx sqrt 3 within 5 %) between walls at z = 1 and z = lz
+    (module_geometry.f90:11-49)."""
+    s3 = np.float32(math.sqrt(3.0))
+    if abs(np.float32(ly) / np.float32(lx) - s3) / s3 >= np.float32(0.05):
+        raise ValueError("ly should be lx*sqrt(3)")
+    if lz < 3:
+        raise ValueError("lz should be greater than 2")
+    i, j, _ = _grid(lx, ly, lz)
+    midx, midy = (lx + 1) / 2.0, (ly + 1) / 2.0
+    radius = 0.2 * lx
+    solid = np.zeros(i.shape, dtype=bool)
+    for cx, cy in ((1.0, midy), (float(lx), midy), (midx, 1.0), (midx, float(ly))):
+        solid |= norm2(i - cx, j - cy) <= radius
+    nat = solid.astype(np.int8)
+    nat[0] = SOLID
+    nat[-1] = SOLID
+    return nat
+
+
 def custom(lx, ly, lz, solid_nodes):
     """geometryLabel = 0: list of 1-based (i, j, k) solid nodes as in geom.in
     (module_geometry.f90:380-426)."""
@@ -124,6 +205,47 @@ def read_geom_in(path, lx, ly, lz):
             if len(parts) >= 3:
                 nodes.append(tuple(int(p) for p in parts[:3]))
     return custom(lx, ly, lz, nodes)
+
+
+def read_pbm(path, lx, ly, lz):
+    """geometryLabel = 11: a plain PBM image (P1) of ly columns and lz lines, '1' = solid, in the
+    plane x = 1 (module_geometry.f90:430-511); lx must be 1."""
+    if lx != 1:
+        raise ValueError("lx must be 1 if geom.pbm is used")
+    with open(path) as fh:
+        tokens = fh.read().split()
+    if not tokens or tokens[0] != "P1":
+        raise ValueError("geom.pbm: magic number is not P1")
+    ncol, nline = int(tokens[1]), int(tokens[2])
+    if ncol != ly or nline != lz:
+        raise ValueError("geom.pbm: columns / lines differ from ly / lz")
+    pix = "".join(tokens[3:])
+    if len(pix) < ncol * nline or set(pix[:ncol * nline]) - {"0", "1"}:
+        raise ValueError("geom.pbm: pixels must be 0 or 1")
+    nat = np.zeros((lz, ly, 1), dtype=np.int8)
+    nat[:, :, 0] = (np.frombuffer(pix[:ncol * nline].encode(), dtype=np.uint8) - ord("0")).reshape(nline, ncol)
+    return nat
+
+
+LABELS = {-1: bulk, 1: slit, 2: cylinder, 3: cc, 4: disc_benichou, 5: sinusoidal_walls,
+          6: planes_two_radii, 7: tube_varying_diameter, 8: spherical_cavity, 9: sphere_benichou,
+          10: cylinders_between_walls}
+
+
+def build(label, lx, ly, lz, params=None):
+    """The builder of geometryLabel `label` (supercell_definition.f90:52-80); label 7 takes
+    params = (lw_o_lx, a_o_R), the two numbers of tube.in.  Labels 0 (geom.in) and 11 (geom.pbm)
+    read files: read_geom_in, read_pbm."""
+    if label not in LABELS:
+        raise ValueError(f"geometryLabel {label}: no builder (0 and 11 read geom.in / geom.pbm)")
+    if label == 7:
+        lw, ar = params if params is not None else (0.5, 0.5)
+        nat = tube_varying_diameter(lx, ly, lz, lw, ar)
+    else:
+        nat = LABELS[label](lx, ly, lz)
+    if not (nat == FLUID).any():
+        raise ValueError("All nodes are solid: no fluid, no fluid dynamics!")
+    return nat
 
 
 def write_geom_in(path, nature):

@@ -121,6 +121,8 @@ def library():
         ("lbgpu_compensated_force_field", [vp, i, vp, i, vp, vp, vp]),
         ("lbgpu_set_force_field", [vp, vp, vp, vp]),
         ("lbgpu_profiles", [vp, i, vp, vp]),
+        ("lbgpu_geometry", [i, i, i, i, i, vp, vp]),
+        ("lbgpu_create_label", [C.POINTER(Params), i, vp, C.POINTER(vp)]),
     ):
         if hasattr(L, name):
             getattr(L, name).argtypes = args
@@ -151,9 +153,31 @@ class Box:
         nature = np.ascontiguousarray(nature, dtype=np.int8)
         if nature.ndim != 3:
             raise ValueError("nature must be (lz, ly, lx)")
-        self.shape = nature.shape
         lz, ly, lx = nature.shape
-        self.N = nature.size
+        self._setup(lx, ly, lz, relaxation_time, f_ext, target_error, rho0, precision, device)
+        rc = self.L.lbgpu_create(C.byref(self.params), nature.ctypes.data, C.byref(self.ctx))
+        if rc:
+            raise LbgpuError(rc, self._msg(None))
+        self.nature = nature
+
+    @classmethod
+    def from_label(cls, label, lx, ly, lz, params=None, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0),
+                   target_error=1e-10, rho0=1.0, precision=FP64, device=0):
+        """A box of the reference's geometryLabel `label` built on the device
+        (lbgpu_create_label); params: (lw_o_lx, a_o_R) for label 7."""
+        self = cls.__new__(cls)
+        self.L = library()
+        self._setup(lx, ly, lz, relaxation_time, f_ext, target_error, rho0, precision, device)
+        par = None if params is None else (C.c_double * len(params))(*params)
+        rc = self.L.lbgpu_create_label(C.byref(self.params), label, par, C.byref(self.ctx))
+        if rc:
+            raise LbgpuError(rc, self._msg(None))
+        self.nature = device_geometry(label, lx, ly, lz, params, device)
+        return self
+
+    def _setup(self, lx, ly, lz, relaxation_time, f_ext, target_error, rho0, precision, device):
+        self.shape = (lz, ly, lx)
+        self.N = lx * ly * lz
         p = Params()
         self.L.lbgpu_default_params(C.byref(p), lx, ly, lz)
         p.relaxation_time = relaxation_time
@@ -164,10 +188,6 @@ class Box:
         p.device = device
         self.params = p
         self.ctx = C.c_void_p()
-        rc = self.L.lbgpu_create(C.byref(p), nature.ctypes.data, C.byref(self.ctx))
-        if rc:
-            raise LbgpuError(rc, self._msg(None))
-        self.nature = nature
 
     # -------------------------------------------------------------- helpers
     def _msg(self, ctx):
@@ -494,6 +514,20 @@ def _batch_lib():
         f.argtypes = args
         f.restype = res
     return L
+
+
+def device_geometry(label, lx, ly, lz, params=None, device=0):
+    """nature (lz, ly, lx) int8 of the reference's geometryLabel `label`, built on the device
+    (lbgpu_geometry); LbgpuError with the reference's message for a box it refuses."""
+    L = library()
+    nat = np.zeros((lz, ly, lx), dtype=np.int8)
+    par = None if params is None else (C.c_double * len(params))(*params)
+    rc = L.lbgpu_geometry(device, label, lx, ly, lz, par, nat.ctypes.data)
+    if rc:
+        buf = C.create_string_buffer(1024)
+        L.lbgpu_last_error(None, buf, 1024)
+        raise LbgpuError(rc, buf.value.decode(errors="replace"))
+    return nat
 
 
 def footprint(cell: Cell) -> int:

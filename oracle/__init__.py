@@ -107,6 +107,7 @@ def lib():
         L.orc_pnp.argtypes = [_int, _int, _int, _i8, _d, _d, _d, _d, _d, _int, _dp, _dp, _dp,
                               _pd, _int, _pi, _pi]
         L.orc_profiles.argtypes = [_int, _int, _int] + [_dp] * 4 + [_int, _dp, _dp]
+        L.orc_geometry.argtypes = [_int, _int, _int, _int, _vp, _vp]
         L.orc_profiles.restype = None
         _lib = L
     return _lib
@@ -330,3 +331,12 @@ def profiles(nature, rho, j, axis):
     dens = np.zeros(L)
     lib().orc_profiles(lx, ly, lz, *arrs, axis, flux, dens)
     return flux, dens
+
+
+def geometry(label, lx, ly, lz, params=None):
+    """module_geometry.f90 builder of geometryLabel `label`: (code, nature (lz, ly, lx) int8);
+    code 0, or 1 shape / 2 parameters / 3 label / 4 no fluid node (the reference's STOPs)."""
+    nat = np.zeros((lz, ly, lx), dtype=np.int8)
+    p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+    code = lib().orc_geometry(label, lx, ly, lz, None if p is None else p.ctypes.data, nat.ctypes.data)
+    return code, nat

@@ -868,3 +868,194 @@ void orc_profiles(int lx, int ly, int lz, const double *density, const double *j
         mean_density[k] = sd / (double)(cnt > 0 ? cnt : 1);   /* MAX(COUNT(...), 1) */
     }
 }
+
+/* ------------------------------------------------------------------ geometry builders */
+
+/* gfortran's inline NORM2 (scaled sum of squares, scale starting at 1): the reference's
+ * distance in every builder of module_geometry.f90. */
+static double orc_norm2(int n, const double *v)
+{
+    double scale = 1.0, ssq = 0.0;
+    for (int q = 0; q < n; ++q) {
+        if (v[q] != 0.0) {
+            const double ax = fabs(v[q]);
+            if (scale < ax) {
+                const double t = scale / ax;
+                ssq = 1.0 + ssq * t * t;
+                scale = ax;
+            } else {
+                const double t = ax / scale;
+                ssq = ssq + t * t;
+            }
+        }
+    }
+    return scale * sqrt(ssq);
+}
+
+static double n2(double a, double b)
+{
+    const double v[2] = {a, b};
+    return orc_norm2(2, v);
+}
+
+static double n3(double a, double b, double c)
+{
+    const double v[3] = {a, b, c};
+    return orc_norm2(3, v);
+}
+
+int orc_geometry(int label, int lx, int ly, int lz, const double *params, int8_t *nature)
+{
+    const long long N = (long long)lx * ly * lz;
+    if (lx < 1 || ly < 1 || lz < 1) return 1;
+#define NAT(i, j, k) nature[((i) - 1) + (long long)lx * (((j) - 1) + (long long)ly * ((k) - 1))]
+    for (long long q = 0; q < N; ++q) nature[q] = 0;   /* supercell_definition.f90:45 */
+    switch (label) {
+    case -1:
+        break;
+    case 1:   /* module_geometry.f90:158-166 */
+        for (int j = 1; j <= ly; ++j)
+            for (int i = 1; i <= lx; ++i) {
+                NAT(i, j, 1) = 1;
+                NAT(i, j, lz) = 1;
+            }
+        break;
+    case 2: { /* module_geometry.f90:253-277 */
+        if (lx != ly || lx < 3) return 1;
+        const double ox = (double)(lx + 1) / 2.0, oy = (double)(ly + 1) / 2.0;
+        const double radius = (double)(lx - 1) / 2.0;
+        for (int i = 1; i <= lx; ++i)
+            for (int j = 1; j <= ly; ++j) {
+                const int8_t v = n2((double)i - ox, (double)j - oy) >= radius;
+                for (int k = 1; k <= lz; ++k) NAT(i, j, k) = v;
+            }
+        break;
+    }
+    case 3: { /* module_geometry.f90:206-245 */
+        if (lx != ly || lx != lz) return 1;
+        const double thr = (double)(lx - 1) * sqrt(3.0) / 4.0;
+        const double cen[9][3] = {{1, 1, 1}, {lx, 1, 1}, {1, ly, 1}, {1, 1, lz}, {lx, ly, 1},
+                                  {lx, 1, lz}, {1, ly, lz}, {lx, ly, lz},
+                                  {(double)(float)(lx + 1) / 2.0, (double)(float)(ly + 1) / 2.0,
+                                   (double)(float)(lz + 1) / 2.0}};
+        for (int k = 1; k <= lz; ++k)
+            for (int j = 1; j <= ly; ++j)
+                for (int i = 1; i <= lx; ++i) {
+                    int in = 0;
+                    for (int c = 0; c < 9; ++c)
+                        if (n3((double)i - cen[c][0], (double)j - cen[c][1], (double)k - cen[c][2]) <= thr) in = 1;
+                    NAT(i, j, k) = (int8_t)in;
+                }
+        break;
+    }
+    case 4: { /* module_geometry.f90:336-378 */
+        if (lx != ly || lx % 2 == 0) return 1;
+        const double ox = (double)(lx + 1) / 2.0, oy = (double)(ly + 1) / 2.0;
+        const double radius = n2(1.0 - ox, (double)((lx + 1) / 2) - oy);
+        for (int i = 1; i <= lx; ++i)
+            for (int j = 1; j <= ly; ++j) {
+                const int8_t v = n2((double)i - ox, (double)j - oy) > radius;
+                for (int k = 1; k <= lz; ++k) NAT(i, j, k) = v;
+            }
+        break;
+    }
+    case 5: { /* module_geometry.f90:122-153 */
+        if (ly % 2 == 0) return 1;
+        const int midly = (ly + 1) / 2;
+        const double b = (double)((float)(2.0f / 3.0f) * (float)midly);   /* 2./3.*midly, REAL */
+        const double a = (double)midly - b - 1.0;
+        if (a <= 0.0 || b <= 0.0) return 2;
+        const double pi = 3.141592653589793;   /* acos(-1.0_dp) */
+        for (int i = 1; i <= lx; ++i) {
+            const double xi = (double)(i - 1);
+            const double yi = a * sin(2.0 * pi * xi / (double)lx) + b + (double)midly;
+            const long ninty = lround(yi);   /* NINT: half away from zero */
+            for (int j = midly; j <= ly; ++j) {
+                const int8_t v = (long)j < ninty ? 0 : 1;
+                const int mirror = 2 * midly - j;
+                for (int k = 1; k <= lz; ++k) {
+                    NAT(i, j, k) = v;
+                    NAT(i, mirror, k) = v;
+                }
+            }
+        }
+        break;
+    }
+    case 6: { /* module_geometry.f90:96-119 */
+        for (int k = 1; k <= lz; ++k)
+            for (int i = 1; i <= lx; ++i) {
+                NAT(i, 1, k) = 1;
+                NAT(i, ly, k) = 1;
+                if (i > lx / 2) {
+                    for (int j = 2; j <= 1 + (ly - 2) / 4; ++j) NAT(i, j, k) = 1;
+                    for (int j = ly - (ly - 2) / 4; j <= ly - 1; ++j) NAT(i, j, k) = 1;
+                }
+            }
+        break;
+    }
+    case 7: { /* module_geometry.f90:52-89 */
+        if (ly != lz) return 1;
+        if (!params) return 2;
+        const double lw_o_lx = params[0], a_o_R = params[1];
+        const double R = (double)((float)(ly - 1) / 2.0f);   /* real(ly-1)/2.0, REAL */
+        const double a = a_o_R * R;
+        const double r0y = (double)((float)(ly + 1) / 2.0f), r0z = (double)((float)(lz + 1) / 2.0f);
+        for (int k = 1; k <= lz; ++k)
+            for (int j = 1; j <= ly; ++j) {
+                const double d = n2((double)(float)j - r0y, (double)(float)k - r0z);
+                for (int i = 1; i <= lx; ++i) {
+                    const int fluid = (double)i > lw_o_lx * (double)lx ? d < a : d < R;
+                    NAT(i, j, k) = fluid ? 0 : 1;
+                }
+            }
+        break;
+    }
+    case 8: { /* module_geometry.f90:173-198 */
+        if (lx != ly || lx != lz || lx < 3) return 1;
+        const double o = (double)(lx + 1) / 2.0, radius = (double)(lx - 1) / 2.0;
+        for (int k = 1; k <= lz; ++k)
+            for (int j = 1; j <= ly; ++j)
+                for (int i = 1; i <= lx; ++i)
+                    NAT(i, j, k) = n3((double)i - o, (double)j - o, (double)k - o) >= radius;
+        break;
+    }
+    case 9: { /* module_geometry.f90:287-331 */
+        if (lx != ly || lx != lz || lx % 2 == 0) return 1;
+        const double o = (double)(lx + 1) / 2.0;
+        const double radius = n3(1.0 - o, (double)((ly + 1) / 2) - o, (double)((lz + 1) / 2) - o);
+        for (int k = 1; k <= lz; ++k)
+            for (int j = 1; j <= ly; ++j)
+                for (int i = 1; i <= lx; ++i)
+                    NAT(i, j, k) = n3((double)i - o, (double)j - o, (double)k - o) > radius;
+        break;
+    }
+    case 10: { /* module_geometry.f90:11-49 */
+        const float s3 = sqrtf(3.0f);
+        if (fabsf((float)ly / (float)lx - s3) / s3 >= 0.05f) return 1;
+        if (lz < 3) return 1;
+        const double midx = (double)(lx + 1) / 2.0, midy = (double)(ly + 1) / 2.0;
+        const double cx[4] = {1.0, (double)lx, midx, midx}, cy[4] = {midy, midy, 1.0, (double)ly};
+        const double radius = 0.2 * (double)lx;
+        for (int i = 1; i <= lx; ++i)
+            for (int j = 1; j <= ly; ++j) {
+                int in = 0;
+                for (int c = 0; c < 4 && !in; ++c)
+                    if (n2((double)i - cx[c], (double)j - cy[c]) <= radius) in = 1;
+                if (in)
+                    for (int k = 1; k <= lz; ++k) NAT(i, j, k) = 1;
+            }
+        for (int j = 1; j <= ly; ++j)
+            for (int i = 1; i <= lx; ++i) {
+                NAT(i, j, 1) = 1;
+                NAT(i, j, lz) = 1;
+            }
+        break;
+    }
+    default:
+        return 3;
+    }
+#undef NAT
+    for (long long q = 0; q < N; ++q)   /* supercell_definition.f90:92-94 */
+        if (nature[q] == 0) return 0;
+    return 4;
+}

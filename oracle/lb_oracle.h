@@ -155,6 +155,14 @@ int orc_pnp(int lx, int ly, int lz, const int8_t *nature, double bjl, double sig
 void orc_profiles(int lx, int ly, int lz, const double *density, const double *jx,
                   const double *jy, const double *jz, int axis, double *flux, double *mean_density);
 
+/* module_geometry.f90 builders selected by geometryLabel (supercell_definition.f90:52-80):
+ * -1 no solid, 1 slit, 2 cylinder, 3 cc, 4 disc (Benichou), 5 sinusoidal walls, 6 planes with
+ * two radii, 7 tube with varying diameter (params = {lw_o_lx, a_o_R} of tube.in), 8 spherical
+ * cavity, 9 sphere (Benichou), 10 cylinders between walls.  nature(lx,ly,lz) x fastest, 0 fluid,
+ * 1 solid.  Returns 0, or the number of the reference's STOP condition that the box meets
+ * (1: shape, 2: parameters, 3: label outside -1..10 or file-based (0, 11), 4: no fluid node). */
+int orc_geometry(int label, int lx, int ly, int lz, const double *params, int8_t *nature);
+
 #ifdef __cplusplus
 }
 #endif
