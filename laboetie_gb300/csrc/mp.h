@@ -53,6 +53,10 @@ struct MpArgs32 {
     const float4 *V;                   // (j + f_ext)/rho at every fluid node (w unused)
     float4 *P[2];                      // propagated quantity (x, y, z, 0), now/next by parity
     float4 *A[2];                      // adsorbed part
+    // per fluid node, fixed for the run (set by the init pass): u* = sum_l c_l sp_out(l) and
+    // D = sum_l sp_in(l) - sum_l sp_out(l), with sp_in / sp_out the link's scattering into the
+    // node from r + c_l / out of it towards r + c_l (0 across a bounce-back link)
+    float4 *aux;                       // (u*x, u*y, u*z, D)
     double *partial;
     MpCtl *ctl;
     double *hist;

@@ -174,6 +174,7 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
             if ((rc = alloc_zero(ctx, s, &b.P[q], (size_t)N))) return rc;
             if (s->ads && (rc = alloc_zero(ctx, s, &b.A[q], (size_t)N))) return rc;
         }
+        if ((rc = alloc_zero(ctx, s, &b.aux, (size_t)N))) return rc;
         b.partial = a.partial;
         b.ctl = a.ctl;
         b.N = N;

@@ -4,10 +4,11 @@
 //   n_l/rho - w_l + lambda w_l/2 = a1_l (c_l . V(r)) + lambda w_l / 2,   V = (j + f_ext)/rho
 // (drop_tracers.f90:97-100 divided by rho), so every probability of a step follows from V at
 // the node and at its neighbours.  V and the propagated quantity P are stored as float4
-// records (x, y, z, unused).  Boxes at least 32 x 8 wide are stepped by k_mp32_slab, which
-// stages planes of V and P in shared memory (mp_slab.cuh); others by k_mp32, where a link costs
-// two 16-byte gathers.  A step moves 40 algorithmic bytes per fluid node (V and P read, P
-// written, the flag word); the VACF node sum is formed per thread in FP32 over a few nodes and
+// records (x, y, z, unused); the init pass also stores each fluid node's fixed (u*, D) (below).
+// Boxes at least 32 x 8 wide are stepped by k_mp32_slab, which stages planes of V and P in shared
+// memory (mp_slab.cuh); others by k_mp32, where a link costs two 16-byte gathers.  A step moves
+// 40 algorithmic bytes per fluid node (V and P read, P written, the flag word; the code also
+// reads the node's (u*, D)); the VACF node sum is formed per thread in FP32 over a few nodes and
 // in FP64 across threads and blocks.  Solid neighbours hold V = 0 and P = 0 and their links are
 // masked to zero, so the gathers are branch-free and can all be in flight at once.
 #include "common.cuh"
@@ -33,12 +34,17 @@ __device__ __forceinline__ float cdot(const float4 &v)
     return s;
 }
 
-// INIT: P(t=1) and VACF(0) (module_moment_propagation.f90:112-136); else one step
-// (module_moment_propagation.f90:207-253) in flux form:
-//   P_next(r) = P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)]   (+ adsorption terms)
+// INIT: P(t=1) and VACF(0) (module_moment_propagation.f90:112-136), and the node's fixed
+// aux = (u*, D); else one step (module_moment_propagation.f90:207-253) in difference form:
+//   P_next(r) = P(r) + [sum_l sp_in(l) (P(r+c_l) - P(r)) + D P(r)]   (+ adsorption terms)
 // which is (1 - sum sp_out) P(r) + sum_l P(r+c_l) sp_in(l) without ever forming the remaining
 // fraction 1 - sum sp_out, whose FP32 rounding would otherwise bias the total probability by
-// the same amount at every step.
+// the same amount at every step: the bracket is a small correction to P(r) wherever P varies
+// slowly, and D (a sum of exact FP32 link values formed in FP64) is a small net in-minus-out
+// scattering.  The outgoing scatterings enter a step only through u* (the VACF) and D, both fixed
+// for the run, so a step evaluates the 18 incoming ones and no outgoing one.
+// The per-link operations (mp32_scatter, mp32_link) and the end of the step (mp32_finish) are
+// shared with mp_slab.cuh and explicitly rounded, so both kernels give identical P.
 template <bool INIT>
 __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
 {
@@ -68,6 +74,7 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
         float frac = 1.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
         float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
         float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+        double dnet = 0.0;
         static_for<1, Q>([&](auto L) {
             constexpr int l = decltype(L)::value;
             constexpr Vel c = vel(l);
@@ -75,13 +82,14 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
             const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
             const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
             const float4 vn = __ldg(V + rp);
-            const float sp = on * (a.a1[w] * cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
-            const float spp = on * (a.a1[w] * cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
-            frac -= sp;
-            ux += c.x * sp;
-            uy += c.y * sp;
-            uz += c.z * sp;
+            const float spp = mp32_scatter(on, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), a.lwh[w]);
             if constexpr (INIT) {
+                const float sp = mp32_scatter(on, a.a1[w], cdot<c.x, c.y, c.z>(vr), a.lwh[w]);
+                frac -= sp;
+                ux += c.x * sp;
+                uy += c.y * sp;
+                uz += c.z * sp;
+                dnet += (double)spp - (double)sp;
                 v0 += c.x * c.x * sp;
                 v1 += c.y * c.y * sp;
                 v2 += c.z * c.z * sp;
@@ -89,26 +97,23 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                 n1 -= c.y * spp;
                 n2 -= c.z * spp;
             } else {
-                const float4 pn = __ldg(Pn + rp);
-                n0 += pn.x * spp - p.x * sp;
-                n1 += pn.y * spp - p.y * sp;
-                n2 += pn.z * spp - p.z * sp;
+                mp32_link(spp, __ldg(Pn + rp), p, n0, n1, n2);
             }
         });
         if constexpr (INIT) {
             a.P[0][r] = make_float4(n0 * bw, n1 * bw, n2 * bw, 0.0f);
+            a.aux[r] = make_float4(ux, uy, uz, (float)dnet);
             vt[0] += v0;
             vt[1] += v1;
             vt[2] += v2;
             const float fr = (a.ads && (m & INTERFACIAL_BIT)) ? frac - a.ka : frac;
             if (fr < 1.1920929e-07f) bad = LBGPU_ERR_FRACTION;
         } else {
-            vt[0] += p.x * ux;
-            vt[1] += p.y * uy;
-            vt[2] += p.z * uz;
-            n0 += p.x;
-            n1 += p.y;
-            n2 += p.z;
+            const float4 ax = __ldg(a.aux + r);
+            vt[0] += p.x * ax.x;
+            vt[1] += p.y * ax.y;
+            vt[2] += p.z * ax.z;
+            mp32_finish(p, ax.w, n0, n1, n2);
             if (a.ads && (m & INTERFACIAL_BIT)) {
                 const float4 q = a.A[par][r];
                 n0 += q.x * a.kd - a.ka * p.x;
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
 
 // One tracer step of a box with V and P staged in shared memory (mp_slab.cuh): a block owns a
 // 32 x 8 column tile and a chunk of zc planes.
-__global__ void __launch_bounds__(MP_BLOCK) k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc)
+__global__ void __launch_bounds__(MP_BLOCK, 5) k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc)
 {
     const volatile MpCtl *vc = a.ctl;
     if (vc->done) return;
@@ -146,7 +151,7 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32_slab(const MpArgs32 a, int ti
     const int tile = (int)blockIdx.x % nxy, chunk = (int)blockIdx.x / nxy;
     const int z0 = chunk * zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    mp_slab_sweep(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
+    mp_slab_sweep<true>(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
                   sm4, vt);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     grid_sum3(v, a.partial, &a.ctl->blocks_done,

@@ -1,13 +1,15 @@
 // mp_slab.cuh -- FP32 tracer step of a column tile with V and P staged in shared memory.
 //
-// The flux form of mp_f32.cu:k_mp32 (same operations in the same order, so P is bit-identical),
-// for the nodes (x0..x0+31, y0..y0+7, z0..z1-1) of a box with lx >= 32, ly >= 8, lz >= 3.  A ring
+// The step of mp_f32.cu:k_mp32 (same operations in the same order, so P is bit-identical), for
+// the nodes (x0..x0+31, y0..y0+7, z0..z1-1) of a box with lx >= 32, ly >= 8, lz >= 3.  A ring
 // of 4 planes (z-1, z, z+1 and the one being fetched) of V and P with a one-node halo is filled
-// by asynchronous copies one plane ahead, so the 36 neighbour reads per node are shared-memory
-// reads and every V and P value is fetched from L2/HBM about 1.3 times (halo) per step.  One
-// block barrier per plane: after it, plane z+1 is in shared memory and every thread is done with
-// plane z-1, so the fetch of plane z+2 may overwrite the slot of plane z-2.  The argument struct
-// provides V, P[2], A[2], mask, lx, ly, lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3].
+// by asynchronous copies one plane ahead, so the neighbour reads are shared-memory reads and
+// every V and P value is fetched from L2/HBM about 1.3 times (halo) per step; the column's flag
+// word (and the node's fixed (u*, D)) is loaded into registers a plane ahead.  One block barrier
+// per plane: after it, plane z+1 is in shared memory and every thread is done with plane z-1, so
+// the fetch of plane z+2 may overwrite the slot of plane z-2.  The argument struct provides V,
+// P[2], A[2], mask, lx, ly, lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3] (and aux for the
+// difference form).
 #pragma once
 
 #include "common.cuh"
@@ -18,6 +20,30 @@ namespace lbg {
 
 constexpr int SHX = MPS_TX + 2, SHY = MPS_TY + 2, SPL = SHX * SHY;  // a plane with its halo
 constexpr size_t MPS_SMEM = sizeof(float4) * 8 * SPL;                // 4 planes of V and of P
+
+// Scattering probability of a link, on * (a1 (c.V) + lambda w / 2) (on = 0 across a
+// bounce-back link), rounded as written.
+__device__ __forceinline__ float mp32_scatter(float on, float a1, float cv, float lwh)
+{
+    return __fmul_rn(on, __fmaf_rn(a1, cv, lwh));
+}
+
+// One incoming link of an FP32 step: n += sp_in (P(r + c_l) - P(r)).
+__device__ __forceinline__ void mp32_link(float spp, const float4 &pn, const float4 &p, float &n0,
+                                          float &n1, float &n2)
+{
+    n0 = __fmaf_rn(spp, __fsub_rn(pn.x, p.x), n0);
+    n1 = __fmaf_rn(spp, __fsub_rn(pn.y, p.y), n1);
+    n2 = __fmaf_rn(spp, __fsub_rn(pn.z, p.z), n2);
+}
+
+// End of an FP32 step: n = P(r) + (n + D P(r)), D = sum sp_in - sum sp_out of the node.
+__device__ __forceinline__ void mp32_finish(const float4 &p, float D, float &n0, float &n1, float &n2)
+{
+    n0 = __fadd_rn(p.x, __fmaf_rn(D, p.x, n0));
+    n1 = __fadd_rn(p.y, __fmaf_rn(D, p.y, n1));
+    n2 = __fadd_rn(p.z, __fmaf_rn(D, p.z, n2));
+}
 
 template <int CX, int CY, int CZ>
 __device__ __forceinline__ float slab_cdot(const float4 &v)
@@ -34,8 +60,10 @@ __device__ __forceinline__ float slab_cdot(const float4 &v)
 
 // Sweep of one tile: P(par) -> P(par^1) (and A) for its fluid nodes; vt += the nodes' VACF
 // terms (FP32, per thread).  sm: MPS_SMEM bytes of shared memory.  Every thread of the block
-// (MP_BLOCK = 256 = 32 x 8) must call it.
-template <typename Args>
+// (MP_BLOCK = 256 = 32 x 8) must call it.  AUX: the difference form of mp_f32.cu:k_mp32 with the
+// node's fixed (u*, D) from a.aux (18 scatterings per node and step); otherwise the flux form
+// P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings).
+template <bool AUX, typename Args>
 __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, int y0, int z0, int z1,
                                               float4 *sm, float (&vt)[3])
 {
@@ -63,12 +91,24 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
     load_plane(z0 - 1);
     load_plane(z0);
     load_plane(z0 + 1);
+    // the column's flag word (and, AUX, fixed node data) of the next plane, loaded a plane ahead
+    // so that no plane starts on a global-memory round trip
+    const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
+    uint32_t m_next = col ? __ldg(a.mask + col0 + plane * z0) : 0u;
+    float4 ax_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (AUX)
+        if (col) ax_next = __ldg(a.aux + col0 + plane * z0);
     for (int z = z0; z < z1; ++z) {
         cp_async_wait0();
         __syncthreads();
         if (z + 2 <= z1) load_plane(z + 2);
-        const size_t r = (size_t)x + (size_t)lx * ((size_t)y + (size_t)ly * z);
-        const uint32_t m = col ? __ldg(a.mask + r) : 0u;
+        const size_t r = col0 + plane * z;
+        const uint32_t m = m_next;
+        const float4 ax = ax_next;
+        if (col && z + 1 < z1) {
+            m_next = __ldg(a.mask + r + plane);
+            if constexpr (AUX) ax_next = __ldg(a.aux + r + plane);
+        }
         if (m & FLUID_BIT) {
             const int c0 = (ty + 1) * SHX + (tx + 1);
             const int s0 = (z - z0 + 1) & 3;
@@ -83,22 +123,34 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
                 const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
                 const int q = ((z + c.z - z0 + 1) & 3) * SPL + c0 + c.y * SHX + c.x;
                 const float4 vn = sV[q];
-                const float sp = on * (a.a1[w] * slab_cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
-                const float spp = on * (a.a1[w] * slab_cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
-                ux += c.x * sp;
-                uy += c.y * sp;
-                uz += c.z * sp;
                 const float4 pn = sP[q];
-                n0 += pn.x * spp - p.x * sp;
-                n1 += pn.y * spp - p.y * sp;
-                n2 += pn.z * spp - p.z * sp;
+                if constexpr (AUX) {
+                    mp32_link(mp32_scatter(on, a.a1[w], slab_cdot<-c.x, -c.y, -c.z>(vn), a.lwh[w]), pn, p,
+                              n0, n1, n2);
+                } else {
+                    const float sp = on * (a.a1[w] * slab_cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
+                    const float spp = on * (a.a1[w] * slab_cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
+                    ux += c.x * sp;
+                    uy += c.y * sp;
+                    uz += c.z * sp;
+                    n0 += pn.x * spp - p.x * sp;
+                    n1 += pn.y * spp - p.y * sp;
+                    n2 += pn.z * spp - p.z * sp;
+                }
             });
-            vt[0] += p.x * ux;
-            vt[1] += p.y * uy;
-            vt[2] += p.z * uz;
-            n0 += p.x;
-            n1 += p.y;
-            n2 += p.z;
+            if constexpr (AUX) {
+                vt[0] += p.x * ax.x;
+                vt[1] += p.y * ax.y;
+                vt[2] += p.z * ax.z;
+                mp32_finish(p, ax.w, n0, n1, n2);
+            } else {
+                vt[0] += p.x * ux;
+                vt[1] += p.y * uy;
+                vt[2] += p.z * uz;
+                n0 += p.x;
+                n1 += p.y;
+                n2 += p.z;
+            }
             if (a.ads && (m & INTERFACIAL_BIT)) {
                 const float4 qa = a.A[par][r];
                 n0 += qa.x * a.kd - a.ka * p.x;
