@@ -1,7 +1,7 @@
 #!/usr/bin/env python
-"""Benchmark of the D3Q19 flow step on the 192^3 porous medium (BASELINE configuration
-"single large 3D porous medium": spheres of radius 8 at seeded uniform centres, overlap allowed,
-porosity 0.60, tau 0.8, f_ext (1e-6,0,0)).
+"""Benchmark of the D3Q19 flow step on a single large 3D porous medium: a 192^3 periodic box of
+solid spheres of radius 8 at seeded uniform centres, overlap allowed, porosity 0.60, tau 0.8,
+f_ext (1e-6,0,0).
 
 One "step" is one fused pull-stream + bounce-back + moments + BGK/Guo collision over the whole
 box.  The headline is the FP32-deviation kernel (MLUPS = fluid-node updates per microsecond);
@@ -514,7 +514,7 @@ def main():
     box.sync()
     ms32 = max_over_ranks(dist, ms32)
     barrier(dist)
-    # tracer moment propagation on the FP32 flow field (BASELINE: Db 0.01, beta dF = -2)
+    # tracer moment propagation on the FP32 flow field (Db 0.01, beta dF = -2)
     KMP = a.mp_steps or min(K, 400)
     box.mp_init(f_ext=FEXT, Db=0.01, ka=0.01 * math.exp(2.0), kd=0.01)
     box.time_mp_steps(W)
