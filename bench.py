@@ -256,8 +256,9 @@ def bench_charged(a):
     interfacial solid node, bjl 0.4, lambda_D 4, D+- 0.05): the Poisson-Nernst-Planck loop with
     the reference's Jacobi solver (bit-identical to the oracle) and with the 4-colour SOR
     (omega 1.8, tol 1e-10), the SOR error on potential and ion densities against the reference
-    solver, then FP32 vs FP64 flow (f_ext 1e-6) and tracer VACF in the charged geometry (the
-    tracer is neutral: the reference stops on a charged one, module_moment_propagation.f90:71-79)."""
+    solver, then FP32 vs FP64 flow (f_ext 1e-6) and tracer VACF in the charged geometry for a
+    neutral tracer and for a charged one (z = +1) in the potential, which the reference stops on
+    (module_moment_propagation.f90:71-79) and this library computes with its formulas."""
     from laboetie_gb300 import FP32_DEV, FP64, Box
     from laboetie_gb300 import geometry as geo
     from laboetie_gb300.lbgpu import POISSON_REFERENCE, POISSON_SOR4
@@ -277,8 +278,8 @@ def bench_charged(a):
                 t = time.perf_counter()
                 outer, sweeps, rc = box.poisson_nernst_planck(max_outer=a.pnp_max_outer, check=False)
                 dt = time.perf_counter() - t
-                cp, cm, phi, _ = box.pnp_get()
-            sol[sname] = (cp, cm, phi)
+                cp, cm, phi, an = box.pnp_get()
+            sol[sname] = (cp, cm, phi, an)
             res[sname] = {"outer": outer, "sweeps": sweeps, "seconds": round(dt, 4), "status": rc,
                           "sweeps_per_s": round(sweeps / dt, 1) if dt > 0 else None}
             if solver == POISSON_SOR4 and any(d % 2 for d in nat.shape):
@@ -287,22 +288,32 @@ def bench_charged(a):
         r, q = sol["reference_jacobi"], sol["sor4"]
         res["sor4_vs_reference"] = {"phi": rel(q[2], r[2]), "c_plus": rel(q[0], r[0]),
                                     "c_minus": rel(q[1], r[1])}
-        v = {}
-        for pname, prec in (("fp64", FP64), ("fp32", FP32_DEV)):
-            with Box(nat, relaxation_time=1.0, f_ext=(1e-6, 0.0, 0.0), precision=prec) as box:
-                box.flow_init()
-                box.flow_steps(a.charged_flow_steps, force_on=True)
-                v0 = box.mp_init(f_ext=(1e-6, 0.0, 0.0), Db=0.01, ka=0.01 * math.e, kd=0.01)
-                vac, _ = box.mp_propagate(a.charged_mp_steps)
-            v[pname] = (v0, vac)
-        scale = float(np.abs(v["fp64"][0]).max())
-        n = min(len(v["fp64"][1]), len(v["fp32"][1]))
-        res["vacf_fp32_vs_fp64"] = {
-            "max_abs_over_vacf0": float(np.max(np.abs(v["fp32"][1][:n] - v["fp64"][1][:n]))) / scale,
-            "d_eff_rel": float(abs((v["fp32"][0][0] / 2 + v["fp32"][1][:n, 0].sum()) -
-                                   (v["fp64"][0][0] / 2 + v["fp64"][1][:n, 0].sum())) /
-                               abs(v["fp64"][0][0] / 2 + v["fp64"][1][:n, 0].sum())),
-            "steps": n}
+        # tracers in the flow (f_ext 1e-6) of the charged geometry: a neutral one, and a charged
+        # one (z = +1) in the reference solver's potential (lbgpu_mp_init_charged; the reference
+        # itself stops on a charged tracer, module_moment_propagation.f90:71-79)
+        for tkey, z in (("vacf_fp32_vs_fp64", 0.0), ("charged_tracer", 1.0)):
+            v = {}
+            for pname, prec in (("fp64", FP64), ("fp32", FP32_DEV)):
+                with Box(nat, relaxation_time=1.0, f_ext=(1e-6, 0.0, 0.0), precision=prec) as box:
+                    box.flow_init()
+                    box.flow_steps(a.charged_flow_steps, force_on=True)
+                    if z:
+                        box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05)
+                        box.pnp_set(*sol["reference_jacobi"])
+                    v0 = box.mp_init(f_ext=(1e-6, 0.0, 0.0), Db=0.01, ka=0.01 * math.e, kd=0.01,
+                                     z=z, charged=bool(z))
+                    vac, _ = box.mp_propagate(a.charged_mp_steps)
+                v[pname] = (v0, vac)
+            scale = float(np.abs(v["fp64"][0]).max())
+            n = min(len(v["fp64"][1]), len(v["fp32"][1]))
+            deff = {p_: float(v[p_][0][0] / 2 + v[p_][1][:n, 0].sum()) for p_ in ("fp64", "fp32")}
+            res[tkey] = {
+                "max_abs_over_vacf0": float(np.max(np.abs(v["fp32"][1][:n] - v["fp64"][1][:n]))) / scale,
+                "d_eff_rel": abs(deff["fp32"] - deff["fp64"]) / abs(deff["fp64"]),
+                "steps": n}
+            if z:
+                res[tkey].update({"z": z, "d_eff_x_fp64": deff["fp64"], "d_eff_x_fp32": deff["fp32"],
+                                  "tracer": "Db 0.01, K = e (kd 0.01), in the reference solver's potential"})
         out.append(res)
     # Poisson sweep roofline on a large charged box: 4 x 8 B per node and sweep (phi read and
     # written, c+ and c- read).  Tolerance 0, so every solve runs exactly its sweep cap; an odd box
@@ -334,7 +345,8 @@ def bench_charged(a):
     return {"cases": out, "config": {"bjl": 0.4, "lambda_D": 4.0, "D_plus": 0.05, "D_minus": 0.05,
                                      "surface_charge_per_interfacial_solid_node": -0.01,
                                      "max_outer": a.pnp_max_outer, "flow_steps": a.charged_flow_steps,
-                                     "mp_steps": a.charged_mp_steps, "tracer": "neutral, Db 0.01, K = e"}}
+                                     "mp_steps": a.charged_mp_steps,
+                                     "tracer": "neutral and charged (z = +1), Db 0.01, K = e"}}
 
 
 def bench_batched(a):

@@ -221,7 +221,7 @@ typedef struct {
     double Db;             /* tracer_Db, bulk diffusion coefficient (> epsilon) */
     double ka, kd;         /* tracer_ka, tracer_kd adsorption / desorption rates (>= 0) */
     double Ds;             /* tracer_Ds, must be 0 as in the reference */
-    double z;              /* tracer_z; charged tracers are refused as in the reference */
+    double z;              /* tracer_z; lbgpu_mp_init refuses z != 0 as the reference does */
     double f_ext[3];       /* lb.in f_ext, added to the flux of the tracer populations */
     double elec_slope[3];  /* system elec_slope (0 unless the PNP stage read it) */
 } lbgpu_tracer;
@@ -235,6 +235,18 @@ typedef struct {
  * lbgpu_mp_propagate (module_moment_propagation.f90:249,257), as the reference stops there. */
 int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tracer, const double *density,
                   const double *jx, const double *jy, const double *jz, double vacf0[3]);
+
+/* lbgpu_mp_init for a charged tracer (tracer->z != 0), which the reference refuses
+ * (module_moment_propagation.f90:71-79) although it holds the formulas; no counterpart call.
+ * The potential is the context's Poisson-Nernst-Planck phi (after lbgpu_pnp_init and
+ * lbgpu_poisson_nernst_planck, or lbgpu_pnp_set; LBGPU_ERR_INVALID without one), with
+ * tracer->elec_slope.  Pstat = SUM(exp(-z phi)) over fluid nodes + SUM(exp(-z phi) K) over
+ * interfacial fluid nodes, in Fortran SUM order (:97-101); each node's Boltzmann weight
+ * exp(-z phi)/Pstat (:110); each link's fermi = 1/(1 + exp(z dphi)), dphi = phi(r') - phi(r)
+ * plus the elec_slope term of a link across the periodic boundary (:295-322); P(t=1) with the
+ * factor exp(-z dphi) (:123-135).  The steps are lbgpu_mp_propagate's.  z = 0 is lbgpu_mp_init. */
+int lbgpu_mp_init_charged(lbgpu_ctx *ctx, const lbgpu_tracer *tracer, const double *density,
+                          const double *jx, const double *jy, const double *jz, double vacf0[3]);
 
 /* moment_propagation::propagate (module_moment_propagation.f90:164-289) for steps it = k+1 ...
  * k+nsteps, stopping early once converged (it > 2 and |VACF| < min(Db/(2 lx ly lz), 1e-12)).

@@ -100,6 +100,8 @@ void fill_args64(lbgpu_ctx *ctx, FlowArgs64 &a);
 int force_mask(const double f[3]);
 void mp_release(lbgpu_ctx *ctx);
 void pnp_release(lbgpu_ctx *ctx);
+// device potential phi of the Poisson-Nernst-Planck state (N doubles), or null without one
+const double *pnp_potential(const lbgpu_ctx *ctx);
 
 #define LBG_CK(ctx, call)                                                   \
     do {                                                                    \

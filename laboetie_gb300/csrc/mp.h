@@ -46,6 +46,11 @@ struct MpArgs64 {
     double lambda, ka, kd, one_minus_kd, bw;
     double a0[3], a1[3], lwh[3];       // lwh = (lambda*a0)*0.5 (fermi = 1/2 for a neutral tracer)
     double fext[3], q, D, E[3];        // drop_tracers.f90:88-100
+    // charged tracer (lbgpu_mp_init_charged): lambda*a0, the potential, tracer_z and
+    // 1/Pstat's denominator Pstat = SUM(exp(-z phi)) over fluid (+ K over interfacial fluid)
+    double lw[3];
+    const double *phi;
+    double z, pstat;
 };
 
 struct MpArgs32 {
@@ -66,6 +71,10 @@ struct MpArgs32 {
     float ka, kd, one_minus_kd;
     float a1[3], lwh[3];
     int slab;                          // shared-memory slab step where the box allows it
+    // charged tracer: V.w holds the potential phi at every node; lambda*a0, tracer_z, 1/Pstat
+    // and elec_slope for the per-link fermi factors (the grid-stride step is used)
+    int charged;
+    float lw[3], z, inv_pstat, E[3];
 };
 
 // Shared-memory slab variant of the FP32 step (mp_f32.cu): 32 x 8 column tiles sweeping a chunk

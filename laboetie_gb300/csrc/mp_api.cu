@@ -67,10 +67,34 @@ using namespace lbg;
 
 extern "C" {
 
+namespace lbg {
+namespace {
+int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, const double *jx,
+                 const double *jy, const double *jz, double vacf0[3], bool allow_charged);
+}
+}  // namespace lbg
+
 int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, const double *jx,
                   const double *jy, const double *jz, double vacf0[3])
 {
     TraceRange trace_("lbgpu_mp_init");
+    return mp_init_impl(ctx, tr, density, jx, jy, jz, vacf0, false);
+}
+
+int lbgpu_mp_init_charged(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
+                          const double *jx, const double *jy, const double *jz, double vacf0[3])
+{
+    TraceRange trace_("lbgpu_mp_init_charged");
+    return mp_init_impl(ctx, tr, density, jx, jy, jz, vacf0, true);
+}
+
+}  // extern "C"
+
+namespace lbg {
+namespace {
+int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, const double *jx,
+                 const double *jy, const double *jz, double vacf0[3], bool allow_charged)
+{
     if (!ctx || !tr) return LBGPU_ERR_INVALID;
     if ((density == nullptr) != (jx == nullptr) || (jx == nullptr) != (jy == nullptr) ||
         (jy == nullptr) != (jz == nullptr))
@@ -84,21 +108,43 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
     if (std::fabs(tr->Ds) > EPS)
         return ctx_fail(ctx, LBGPU_ERR_UNSUPPORTED,
                         "Tracers you defined have non-zero surface diffusion coefficient");
-    if (std::fabs(tr->z) > EPS)
+    const bool charged = std::fabs(tr->z) > EPS;
+    if (charged && !allow_charged)
         return ctx_fail(ctx, LBGPU_ERR_UNSUPPORTED, "charged tracers are not implemented");
+    const double *d_phi = charged ? pnp_potential(ctx) : nullptr;
+    if (charged && !d_phi)
+        return ctx_fail(ctx, LBGPU_ERR_INVALID,
+                        "lbgpu_mp_init_charged: no potential (run lbgpu_pnp_init and the "
+                        "Poisson-Nernst-Planck loop, or lbgpu_pnp_set, first)");
+    const long long N = ctx->N;
+    cudaStream_t st = ctx->stream;
+    double K = std::fabs(tr->kd) <= EPS ? 0.0 : tr->ka / tr->kd;
+    double Pstat = (double)ctx->counts[0] + K * (double)ctx->counts[2];  // :97
+    if (charged) {
+        // module_moment_propagation.f90:99-100 in the Fortran SUM order (storage order), on the
+        // host: SUM(exp(-z phi)) over fluid nodes + SUM(exp(-z phi) K) over interfacial fluid
+        std::vector<double> phi((size_t)N);
+        std::vector<uint32_t> msk((size_t)N);
+        LBG_CK(ctx, cudaMemcpyAsync(phi.data(), d_phi, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+        LBG_CK(ctx, cudaMemcpyAsync(msk.data(), ctx->d_mask, sizeof(uint32_t) * N, cudaMemcpyDeviceToHost, st));
+        LBG_CK(ctx, cudaStreamSynchronize(st));
+        double s1 = 0.0, s2 = 0.0;
+        for (long long r = 0; r < N; ++r)
+            if (msk[r] & FLUID_BIT) s1 = s1 + std::exp(-(tr->z * phi[r]));
+        for (long long r = 0; r < N; ++r)
+            if ((msk[r] & FLUID_BIT) && (msk[r] & INTERFACIAL_BIT)) s2 = s2 + std::exp(-(tr->z * phi[r])) * K;
+        Pstat = s1 + s2;
+    }
     mp_release(ctx);
     MpState *s = new MpState();
     ctx->mp = s;
     s->prec = ctx->p.precision;
     s->tr = *tr;
-    s->K = std::fabs(tr->kd) <= EPS ? 0.0 : tr->ka / tr->kd;
+    s->K = K;
     s->ads = std::fabs(s->K) > EPS;
     const volatile double kBT = 1.0 / 3.0;
     s->lambda = 4.0 * tr->Db / kBT;                         // module_moment_propagation.f90:331-337
-    const double Pstat = (double)ctx->counts[0] + s->K * (double)ctx->counts[2];  // :97
     s->bw = 1.0 / Pstat;
-    const long long N = ctx->N;
-    cudaStream_t st = ctx->stream;
     int rc;
 
     // moments the tracer populations are built from (node%solventDensity / solventFlux)
@@ -138,6 +184,7 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
         a.a0[w] = ctx->K64.a0[w];
         a.a1[w] = ctx->K64.a1[w];
         const volatile double lw = s->lambda * ctx->K64.a0[w];
+        a.lw[w] = lw;
         a.lwh[w] = lw * 0.5;
     }
     for (int d = 0; d < 3; ++d) {
@@ -146,6 +193,9 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
     }
     a.q = tr->z;
     a.D = tr->Db;
+    a.phi = d_phi;      // charged: exp(-z phi)/Pstat per node, fermi factors per link
+    a.z = tr->z;
+    a.pstat = Pstat;
     s->nblocks = (unsigned)((N + MP_BLOCK - 1) / MP_BLOCK);
     int zc = 0;
     const unsigned slab = s->prec == LBGPU_FP64 ? 0u : mp32_slab_grid(a.lx, a.ly, a.lz, &zc);
@@ -191,7 +241,12 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
         for (int w = 0; w < 3; ++w) {
             b.a1[w] = (float)a.a1[w];
             b.lwh[w] = (float)a.lwh[w];
+            b.lw[w] = (float)a.lw[w];
         }
+        b.charged = charged ? 1 : 0;
+        b.z = (float)tr->z;
+        b.inv_pstat = (float)(1.0 / Pstat);
+        for (int d = 0; d < 3; ++d) b.E[d] = (float)tr->elec_slope[d];
         LBG_CK(ctx, launch_mp_v32(a, V, st));
         LBG_CK(ctx, launch_mp_init_f32(b, (float)s->bw, s->nblocks, st));
     }
@@ -209,6 +264,10 @@ int lbgpu_mp_init(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density,
     s->it_next = 1;
     return LBGPU_OK;
 }
+}  // namespace
+}  // namespace lbg
+
+extern "C" {
 
 static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done, int *is_converged,
                   bool timing, float *ms)

@@ -45,7 +45,25 @@ __device__ __forceinline__ float cdot(const float4 &v)
 // for the run, so a step evaluates the 18 incoming ones and no outgoing one.
 // The per-link operations (mp32_scatter, mp32_link) and the end of the step (mp32_finish) are
 // shared with mp_slab.cuh and explicitly rounded, so both kernels give identical P.
-template <bool INIT>
+// module_moment_propagation.f90:303-322 in FP32: phi(r') - phi(r) with the elec_slope correction
+// of a link across the periodic boundary (only the first matching case of the chain).
+__device__ __forceinline__ float dphi32(const MpArgs32 &a, float phi_r, float phi_p, int x, int y, int z,
+                                       int xp, int yp, int zp)
+{
+    float d = phi_p - phi_r;
+    if (x == a.lx - 1 && xp == 0) d += a.E[0] * (float)(a.lx + 1);
+    else if (x == 0 && xp == a.lx - 1) d -= a.E[0] * (float)(a.lx + 1);
+    else if (y == a.ly - 1 && yp == 0) d += a.E[1] * (float)(a.ly + 1);
+    else if (y == 0 && yp == a.ly - 1) d -= a.E[1] * (float)(a.ly + 1);
+    else if (z == a.lz - 1 && zp == 0) d += a.E[2] * (float)(a.lz + 1);
+    else if (z == 0 && zp == a.lz - 1) d -= a.E[2] * (float)(a.lz + 1);
+    return d;
+}
+
+// CHARGED: the scatterings carry the link's fermi factor 1/(1 + exp(z dphi)) (out of the node)
+// and 1 - fermi (into it), P(t=1) the factor exp(-z dphi) and each node its Boltzmann weight
+// exp(-z phi)/Pstat (module_moment_propagation.f90:97-135, 223-229, 295-327); bw is then unused.
+template <bool INIT, bool CHARGED>
 __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
 {
     const volatile MpCtl *vc = a.ctl;
@@ -82,9 +100,18 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
             const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
             const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
             const float4 vn = __ldg(V + rp);
-            const float spp = mp32_scatter(on, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), a.lwh[w]);
+            float lw_out = a.lwh[w], lw_in = a.lwh[w], emd = 1.0f;
+            if constexpr (CHARGED) {
+                const float e = expf(a.z * dphi32(a, vr.w, vn.w, x, y, z, X[c.x + 1], Y[c.y + 1] / sy,
+                                                  Z[c.z + 1] / sz));
+                const float fermi = 1.0f / (1.0f + e);
+                lw_out = a.lw[w] * fermi;
+                lw_in = a.lw[w] * (1.0f - fermi);
+                emd = on != 0.0f ? 1.0f / e : 0.0f;
+            }
+            const float spp = mp32_scatter(on, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), lw_in);
             if constexpr (INIT) {
-                const float sp = mp32_scatter(on, a.a1[w], cdot<c.x, c.y, c.z>(vr), a.lwh[w]);
+                const float sp = mp32_scatter(on, a.a1[w], cdot<c.x, c.y, c.z>(vr), lw_out);
                 frac -= sp;
                 ux += c.x * sp;
                 uy += c.y * sp;
@@ -93,19 +120,21 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                 v0 += c.x * c.x * sp;
                 v1 += c.y * c.y * sp;
                 v2 += c.z * c.z * sp;
-                n0 -= c.x * spp;
-                n1 -= c.y * spp;
-                n2 -= c.z * spp;
+                const float t = CHARGED ? emd * spp : spp;
+                n0 -= c.x * t;
+                n1 -= c.y * t;
+                n2 -= c.z * t;
             } else {
                 mp32_link(spp, __ldg(Pn + rp), p, n0, n1, n2);
             }
         });
         if constexpr (INIT) {
-            a.P[0][r] = make_float4(n0 * bw, n1 * bw, n2 * bw, 0.0f);
+            const float bwr = CHARGED ? expf(-(a.z * vr.w)) * a.inv_pstat : bw;
+            a.P[0][r] = make_float4(n0 * bwr, n1 * bwr, n2 * bwr, 0.0f);
             a.aux[r] = make_float4(ux, uy, uz, (float)dnet);
-            vt[0] += v0;
-            vt[1] += v1;
-            vt[2] += v2;
+            vt[0] += CHARGED ? v0 * bwr : v0;
+            vt[1] += CHARGED ? v1 * bwr : v1;
+            vt[2] += CHARGED ? v2 * bwr : v2;
             const float fr = (a.ads && (m & INTERFACIAL_BIT)) ? frac - a.ka : frac;
             if (fr < 1.1920929e-07f) bad = LBGPU_ERR_FRACTION;
         } else {
@@ -128,7 +157,8 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
     }
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     if constexpr (INIT) {
-        for (int d = 0; d < 3; ++d) v[d] *= (double)bw;
+        if (!CHARGED)
+            for (int d = 0; d < 3; ++d) v[d] *= (double)bw;
         block_sum3_fixed(v);
         if (threadIdx.x == 0)
             for (int d = 0; d < 3; ++d) a.partial[3 * blockIdx.x + d] = v[d];
@@ -163,15 +193,16 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_v(const MpArgs64 a, float4 *V)
 {
     const long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x;
     if (r >= a.N) return;
+    const float phi = a.phi ? (float)a.phi[r] : 0.0f;   // charged tracer: the potential
     if (!(a.mask[r] & FLUID_BIT)) {
-        V[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        V[r] = make_float4(0.f, 0.f, 0.f, phi);
         return;
     }
     const double rho = a.rho[r];
     const double J[3] = {a.jx[r], a.jy[r], a.jz[r]};
     float o[3];
     for (int d = 0; d < 3; ++d) o[d] = (float)((J[d] + a.fext[d] - rho * a.q * a.D * a.E[d]) / rho);
-    V[r] = make_float4(o[0], o[1], o[2], 0.0f);
+    V[r] = make_float4(o[0], o[1], o[2], phi);
 }
 
 }  // namespace
@@ -185,19 +216,21 @@ cudaError_t launch_mp_v32(const MpArgs64 &a64, float4 *V, cudaStream_t s)
 cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, cudaStream_t s)
 {
     int zc = 0;
-    const unsigned sg = a.slab ? mp32_slab_grid(a.lx, a.ly, a.lz, &zc) : 0u;
+    const unsigned sg = a.slab && !a.charged ? mp32_slab_grid(a.lx, a.ly, a.lz, &zc) : 0u;
     if (sg) {
         const int tx = (a.lx + MPS_TX - 1) / MPS_TX, ty = (a.ly + MPS_TY - 1) / MPS_TY;
         k_mp32_slab<<<sg, MP_BLOCK, MPS_SMEM, s>>>(a, tx, ty, zc);
     } else {
-        k_mp32<false><<<grid, MP_BLOCK, 0, s>>>(a, 0.0f);
+        if (a.charged) k_mp32<false, true><<<grid, MP_BLOCK, 0, s>>>(a, 0.0f);
+        else k_mp32<false, false><<<grid, MP_BLOCK, 0, s>>>(a, 0.0f);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_mp_init_f32(const MpArgs32 &a, float bw, unsigned grid, cudaStream_t s)
 {
-    k_mp32<true><<<grid, MP_BLOCK, 0, s>>>(a, bw);
+    if (a.charged) k_mp32<true, true><<<grid, MP_BLOCK, 0, s>>>(a, bw);
+    else k_mp32<true, false><<<grid, MP_BLOCK, 0, s>>>(a, bw);
     return cudaGetLastError();
 }
 

@@ -1,7 +1,8 @@
 // mp_f64.cu -- FP64 strict tracer moment propagation (compiled with -fmad=false).
 //
-// The scattering probabilities of a neutral tracer (module_moment_propagation.f90:341-346,
-// fermi = 1/2) depend only on the converged flow, so they are computed once, in the reference's
+// The scattering probabilities (module_moment_propagation.f90:341-346; fermi = 1/2 for a neutral
+// tracer, per link from the potential for a charged one) depend only on the converged flow (and
+// the potential), so they are computed once, in the reference's
 // operation order, into a table coef[(l-1)*N + r] = scattprop of node r+c_l towards r.  A step
 // then gathers P_now from the fluid neighbours through that table, in l order, exactly as the
 // reference's sweep does (module_moment_propagation.f90:207-253): the propagated quantities are
@@ -61,8 +62,34 @@ __device__ __forceinline__ double scattprop(double n, double rho, const MpArgs64
     return n / rho - a.a0[wclass(L)] + a.lwh[wclass(L)];
 }
 
+// module_moment_propagation.f90:303-322: phi(r') - phi(r) of the link from (x, y, z) to
+// (xp, yp, zp) (0-based), with the elec_slope correction of a link across the periodic boundary;
+// only the first matching case of the reference's chain applies.
+__device__ __forceinline__ double dphi64(const MpArgs64 &a, long long r, long long rp, int x, int y,
+                                         int z, int xp, int yp, int zp)
+{
+    double d = a.phi[rp] - a.phi[r];
+    if (x == a.lx - 1 && xp == 0) d = d + a.E[0] * (double)(a.lx + 1);
+    else if (x == 0 && xp == a.lx - 1) d = d - a.E[0] * (double)(a.lx + 1);
+    else if (y == a.ly - 1 && yp == 0) d = d + a.E[1] * (double)(a.ly + 1);
+    else if (y == 0 && yp == a.ly - 1) d = d - a.E[1] * (double)(a.ly + 1);
+    else if (z == a.lz - 1 && zp == 0) d = d + a.E[2] * (double)(a.lz + 1);
+    else if (z == 0 && zp == a.lz - 1) d = d - a.E[2] * (double)(a.lz + 1);
+    return d;
+}
+
+// n/rho - w + (lambda*w)*fermi (module_moment_propagation.f90:345) for a link's fermi factor
+template <int L>
+__device__ __forceinline__ double scattprop_f(double n, double rho, double fermi, const MpArgs64 &a)
+{
+    return n / rho - a.a0[wclass(L)] + a.lw[wclass(L)] * fermi;
+}
+
 // module_moment_propagation.f90:30-160 (init) for every fluid node: scattering table, remaining
-// fraction, u*, P(t=1) and this block's share of VACF(0).
+// fraction, u*, P(t=1) and this block's share of VACF(0).  CHARGED: Boltzmann weight
+// exp(-z phi)/Pstat per node and fermi = 1/(1 + exp(z dphi)) per link (:97-135, 295-327); the
+// table then holds the charged scatterings and the step kernel is the same.
+template <bool CHARGED>
 __global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
 {
     __shared__ double sh[MP_BLOCK / 32];
@@ -78,6 +105,10 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
             const double rho = a.rho[r], Jx = a.jx[r], Jy = a.jy[r], Jz = a.jz[r];
             double frac = 1.0, ux = 0.0, uy = 0.0, uz = 0.0;
             double P[3] = {0.0, 0.0, 0.0};
+            // boltz_weight (module_moment_propagation.f90:105-111)
+            const double bw = CHARGED ? exp(-(a.z * a.phi[r])) / a.pstat : a.bw;
+            const int sx = a.lx, sxy = a.lx * a.ly;
+            const int x = (int)(r % sx), y = (int)((r / sx) % a.ly), z = (int)(r / sxy);
             static_for<1, Q>([&](auto L) {
                 constexpr int l = decltype(L)::value;
                 constexpr int li = inv(l);
@@ -87,24 +118,36 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
                     a.coef[(long long)(l - 1) * N + r] = 0.0;
                     return;
                 }
-                const double sp = scattprop<l>(n_tracer<l>(rho, Jx, Jy, Jz, a), rho, a);
+                const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
+                double sp, spp, emd = 1.0;
+                const double rhop = a.rho[rp];
+                if constexpr (CHARGED) {
+                    const int xp = (int)(X[c.x + 1]), yp = (int)(Y[c.y + 1] / sx), zp = (int)(Z[c.z + 1] / sxy);
+                    const double e = exp(a.z * dphi64(a, r, rp, x, y, z, xp, yp, zp));
+                    emd = 1.0 / e;
+                    const double fermi = 1.0 / (1.0 + e);
+                    sp = scattprop_f<l>(n_tracer<l>(rho, Jx, Jy, Jz, a), rho, fermi, a);
+                    spp = scattprop_f<li>(n_tracer<li>(rhop, a.jx[rp], a.jy[rp], a.jz[rp], a), rhop,
+                                          1.0 - fermi, a);
+                } else {
+                    sp = scattprop<l>(n_tracer<l>(rho, Jx, Jy, Jz, a), rho, a);
+                    spp = scattprop<li>(n_tracer<li>(rhop, a.jx[rp], a.jy[rp], a.jz[rp], a), rhop, a);
+                }
                 frac = frac - sp;
                 if constexpr (c.x != 0) ux = c.x > 0 ? ux + sp : ux - sp;
                 if constexpr (c.y != 0) uy = c.y > 0 ? uy + sp : uy - sp;
                 if constexpr (c.z != 0) uz = c.z > 0 ? uz + sp : uz - sp;
-                const double bs = a.bw * sp;
+                const double bs = bw * sp;
                 if constexpr (c.x != 0) v[0] = v[0] + bs;
                 if constexpr (c.y != 0) v[1] = v[1] + bs;
                 if constexpr (c.z != 0) v[2] = v[2] + bs;
-                const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
-                const double rhop = a.rho[rp];
-                const double spp =
-                    scattprop<li>(n_tracer<li>(rhop, a.jx[rp], a.jy[rp], a.jz[rp], a), rhop, a);
                 a.coef[(long long)(l - 1) * N + r] = spp;
-                // P(r,1) += exp_min_dphi * scattprop_p * c_inv * boltz_weight, exp_min_dphi = 1
-                if constexpr (ci.x != 0) P[0] = P[0] + (ci.x > 0 ? spp : -spp) * a.bw;
-                if constexpr (ci.y != 0) P[1] = P[1] + (ci.y > 0 ? spp : -spp) * a.bw;
-                if constexpr (ci.z != 0) P[2] = P[2] + (ci.z > 0 ? spp : -spp) * a.bw;
+                // P(r,1) += exp_min_dphi * scattprop_p * c_inv * boltz_weight
+                // (exp_min_dphi = 1 for a neutral tracer: the product is dropped, exactly)
+                const double t = CHARGED ? emd * spp : spp;
+                if constexpr (ci.x != 0) P[0] = P[0] + (ci.x > 0 ? t : -t) * bw;
+                if constexpr (ci.y != 0) P[1] = P[1] + (ci.y > 0 ? t : -t) * bw;
+                if constexpr (ci.z != 0) P[2] = P[2] + (ci.z > 0 ? t : -t) * bw;
             });
             a.frac[r] = frac;
             a.us[0][r] = ux;
@@ -195,7 +238,8 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_reduce(const double *partial, u
 
 cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
 {
-    k_mp_init<<<grid, MP_BLOCK, 0, s>>>(a);
+    if (a.phi) k_mp_init<true><<<grid, MP_BLOCK, 0, s>>>(a);
+    else k_mp_init<false><<<grid, MP_BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
 

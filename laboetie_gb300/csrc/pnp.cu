@@ -57,6 +57,11 @@ struct PnpState {
     cudaGraphExec_t sor_exec[2] = {nullptr, nullptr};
 };
 
+const double *pnp_potential(const lbgpu_ctx *ctx)
+{
+    return ctx->pnp ? ctx->pnp->phi[ctx->pnp->par] : nullptr;
+}
+
 void pnp_release(lbgpu_ctx *ctx)
 {
     if (!ctx->pnp) return;

@@ -106,6 +106,7 @@ def library():
     L.lbgpu_host_unregister.argtypes = [vp]
     for name, args in (
         ("lbgpu_mp_init", [vp, C.POINTER(Tracer), vp, vp, vp, vp, vp]),
+        ("lbgpu_mp_init_charged", [vp, C.POINTER(Tracer), vp, vp, vp, vp, vp]),
         ("lbgpu_mp_propagate", [vp, i, vp, pi, pi]),
         ("lbgpu_mp_get", [vp, vp, vp]),
         ("lbgpu_mp_release", [vp]),
@@ -309,17 +310,19 @@ def _tracer(Db=0.01, ka=0.0, kd=0.0, Ds=0.0, z=0.0, f_ext=(0.0, 0.0, 0.0),
     return t
 
 
-def _mp_init(self, moments=None, **tracer):
+def _mp_init(self, moments=None, charged=False, **tracer):
     """update_tracer_population + moment_propagation::init.  moments = (rho, (jx, jy, jz)) as
-    host arrays, or None for the box's own flow state.  Returns VACF(0)."""
+    host arrays, or None for the box's own flow state.  charged=True: lbgpu_mp_init_charged (a
+    tracer with z != 0 in the box's Poisson-Nernst-Planck potential).  Returns VACF(0)."""
     t = _tracer(**tracer)
     v0 = (C.c_double * 3)()
+    init = self.L.lbgpu_mp_init_charged if charged else self.L.lbgpu_mp_init
     if moments is None:
-        rc = self.L.lbgpu_mp_init(self.ctx, C.byref(t), None, None, None, None, v0)
+        rc = init(self.ctx, C.byref(t), None, None, None, None, v0)
     else:
         rho, j = moments
         arrs = [_f64(rho, self.shape)] + [_f64(x, self.shape) for x in j]
-        rc = self.L.lbgpu_mp_init(self.ctx, C.byref(t), *(_ptr(x) for x in arrs), v0)
+        rc = init(self.ctx, C.byref(t), *(_ptr(x) for x in arrs), v0)
     self._chk(rc, "mp_init")
     return np.array(list(v0))
 

@@ -56,6 +56,7 @@ class MPState(C.Structure):
         ("vacf", _d * 3),
         ("P_now", _pd), ("P_next", _pd), ("A_now", _pd), ("A_next", _pd),
         ("nthreads", _int),
+        ("phi", _pd), ("E", _d * 3),
     ]
 
 
@@ -96,6 +97,8 @@ def lib():
                                   _d, _d, _d, _d, _d, _pd]
         L.orc_mp_propagate.argtypes = [C.POINTER(MPState), _int, _i8, _u8, _dp, _dp, _pd, _pi]
         L.orc_mp_free.argtypes = [C.POINTER(MPState)]
+        L.orc_mp_init_charged.argtypes = [C.POINTER(MPState), _int, _int, _int, _i8, _u8, _dp, _dp,
+                                          _d, _d, _d, _d, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_charges_init.argtypes = [_int, _int, _int, _i8, _u8, _d, _d, _d, _int, _dp, _dp,
                                        _dp, _pd, _pd]
         L.orc_sor.argtypes = [_int, _int, _int, _d, _d, _dp, _dp, _dp, _pd, _pi]
@@ -215,15 +218,23 @@ class MomentPropagation:
     """module_moment_propagation.f90 init/propagate on the CPU."""
 
     def __init__(self, nature, interfacial, rho, n_mp, ka=0.0, kd=0.0, Db=0.01, Ds=0.0, z=0.0,
-                 nthreads=1):
+                 nthreads=1, phi=None, elec_slope=(0.0, 0.0, 0.0)):
+        """phi (same shape as nature) with z != 0: a charged tracer (orc_mp_init_charged)."""
         self.nature = np.ascontiguousarray(nature, dtype=np.int8)
         self.inter = np.ascontiguousarray(interfacial, dtype=np.uint8)
         self.rho = np.ascontiguousarray(rho, dtype=np.float64)
         self.nmp = np.ascontiguousarray(n_mp, dtype=np.float64)
         self.s = MPState()
         v0 = (C.c_double * 3)()
-        rc = lib().orc_mp_init(C.byref(self.s), *_dims(self.nature), self.nature, self.inter,
-                               self.rho, self.nmp, ka, kd, Db, Ds, z, v0)
+        if phi is None:
+            rc = lib().orc_mp_init(C.byref(self.s), *_dims(self.nature), self.nature, self.inter,
+                                   self.rho, self.nmp, ka, kd, Db, Ds, z, v0)
+        else:
+            self.phi = np.ascontiguousarray(phi, dtype=np.float64)
+            E = (C.c_double * 3)(*elec_slope)
+            rc = lib().orc_mp_init_charged(C.byref(self.s), *_dims(self.nature), self.nature,
+                                           self.inter, self.rho, self.nmp, ka, kd, Db, z,
+                                           self.phi, E, v0)
         _chk(rc, "mp_init")
         self.s.nthreads = nthreads
         self.vacf0 = np.array(list(v0))

@@ -436,9 +436,32 @@ static inline double scattprop(double n, double rho, double w, double lambda, do
 }
 
 /* module_moment_propagation.f90:30-160 */
-int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
-                const uint8_t *interfacial, const double *density, const double *n_mp,
-                double ka, double kd, double Db, double Ds, double z, double vacf0[3])
+/* module_moment_propagation.f90:303-322: phi(r') - phi(r), corrected by elec_slope for a link
+ * across the periodic boundary; only the first matching case of the chain applies (0-based). */
+static double orc_dphi(const orc_mp_state *s, int i, int j, int k, int ip, int jp, int kp)
+{
+    const int lx = s->lx, ly = s->ly, lz = s->lz;
+    double d = s->phi[nid(ip, jp, kp, lx, ly)] - s->phi[nid(i, j, k, lx, ly)];
+    if (i == lx - 1 && ip == 0) d = d + s->E[0] * (double)(lx + 1);
+    else if (i == 0 && ip == lx - 1) d = d - s->E[0] * (double)(lx + 1);
+    else if (j == ly - 1 && jp == 0) d = d + s->E[1] * (double)(ly + 1);
+    else if (j == 0 && jp == ly - 1) d = d - s->E[1] * (double)(ly + 1);
+    else if (k == lz - 1 && kp == 0) d = d + s->E[2] * (double)(lz + 1);
+    else if (k == 0 && kp == lz - 1) d = d - s->E[2] * (double)(lz + 1);
+    return d;
+}
+
+/* module_moment_propagation.f90:295-301 */
+static double orc_exp_dphi(const orc_mp_state *s, int i, int j, int k, int ip, int jp, int kp)
+{
+    if (!s->phi) return 1.0;
+    return exp(s->z * orc_dphi(s, i, j, k, ip, jp, kp));
+}
+
+static int mp_init_any(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
+                       const uint8_t *interfacial, const double *density, const double *n_mp,
+                       double ka, double kd, double Db, double Ds, double z, const double *phi,
+                       const double E[3], double vacf0[3])
 {
     init_tables();
     const double eps = 2.220446049250313e-16;
@@ -454,7 +477,8 @@ int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
     if (fabs(Ds) > eps) return ORC_ERR_BAD_INPUT;          /* module_moment_propagation.f90:60-66 */
     s->lambda = 4.0 * Db / kBT;                            /* module_moment_propagation.f90:331-337 */
     s->z = z;
-    if (fabs(z) > eps) return ORC_ERR_BAD_INPUT;            /* module_moment_propagation.f90:71-79 */
+    const int charged = fabs(z) > eps;
+    if (charged && !phi) return ORC_ERR_BAD_INPUT;          /* module_moment_propagation.f90:71-79 */
     long N = (long)lx * ly * lz;
     s->P_now = (double *)calloc(3 * N, sizeof(double));
     s->P_next = (double *)calloc(3 * N, sizeof(double));
@@ -462,26 +486,42 @@ int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
         s->A_now = (double *)calloc(3 * N, sizeof(double));
         s->A_next = (double *)calloc(3 * N, sizeof(double));
     }
-    long nf = 0, nfi = 0;
-    for (long r = 0; r < N; ++r) {
-        nf += nature[r] == 0;
-        nfi += nature[r] == 0 && interfacial[r];
+    if (charged) {
+        s->phi = (double *)malloc(sizeof(double) * N);
+        memcpy(s->phi, phi, sizeof(double) * N);
+        for (int d = 0; d < 3; ++d) s->E[d] = E[d];
     }
-    const double Pstat = (double)nf + s->K * (double)nfi;  /* module_moment_propagation.f90:97 */
+    double Pstat;
+    if (!charged) {
+        long nf = 0, nfi = 0;
+        for (long r = 0; r < N; ++r) {
+            nf += nature[r] == 0;
+            nfi += nature[r] == 0 && interfacial[r];
+        }
+        Pstat = (double)nf + s->K * (double)nfi;           /* module_moment_propagation.f90:97 */
+    } else {                                               /* module_moment_propagation.f90:99-100 */
+        double s1 = 0.0, s2 = 0.0;
+        for (long r = 0; r < N; ++r)
+            if (nature[r] == 0) s1 = s1 + exp(-(z * phi[r]));
+        for (long r = 0; r < N; ++r)
+            if (nature[r] == 0 && interfacial[r]) s2 = s2 + exp(-(z * phi[r])) * s->K;
+        Pstat = s1 + s2;
+    }
     double v[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < lz; ++k)
         for (int j = 0; j < ly; ++j)
             for (int i = 0; i < lx; ++i) {
                 long r = nid(i, j, k, lx, ly);
                 if (nature[r] != 0) continue;
-                const double bw = 1.0 / Pstat;
+                const double bw = charged ? exp(-(z * phi[r])) / Pstat : 1.0 / Pstat;
                 const double rho = density[r];
                 double *P = s->P_now + 3 * r;
                 for (int l = 1; l < Q; ++l) {
-                    long rp = nid(pbc0(i + VC[l][0], lx), pbc0(j + VC[l][1], ly),
-                                  pbc0(k + VC[l][2], lz), lx, ly);
+                    const int ip = pbc0(i + VC[l][0], lx), jp = pbc0(j + VC[l][1], ly),
+                              kp = pbc0(k + VC[l][2], lz);
+                    long rp = nid(ip, jp, kp, lx, ly);
                     if (nature[rp] == 1) continue;
-                    const double exp_dphi = 1.0;
+                    const double exp_dphi = orc_exp_dphi(s, i, j, k, ip, jp, kp);
                     const double exp_min_dphi = 1.0 / exp_dphi;
                     const double fermi = 1.0 / (1.0 + exp_dphi);
                     double sp = scattprop(n_mp[l + Q * r], rho, W0[l], s->lambda, fermi);
@@ -497,6 +537,28 @@ int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
         s->vacf[d] = v[d];
     }
     return ORC_OK;
+}
+
+int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
+                const uint8_t *interfacial, const double *density, const double *n_mp,
+                double ka, double kd, double Db, double Ds, double z, double vacf0[3])
+{
+    const double eps = 2.220446049250313e-16;
+    if (fabs(z) > eps) {                                    /* module_moment_propagation.f90:71-79 */
+        memset(s, 0, sizeof(*s));
+        return ORC_ERR_BAD_INPUT;
+    }
+    return mp_init_any(s, lx, ly, lz, nature, interfacial, density, n_mp, ka, kd, Db, Ds, z, NULL,
+                       NULL, vacf0);
+}
+
+int orc_mp_init_charged(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
+                        const uint8_t *interfacial, const double *density, const double *n_mp,
+                        double ka, double kd, double Db, double z, const double *phi,
+                        const double elec_slope[3], double vacf0[3])
+{
+    return mp_init_any(s, lx, ly, lz, nature, interfacial, density, n_mp, ka, kd, Db, 0.0, z, phi,
+                       elec_slope, vacf0);
 }
 
 /* module_moment_propagation.f90:164-289 */
@@ -522,10 +584,11 @@ int orc_mp_propagate(orc_mp_state *s, int it, const int8_t *nature, const uint8_
                 const double *nl = n_mp + Q * r;
                 double Pl[3] = {s->P_next[3 * r], s->P_next[3 * r + 1], s->P_next[3 * r + 2]};
                 for (int l = 1; l < Q; ++l) {
-                    long rp = nid(pbc0(i + VC[l][0], lx), pbc0(j + VC[l][1], ly),
-                                  pbc0(k + VC[l][2], lz), lx, ly);
+                    const int ip = pbc0(i + VC[l][0], lx), jp = pbc0(j + VC[l][1], ly),
+                              kp = pbc0(k + VC[l][2], lz);
+                    long rp = nid(ip, jp, kp, lx, ly);
                     if (nature[rp] != 0) continue;
-                    const double fermi = 1.0 / (1.0 + 1.0);
+                    const double fermi = 1.0 / (1.0 + orc_exp_dphi(s, i, j, k, ip, jp, kp));
                     double sp = scattprop(nl[l], density[r], W0[l], lambda, fermi);
                     frac = frac - sp;
                     for (int d = 0; d < 3; ++d) us[d] = us[d] + sp * (double)VC[l][d];
@@ -585,7 +648,9 @@ void orc_mp_free(orc_mp_state *s)
     free(s->P_next);
     free(s->A_now);
     free(s->A_next);
+    free(s->phi);
     s->P_now = s->P_next = s->A_now = s->A_next = NULL;
+    s->phi = NULL;
 }
 
 static const double PI_F = 3.141592653589793;   /* acos(-1.0_dp), module_constants.f90:19 */

@@ -97,6 +97,9 @@ typedef struct {
     double *P_now, *P_next;   /* 3*N each */
     double *A_now, *A_next;   /* 3*N each when adsorption is considered, else NULL */
     int nthreads;
+    /* charged tracer (orc_mp_init_charged): the potential phi (N, a copy) and elec_slope */
+    double *phi;
+    double E[3];
 } orc_mp_state;
 
 /* module_moment_propagation.f90:30-160 (init) for a neutral tracer.  Allocates the state's
@@ -104,6 +107,17 @@ typedef struct {
 int orc_mp_init(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
                 const uint8_t *interfacial, const double *density, const double *n_mp,
                 double ka, double kd, double Db, double Ds, double z, double vacf0[3]);
+
+/* The same for a charged tracer (z != 0) in the potential phi(lx,ly,lz) with elec_slope E, by
+ * the formulas the reference holds but stops before (module_moment_propagation.f90:71-79):
+ * Pstat = SUM(exp(-z phi), fluid) + SUM(exp(-z phi) K, fluid .and. interfacial) (:97-101),
+ * boltz_weight = exp(-z phi)/Pstat (:110), fermi = 1/(1 + exp(z dphi)) per link and
+ * P(r,1) += exp(-z dphi) scattprop_p c_inv boltz_weight (:123-135), dphi with the elec_slope
+ * correction of a link across the periodic boundary (:303-322).  z = 0 is orc_mp_init. */
+int orc_mp_init_charged(orc_mp_state *s, int lx, int ly, int lz, const int8_t *nature,
+                        const uint8_t *interfacial, const double *density, const double *n_mp,
+                        double ka, double kd, double Db, double z, const double *phi,
+                        const double elec_slope[3], double vacf0[3]);
 
 /* module_moment_propagation.f90:164-289 (propagate), one step `it` (1-based). */
 int orc_mp_propagate(orc_mp_state *s, int it, const int8_t *nature, const uint8_t *interfacial,

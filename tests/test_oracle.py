@@ -134,6 +134,78 @@ def test_vacf0_closed_form_in_the_slit(oracle_mod):
     mp.close()
 
 
+def _charged_case(oracle_mod, seed=4):
+    nat = geo.cc(7, 7, 7)
+    rng = np.random.default_rng(seed)
+    phi = 0.3 * rng.standard_normal(nat.shape)
+    rho = np.where(nat == 0, 1.0, 0.0)
+    j = [np.zeros(nat.shape)] * 3
+    inter = oracle_mod.detect_interfacial(nat)
+    return nat, phi, rho, j, inter
+
+
+def test_charged_tracer_vacf0_closed_form(oracle_mod):
+    """Fluid at rest, no field: n/rho - w = 0, so each link scatters lambda w_l fermi_l with
+    fermi_l = 1/(1 + exp(z dphi)): VACF_a(0) = sum_r w_B(r) sum_{fluid links} lambda w_l fermi_l
+    c_la^2, w_B(r) = exp(-z phi(r)) / (sum_fluid exp(-z phi) + K sum_interfacial exp(-z phi))."""
+    nat, phi, rho, j, inter = _charged_case(oracle_mod)
+    Db, ka, kd, z = 0.01, 0.01 * np.e, 0.01, 1.0
+    nmp = oracle_mod.update_tracer_population(nat, rho, j, (0, 0, 0), z, Db)
+    mp = oracle_mod.MomentPropagation(nat, inter, rho, nmp, ka=ka, kd=kd, Db=Db, z=z, phi=phi)
+    c, inv, a0, *_ = oracle_mod.tables()
+    lam = 4 * Db / (1 / 3)
+    fl = nat == 0
+    b = np.exp(-z * phi)
+    pstat = b[fl].sum() + (ka / kd) * b[fl & (inter == 1)].sum()
+    want = np.zeros(3)
+    for l in range(1, 19):
+        sh = lambda a: np.roll(a, shift=(-c[l, 2], -c[l, 1], -c[l, 0]), axis=(0, 1, 2))
+        link = fl & (sh(nat) == 0)
+        fermi = 1.0 / (1.0 + np.exp(z * (sh(phi) - phi)))
+        want += (b / pstat * lam * a0[l] * fermi)[link].sum() * c[l] ** 2
+    assert np.allclose(mp.vacf0, want, rtol=1e-12)
+    mp.close()
+
+
+def test_charged_tracer_in_a_uniform_potential_is_the_neutral_tracer(oracle_mod):
+    nat, _, _, _, inter = _charged_case(oracle_mod)
+    rng = np.random.default_rng(9)
+    rho = np.where(nat == 0, 1.0 + 0.01 * rng.standard_normal(nat.shape), 0.0)
+    j = [np.where(nat == 0, 1e-3 * rng.standard_normal(nat.shape), 0.0) for _ in range(3)]
+    Db, ka, kd = 0.02, 0.02, 0.01
+    out = []
+    for z, phi in ((0.0, None), (1.5, np.full(nat.shape, 0.7))):
+        nmp = oracle_mod.update_tracer_population(nat, rho, j, (1e-4, 0, 0), z, Db)
+        mp = oracle_mod.MomentPropagation(nat, inter, rho, nmp, ka=ka, kd=kd, Db=Db, z=z, phi=phi)
+        v = [mp.propagate(it)[0] for it in range(1, 6)]
+        out.append((mp.vacf0.copy(), np.array(v), mp.P()))
+        mp.close()
+    (v0a, va, Pa), (v0b, vb, Pb) = out
+    s = np.abs(v0a).max()
+    assert np.max(np.abs(v0a - v0b)) <= 1e-13 * s and np.max(np.abs(va - vb)) <= 1e-13 * s
+    assert np.max(np.abs(Pa - Pb)) <= 1e-13 * np.abs(Pa).max()
+
+
+def test_charged_tracer_sign_symmetry(oracle_mod):
+    """(z, phi) and (-z, -phi) give the same Boltzmann weights and fermi factors, bit for bit."""
+    nat, phi, rho, j, inter = _charged_case(oracle_mod, seed=6)
+    out = []
+    for z, p in ((1.0, phi), (-1.0, -phi)):
+        nmp = oracle_mod.update_tracer_population(nat, rho, j, (0, 0, 0), 0.0, 0.01)
+        mp = oracle_mod.MomentPropagation(nat, inter, rho, nmp, ka=0.03, kd=0.01, Db=0.01, z=z, phi=p)
+        v = [mp.propagate(it)[0] for it in range(1, 4)]
+        out.append((mp.vacf0.copy(), np.array(v), mp.P()))
+        mp.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out[0], out[1]))
+
+
+def test_neutral_init_still_refuses_a_charged_tracer(oracle_mod):
+    nat, phi, rho, j, inter = _charged_case(oracle_mod)
+    nmp = oracle_mod.update_tracer_population(nat, rho, j, (0, 0, 0), 1.0, 0.01)
+    with pytest.raises(oracle_mod.OracleError):
+        oracle_mod.MomentPropagation(nat, inter, rho, nmp, Db=0.01, z=1.0)
+
+
 def test_pnp_conserves_charge(oracle_mod):
     nat = geo.slit(1, 1, 16)
     inter = oracle_mod.detect_interfacial(nat)
