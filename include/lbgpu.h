@@ -291,6 +291,10 @@ size_t lbgpu_batch_footprint(const lbgpu_cell *cell);
 /* Add a box at rest (rho = rho0, j = 0) in the flow phase; *id is its slot.  LBGPU_ERR_OOM
  * beyond the budget. */
 int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *cell, const int8_t *nature, int *id);
+/* lbgpu_batch_add of the box of geometryLabel `label` (cell->lx, ly, lz; params as for
+ * lbgpu_geometry), built on the batch's device: no host geometry. */
+int lbgpu_batch_add_label(lbgpu_batch *b, const lbgpu_cell *cell, int label, const double *params,
+                          int *id);
 int lbgpu_batch_remove(lbgpu_batch *b, int id);
 /* nsteps (even) steps of every box in its phase; with check, du[id] = max|u - u_prev| per slot
  * of the flow-phase boxes (u_prev: the velocity at the previous check, 0 at the first). */

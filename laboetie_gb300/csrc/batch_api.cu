@@ -534,6 +534,19 @@ void lbgpu_batch_destroy(lbgpu_batch *b)
     delete b;
 }
 
+int lbgpu_batch_add_label(lbgpu_batch *b, const lbgpu_cell *c, int label, const double *params, int *id)
+{
+    if (!b || !c || !id) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add_label: null argument");
+    if (c->lx <= 0 || c->ly <= 0 || c->lz <= 0) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add_label: bad size");
+    const long long N = (long long)c->lx * c->ly * c->lz;
+    if (N >= (1LL << 31)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add_label: box too large");
+    // the compact layout of a tiled box is planned on the host, so the box comes back once
+    std::vector<int8_t> nature((size_t)N);
+    const int rc = lbgpu_geometry(b->device, label, c->lx, c->ly, c->lz, params, nature.data());
+    if (rc) return rc;   // the reference's message is in lbgpu_last_error(NULL, ...)
+    return lbgpu_batch_add(b, c, nature.data(), id);
+}
+
 int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, int *id)
 {
     TraceRange trace_("lbgpu_batch_add");

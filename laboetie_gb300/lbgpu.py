@@ -504,6 +504,7 @@ def _batch_lib():
         ("lbgpu_batch_destroy", [vp], None),
         ("lbgpu_batch_footprint", [C.POINTER(Cell)], C.c_size_t),
         ("lbgpu_batch_add", [vp, C.POINTER(Cell), vp, pi], C.c_int),
+        ("lbgpu_batch_add_label", [vp, C.POINTER(Cell), i, vp, pi], C.c_int),
         ("lbgpu_batch_remove", [vp, i], C.c_int),
         ("lbgpu_batch_steps", [vp, i, i, vp], C.c_int),
         ("lbgpu_batch_time_steps", [vp, i, C.POINTER(C.c_float)], C.c_int),
@@ -578,6 +579,18 @@ class Batch:
         i = C.c_int(-1)
         self._chk(self.L.lbgpu_batch_add(self.b, C.byref(cell), _ptr(nat), C.byref(i)), "batch_add")
         self._shapes[i.value] = nat.shape
+        return i.value
+
+    def add_label(self, label, lx, ly, lz, params=None, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0),
+                  rho0=1.0, tracer=None) -> int:
+        """A box of the reference's geometryLabel `label` built on the device
+        (lbgpu_batch_add_label); params: (lw_o_lx, a_o_R) for label 7."""
+        cell = make_cell((lx, ly, lz), relaxation_time, f_ext, rho0, tracer)
+        par = None if params is None else (C.c_double * len(params))(*params)
+        i = C.c_int(-1)
+        self._chk(self.L.lbgpu_batch_add_label(self.b, C.byref(cell), label, par, C.byref(i)),
+                  "batch_add_label")
+        self._shapes[i.value] = (lz, ly, lx)
         return i.value
 
     def remove(self, box: int):

@@ -51,3 +51,22 @@ def test_all_solid_box_is_refused_on_the_device():
         device_geometry(7, 4, 2, 2, (0.5, 0.1))
     with pytest.raises(LbgpuError, match="All nodes are solid"):
         Box.from_label(7, 4, 2, 2, (0.5, 0.1))
+
+
+def test_batch_box_by_label_equals_box_from_host_nature(oracle_mod):
+    """lbgpu_batch_add_label: the same flow state as lbgpu_batch_add with the oracle's array."""
+    from laboetie_gb300.lbgpu import Batch
+
+    code, nat = oracle_mod.geometry(2, 20, 20, 6)
+    assert code == 0
+    res = []
+    with Batch() as b:
+        a = b.add_label(2, 20, 20, 6, f_ext=(0.0, 0.0, 1e-5))
+        h = b.add(nat, f_ext=(0.0, 0.0, 1e-5))
+        b.steps(40)
+        res = [b.moments(a), b.moments(h)]
+    (ra, ja), (rh, jh) = res
+    assert np.array_equal(ra, rh) and all(np.array_equal(ja[d], jh[d]) for d in range(3))
+    with Batch() as b:
+        with pytest.raises(LbgpuError, match="should have same lx and ly"):
+            b.add_label(2, 20, 21, 6)
