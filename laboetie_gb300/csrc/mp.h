@@ -1,6 +1,7 @@
 // mp.h -- tracer moment propagation (drop_tracers.f90, module_moment_propagation.f90).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -97,7 +98,12 @@ cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
 cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s);
 cudaError_t launch_mp_reduce_init(double *partial, unsigned nblocks, MpCtl *ctl, cudaStream_t s);
 cudaError_t launch_mp_v32(const MpArgs64 &a64, float4 *V, cudaStream_t s);
-cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, cudaStream_t s);
+// tm: the tensor maps of V, P[0], P[1] for the slab step's bulk tensor copies, or null (the slab
+// step then stages every tile with per-thread asynchronous copies)
+cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, const CUtensorMap *tm, cudaStream_t s);
+// tensor maps of a box's float4 field (V or P) for the slab step: dims (4 components, lx, ly, lz),
+// box (4, 34, 10, 1); false if the driver refuses them
+bool mp32_tensor_map(CUtensorMap *tm, const float4 *field, int lx, int ly, int lz);
 cudaError_t launch_mp_init_f32(const MpArgs32 &a, float bw, unsigned grid, cudaStream_t s);
 
 }  // namespace lbg

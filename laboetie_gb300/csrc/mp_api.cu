@@ -18,6 +18,9 @@
 namespace lbg {
 
 struct MpState {
+    // FP32 slab step: tensor maps of V, P[0], P[1] for its bulk tensor copies (tma_ok)
+    CUtensorMap tm[3];
+    bool tma_ok = false;
     int prec = LBGPU_FP64;
     lbgpu_tracer tr{};
     int ads = 0;
@@ -249,6 +252,11 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
         for (int d = 0; d < 3; ++d) b.E[d] = (float)tr->elec_slope[d];
         LBG_CK(ctx, launch_mp_v32(a, V, st));
         LBG_CK(ctx, launch_mp_init_f32(b, (float)s->bw, s->nblocks, st));
+        // bulk tensor copies for the slab step's interior tiles (LBGPU_MP_TMA=0: per-thread copies)
+        const char *tma_env = std::getenv("LBGPU_MP_TMA");
+        s->tma_ok = !(tma_env && std::string(tma_env) == "0") && mp32_tensor_map(&s->tm[0], b.V, a.lx, a.ly, a.lz) &&
+                    mp32_tensor_map(&s->tm[1], b.P[0], a.lx, a.ly, a.lz) &&
+                    mp32_tensor_map(&s->tm[2], b.P[1], a.lx, a.ly, a.lz);
     }
     LBG_CK(ctx, launch_mp_reduce_init(a.partial, s->nblocks, a.ctl, st));
     if (tmp) LBG_CK(ctx, cudaFreeAsync(tmp, st));
@@ -310,7 +318,7 @@ static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done,
     for (int k = 0; k < G; ++k) {
         const unsigned grid = std::min(s->nblocks, MP_MAX_BLOCKS);
         cudaError_t e = s->prec == LBGPU_FP64 ? launch_mp_step_f64(s->a64, grid, st)
-                                              : launch_mp_step_f32(s->a32, grid, st);
+                                              : launch_mp_step_f32(s->a32, grid, s->tma_ok ? s->tm : nullptr, st);
         if (e != cudaSuccess) {
             cudaStreamEndCapture(st, &g);
             return ctx_cuda(ctx, e, "capture moment propagation");
@@ -342,6 +350,9 @@ static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done,
     }
     cudaGraphExecDestroy(exec);
     if (rc) return rc;
+    if (c.status & LBGPU_ERR_TIMEOUT)
+        return ctx_fail(ctx, LBGPU_ERR_TIMEOUT,
+                        "moment propagation: a bulk copy into shared memory did not complete within its wait limit");
     const int done = c.last_it - c.it_base + 1;
     if (hist) {
         if (vacf_out && done > 0)

@@ -11,6 +11,10 @@
 // reads the node's (u*, D)); the VACF node sum is formed per thread in FP32 over a few nodes and
 // in FP64 across threads and blocks.  Solid neighbours hold V = 0 and P = 0 and their links are
 // masked to zero, so the gathers are branch-free and can all be in flight at once.
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
 #include "common.cuh"
 #include "cpasync.cuh"
 #include "lbgpu.h"
@@ -170,8 +174,11 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
 }
 
 // One tracer step of a box with V and P staged in shared memory (mp_slab.cuh): a block owns a
-// 32 x 8 column tile and a chunk of zc planes.
-__global__ void __launch_bounds__(MP_BLOCK, 5) k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc)
+// 32 x 8 column tile and a chunk of zc planes.  With use_tma, interior tiles stage their planes
+// by bulk tensor copies through the tensor maps of V and P[0], P[1] (kernel parameters).
+__global__ void __launch_bounds__(MP_BLOCK, 5)
+    k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc, const __grid_constant__ CUtensorMap tmV,
+                const __grid_constant__ CUtensorMap tmP0, const __grid_constant__ CUtensorMap tmP1, int use_tma)
 {
     const volatile MpCtl *vc = a.ctl;
     if (vc->done) return;
@@ -182,7 +189,8 @@ __global__ void __launch_bounds__(MP_BLOCK, 5) k_mp32_slab(const MpArgs32 a, int
     const int z0 = chunk * zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
     mp_slab_sweep<true>(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
-                  sm4, vt);
+                        sm4, vt, use_tma ? &tmV : nullptr, use_tma ? (par ? &tmP1 : &tmP0) : nullptr,
+                        &a.ctl->status);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     grid_sum3(v, a.partial, &a.ctl->blocks_done,
               [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });
@@ -213,13 +221,41 @@ cudaError_t launch_mp_v32(const MpArgs64 &a64, float4 *V, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, cudaStream_t s)
+bool mp32_tensor_map(CUtensorMap *tm, const float4 *field, int lx, int ly, int lz)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return false;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    // the float4 field as a 4-D FP32 tensor (component, x, y, z); box = one plane of a tile with
+    // its halo (4 x 34 x 10 x 1), landing as the ring plane's SHX x SHY float4 records
+    const cuuint64_t dims[4] = {4, (cuuint64_t)lx, (cuuint64_t)ly, (cuuint64_t)lz};
+    const cuuint64_t strides[3] = {16, 16ull * (cuuint64_t)lx, 16ull * (cuuint64_t)lx * (cuuint64_t)ly};
+    const cuuint32_t box[4] = {4, (cuuint32_t)SHX, (cuuint32_t)SHY, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float4 *>(field), dims, strides, box,
+                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, const CUtensorMap *tm, cudaStream_t s)
 {
     int zc = 0;
     const unsigned sg = a.slab && !a.charged ? mp32_slab_grid(a.lx, a.ly, a.lz, &zc) : 0u;
     if (sg) {
         const int tx = (a.lx + MPS_TX - 1) / MPS_TX, ty = (a.ly + MPS_TY - 1) / MPS_TY;
-        k_mp32_slab<<<sg, MP_BLOCK, MPS_SMEM, s>>>(a, tx, ty, zc);
+        CUtensorMap none;
+        std::memset(&none, 0, sizeof(none));
+        k_mp32_slab<<<sg, MP_BLOCK, MPS_SMEM, s>>>(a, tx, ty, zc, tm ? tm[0] : none, tm ? tm[1] : none,
+                                                   tm ? tm[2] : none, tm ? 1 : 0);
     } else {
         if (a.charged) k_mp32<false, true><<<grid, MP_BLOCK, 0, s>>>(a, 0.0f);
         else k_mp32<false, false><<<grid, MP_BLOCK, 0, s>>>(a, 0.0f);

@@ -14,12 +14,19 @@
 
 #include "common.cuh"
 #include "cpasync.cuh"
+#include "lbgpu.h"
 #include "mp.h"
+#include "tma.cuh"
 
 namespace lbg {
 
 constexpr int SHX = MPS_TX + 2, SHY = MPS_TY + 2, SPL = SHX * SHY;  // a plane with its halo
-constexpr size_t MPS_SMEM = sizeof(float4) * 8 * SPL;                // 4 planes of V and of P
+// plane stride in float4: 344 = SPL rounded up to 128 bytes (a bulk tensor copy lands on a
+// 128-byte boundary)
+constexpr int SPLP = (SPL * 16 + 127) / 128 * 8;
+constexpr unsigned MPS_TMA_BYTES = SPL * 16;                        // one plane of V or of P
+// 4 planes of V and of P, 4 mbarriers, and slack to align the ring to 128 bytes
+constexpr size_t MPS_SMEM = 128 + sizeof(float4) * 8 * SPLP + 4 * sizeof(uint64_t);
 
 // Scattering probability of a link, on * (a1 (c.V) + lambda w / 2) (on = 0 across a
 // bounce-back link), rounded as written.
@@ -63,17 +70,47 @@ __device__ __forceinline__ float slab_cdot(const float4 &v)
 // (MP_BLOCK = 256 = 32 x 8) must call it.  AUX: the difference form of mp_f32.cu:k_mp32 with the
 // node's fixed (u*, D) from a.aux (18 scatterings per node and step); otherwise the flux form
 // P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings).
+// tmV / tmP (optional): tensor maps of V and of P(par) (mp32_tensor_map); a tile whose plane
+// with its halo lies inside the box (no periodic wrap in x or y) then stages each plane with two
+// bulk tensor copies issued by one thread and completed on the ring slot's mbarrier, instead of
+// 2 x 340 per-thread copies with wrap arithmetic; a wait that runs out of its bound sets
+// LBGPU_ERR_TIMEOUT in *status and the tile's nodes are left alone.
 template <bool AUX, typename Args>
 __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, int y0, int z0, int z1,
-                                              float4 *sm, float (&vt)[3])
+                                              float4 *sm_raw, float (&vt)[3],
+                                              const CUtensorMap *tmV = nullptr,
+                                              const CUtensorMap *tmP = nullptr,
+                                              unsigned *status = nullptr)
 {
-    float4 *sV = sm, *sP = sm + 4 * SPL;
+    // align the ring to 128 bytes by offsetting the shared-memory pointer itself (rounding its
+    // generic address would hide from the compiler that it points to shared memory, and every
+    // ring read would become a generic load)
+    float4 *sm = sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u;
+    float4 *sV = sm, *sP = sm + 4 * SPLP;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 8 * SPLP);   // one per ring slot
     const int lx = a.lx, ly = a.ly, lz = a.lz;
     const float4 *__restrict__ Vg = a.V;
     const float4 *__restrict__ Pg = a.P[par];
+    const bool tma = tmV != nullptr && x0 >= 1 && x0 + MPS_TX + 1 <= lx && y0 >= 1 && y0 + MPS_TY + 1 <= ly;
+    if (tma) {
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < 4; ++q) mbar_init(&bars[q], 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+    }
     auto load_plane = [&](int zz) {
         const int gz = zz < 0 ? zz + lz : (zz >= lz ? zz - lz : zz);
-        float4 *dv = sV + ((zz - z0 + 1) & 3) * SPL, *dp = sP + ((zz - z0 + 1) & 3) * SPL;
+        const int slot = (zz - z0 + 1) & 3;
+        float4 *dv = sV + slot * SPLP, *dp = sP + slot * SPLP;
+        if (tma) {
+            if (threadIdx.x == 0) {
+                mbar_arrive_expect_tx(&bars[slot], 2 * MPS_TMA_BYTES);
+                tma_load_4d(dv, tmV, 0, x0 - 1, y0 - 1, gz, &bars[slot]);
+                tma_load_4d(dp, tmP, 0, x0 - 1, y0 - 1, gz, &bars[slot]);
+            }
+            return;
+        }
         for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
             const int hx = k % SHX, hy = k / SHX;
             int gx = x0 + hx - 1, gy = y0 + hy - 1;
@@ -88,9 +125,15 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
     const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
     const int x = x0 + tx, y = y0 + ty;
     const bool col = x < lx && y < ly;
+    // the fill of plane zz is its slot's ((zz - z0 + 1) / 4)-th: the phase parity to wait for
+    auto wait_plane = [&](int zz) {
+        return mbar_wait(&bars[(zz - z0 + 1) & 3], (unsigned)(((zz - z0 + 1) >> 2) & 1));
+    };
     load_plane(z0 - 1);
     load_plane(z0);
     load_plane(z0 + 1);
+    bool ok = true;
+    if (tma) ok = wait_plane(z0 - 1) && wait_plane(z0);
     // the column's flag word (and, AUX, fixed node data) of the next plane, loaded a plane ahead
     // so that no plane starts on a global-memory round trip
     const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
@@ -99,7 +142,8 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
     if constexpr (AUX)
         if (col) ax_next = __ldg(a.aux + col0 + plane * z0);
     for (int z = z0; z < z1; ++z) {
-        cp_async_wait0();
+        if (!tma) cp_async_wait0();
+        else if (ok) ok = wait_plane(z + 1);
         __syncthreads();
         if (z + 2 <= z1) load_plane(z + 2);
         const size_t r = col0 + plane * z;
@@ -109,11 +153,11 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
             m_next = __ldg(a.mask + r + plane);
             if constexpr (AUX) ax_next = __ldg(a.aux + r + plane);
         }
-        if (m & FLUID_BIT) {
+        if (ok && (m & FLUID_BIT)) {
             const int c0 = (ty + 1) * SHX + (tx + 1);
             const int s0 = (z - z0 + 1) & 3;
-            const float4 vr = sV[s0 * SPL + c0];
-            const float4 p = sP[s0 * SPL + c0];
+            const float4 vr = sV[s0 * SPLP + c0];
+            const float4 p = sP[s0 * SPLP + c0];
             float ux = 0.0f, uy = 0.0f, uz = 0.0f;
             float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
             static_for<1, Q>([&](auto L) {
@@ -121,7 +165,7 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
                 constexpr Vel c = vel(l);
                 constexpr int w = wclass(l);
                 const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
-                const int q = ((z + c.z - z0 + 1) & 3) * SPL + c0 + c.y * SHX + c.x;
+                const int q = ((z + c.z - z0 + 1) & 3) * SPLP + c0 + c.y * SHX + c.x;
                 const float4 vn = sV[q];
                 const float4 pn = sP[q];
                 if constexpr (AUX) {
@@ -163,6 +207,7 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
             __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
         }
     }
+    if (!ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
 }
 
 }  // namespace lbg

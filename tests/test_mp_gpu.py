@@ -159,3 +159,26 @@ def test_mp_fp32_slab_and_grid_stride_steps_agree(monkeypatch):
     assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
     assert len(a[1]) == len(b[1]) == 37
     assert np.max(np.abs(a[1] - b[1])) <= 1e-12 * np.abs(a[0]).max()
+
+
+def test_fp32_slab_bulk_tensor_copies_equal_per_thread_copies(monkeypatch):
+    """The slab step stages interior tiles by bulk tensor copies (TMA) and edge tiles (periodic
+    wrap) by per-thread copies; with LBGPU_MP_TMA=0 every tile uses per-thread copies and with
+    LBGPU_MP_SLAB=0 the grid-stride kernel runs: P and P_ads bit-identical in all three.  100 x 40
+    x 12 has interior tiles in x (x0 = 32) and y (y0 = 8 .. 24) beside edge tiles."""
+    rng = np.random.default_rng(11)
+    nat = (rng.random((12, 40, 100)) < 0.3).astype(np.int8)
+    rho = np.where(nat == 0, 1.0 + 1e-3 * rng.standard_normal(nat.shape), 0.0)
+    j = [np.where(nat == 0, 1e-3 * rng.standard_normal(nat.shape), 0.0) for _ in range(3)]
+    out = {}
+    for name, env in (("tma", {}), ("copies", {"LBGPU_MP_TMA": "0"}), ("grid", {"LBGPU_MP_SLAB": "0"})):
+        for k in ("LBGPU_MP_TMA", "LBGPU_MP_SLAB"):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        with Box(nat, precision=FP32_DEV) as box:
+            box.mp_init(moments=(rho, j), Db=0.01, ka=0.02, kd=0.01)
+            box.mp_propagate(23)
+            out[name] = box.mp_get()
+    for name in ("copies", "grid"):
+        assert np.array_equal(out["tma"][0], out[name][0]) and np.array_equal(out["tma"][1], out[name][1])
