@@ -44,8 +44,8 @@ __device__ __forceinline__ unsigned lattice_of(const A &a, unsigned c)
 // x + 1 fluid), and the node's own row needs no lookup (cnt = i).  The eight lookups are made
 // up front, independent of the bounce-back bits, so that they are in flight together and each
 // serves every direction into its row; only a wrap across the periodic x boundary takes a second
-// lookup.
-template <typename A, typename Fn>
+// lookup.  Off: the type of the offsets (unsigned while 19 Nf < 2^32, else 64-bit).
+template <typename Off = unsigned, typename A, typename Fn>
 __device__ __forceinline__ void aa_gather_offsets(const A &a, unsigned i, unsigned c,
                                                   uint32_t m, Fn &&f)
 {
@@ -71,7 +71,7 @@ __device__ __forceinline__ void aa_gather_offsets(const A &a, unsigned i, unsign
         constexpr int l = decltype(L)::value;
         constexpr Vel v = vel(l);
         if constexpr (l == 0) {
-            f(0, i);
+            f(0, (Off)i);
         } else {
             constexpr int k = 3 * (v.y + 1) + (v.z + 1);
             unsigned s;
@@ -90,7 +90,7 @@ __device__ __forceinline__ void aa_gather_offsets(const A &a, unsigned i, unsign
                     else s = x < lx - 1 ? cnt + ((e[k].x >> b) & 1u) : compact_in_row(tab, rb, 0);
                 }
             }
-            f(l, ((m >> l) & 1u) ? (unsigned)l * Nf + i : (unsigned)inv(l) * Nf + s);
+            f(l, ((m >> l) & 1u) ? (Off)l * Nf + i : (Off)inv(l) * Nf + s);
         }
     });
 }

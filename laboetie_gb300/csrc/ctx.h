@@ -73,6 +73,7 @@ struct lbgpu_ctx {
     // rowtab[row*nw + w] = {fluid bits of word w of lattice row y + ly*z, compact index of the
     // first fluid node of that word}
     unsigned Nf = 0;
+    bool aa_wide = false;        // Q*Nf >= 2^32 (or LBGPU_AA_WIDE=1): 64-bit gather offsets
     int nw = 0, xbits = 0, ybits = 0;
     uint32_t *d_cpos = nullptr, *d_cmask = nullptr;
     uint2 *d_rowtab = nullptr;

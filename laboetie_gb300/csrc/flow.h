@@ -53,6 +53,7 @@ struct FlowArgs32 {
     int minb_even, minb_odd;     // AA kernel variants (resident blocks per SM)
     // AA layout over the fluid nodes only (ctx.h): g0 holds Q*Nf deviations
     unsigned Nf;
+    int wide;                    // Q*Nf >= 2^32: gathers form 64-bit slot offsets
     int nw;
     const uint32_t *cpos, *cmask;
     const uint2 *rowtab;

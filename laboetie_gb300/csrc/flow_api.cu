@@ -74,6 +74,18 @@ int build_compact_layout(lbgpu_ctx *ctx, const int8_t *nature)
     return LBGPU_OK;
 }
 
+// LBGPU_ERR_OOM unless `need` bytes are free on the device
+int check_room(lbgpu_ctx *ctx, size_t need)
+{
+    size_t fr = 0, tot = 0;
+    LBG_CK(ctx, cudaMemGetInfo(&fr, &tot));
+    if (need > fr)
+        return ctx_fail(ctx, LBGPU_ERR_OOM,
+                        "lbgpu_create: box needs " + std::to_string(need >> 20) + " MiB, " +
+                            std::to_string(fr >> 20) + " MiB free on the device");
+    return LBGPU_OK;
+}
+
 }  // namespace
 
 int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
@@ -84,15 +96,10 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     LBG_CK(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     LBG_CK(ctx, cudaEventCreate(&ctx->ev0));
     LBG_CK(ctx, cudaEventCreate(&ctx->ev1));
-    const size_t pop = p.precision == LBGPU_FP64 ? sizeof(double) : sizeof(float);
-    const size_t need = (size_t)N * (1 + 4 + 2 * Q * pop + 4 * sizeof(double)) + (1 << 20);
-    size_t fr = 0, tot = 0;
-    LBG_CK(ctx, cudaMemGetInfo(&fr, &tot));
-    if (need > fr) {
-        return ctx_fail(ctx, LBGPU_ERR_OOM,
-                        "lbgpu_create: box needs " + std::to_string(need >> 20) + " MiB, " +
-                            std::to_string(fr >> 20) + " MiB free on the device");
-    }
+    // per lattice node: nature, flag word, rho and j (FP64), and for FP64 two population sets;
+    // FP32 populations are checked once the layout (A/B or fluid nodes only) is known
+    const size_t pop = p.precision == LBGPU_FP64 ? 2 * Q * sizeof(double) : 0;
+    if (int rc = check_room(ctx, (size_t)N * (1 + 4 + pop + 4 * sizeof(double)) + (1 << 20))) return rc;
     LBG_CK(ctx, dalloc(&ctx->d_nature, N));
     LBG_CK(ctx, dalloc(&ctx->d_mask, N));
     LBG_CK(ctx, cudaMemcpyAsync(ctx->d_nature, nature, N, cudaMemcpyHostToDevice, ctx->stream));
@@ -110,10 +117,14 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     } else {
         const char *mode = std::getenv("LBGPU_FP32_STREAMING");
         ctx->aa = !(mode && std::string(mode) == "ab");
-        if (ctx->aa && (unsigned long long)Q * ctx->counts[0] >= (1ULL << 32))
-            return ctx_fail(ctx, LBGPU_ERR_INVALID,
-                            "FP32 in-place streaming addresses 19*Nf populations with 32-bit "
-                            "indices: box too large (use LBGPU_FP32_STREAMING=ab)");
+        // AA: one set of Q*Nf populations + packed position and flag word per fluid node; A/B: two
+        // sets per lattice node
+        const unsigned long long nf = ctx->counts[0];
+        if (int rc = check_room(ctx, ctx->aa ? nf * (Q * sizeof(float) + 8) : 2ull * Q * sizeof(float) * N))
+            return rc;
+        // beyond 2^32 slots the odd launches form 64-bit offsets (LBGPU_AA_WIDE=1 forces them)
+        const char *wide = std::getenv("LBGPU_AA_WIDE");
+        ctx->aa_wide = (unsigned long long)Q * nf >= (1ULL << 32) || (wide && std::string(wide) == "1");
         if (const char *e = std::getenv("LBGPU_AA_MINB")) {  // "<even>,<odd>", e.g. "4,3"
             int ev = 0, od = 0;
             if (std::sscanf(e, "%d,%d", &ev, &od) == 2) {

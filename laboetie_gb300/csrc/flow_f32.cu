@@ -12,6 +12,7 @@
 // for the rest density.  Moments handed back to the host are accumulated in FP64.
 #include <algorithm>
 #include <cfloat>
+#include <type_traits>
 
 #include "collide32.cuh"
 #include "common.cuh"
@@ -112,18 +113,19 @@ __global__ void __launch_bounds__(BLOCK) k_step32(const FlowArgs32 a)
 // writes 19 dense arrays with no solid node in any sector, and the odd launch finds a fluid
 // neighbour's slot through the row bitmask table.
 // One AA update of the compact node i; odd launches take its flag word m and lattice index p.
-template <bool ODD, int FMASK>
+// Off: type of the slot offsets of an odd launch (64-bit once Q*Nf reaches 2^32).
+template <bool ODD, int FMASK, typename Off>
 __device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint32_t m, unsigned p,
-                                          unsigned (*soff)[BLOCK], int fm, int fc)
+                                          Off (*soff)[BLOCK], int fm, int fc)
 {
     // Each thread writes only the slots it has read, and every value it writes depends on all
     // of them: no store can overtake a load, so the two views of the buffer may be restricted.
     const float *__restrict__ gin = a.g0;
     float *__restrict__ gout = a.g0;
-    const unsigned Nf = a.Nf;  // 19*Nf < 2^32 is checked when the context is created
+    const unsigned Nf = a.Nf;  // even launches step pointers by Nf: 64-bit addresses throughout
     float f[Q];
     if constexpr (ODD) {
-        aa_gather_offsets(a, i, p, m, [&](int l, unsigned o) {
+        aa_gather_offsets<Off>(a, i, p, m, [&](int l, Off o) {
             soff[l][threadIdx.x] = o;
             f[l] = __ldg(gin + o);
         });
@@ -165,13 +167,14 @@ __device__ __forceinline__ void aa_update(const FlowArgs32 &a, unsigned i, uint3
 // gather is covered by occupancy: the tuner in flow_f32_api.cu picks the launch bounds).  Odd
 // launches walk the nodes in reverse block order, so each launch starts on the nodes the
 // previous one wrote last, which are still in L2 (about 55 MB of the 323 MB of populations of the
-// 192^3 benchmark box).
-template <bool ODD, int FMASK, int MINB, bool LOOP>
+// 192^3 benchmark box).  WIDE: 64-bit slot offsets, for boxes with Q*Nf >= 2^32.
+template <bool ODD, int FMASK, int MINB, bool LOOP, bool WIDE = false>
 __global__ void __launch_bounds__(BLOCK, MINB) k_aa32(const FlowArgs32 a)
 {
+    using Off = std::conditional_t<WIDE, unsigned long long, unsigned>;
     // odd launches: element index of the slot read for direction l, parked in shared memory
     // ([l][thread], conflict-free) so that it does not occupy registers across the collision
-    __shared__ unsigned soff[ODD ? Q : 1][BLOCK];
+    __shared__ Off soff[ODD ? Q : 1][BLOCK];
     int fm = a.force_moment, fc = a.force_collide;
     if constexpr (LOOP) {   // reference loop: forces decided on the device; no-op after the exit
         const volatile FlowCtl *c = a.ctl;
@@ -232,7 +235,7 @@ __device__ void control_step32(FlowCtl *c, double *hist, int phase)
 // an odd launch, SWAPPED after an even one) with the state's moment force, max |j - j_old| over
 // the fluid nodes, n = d + w rho0 < 0 and non-finite tests, j stored for the next check; the
 // last block runs the control step.  A no-op once the loop has exited.
-template <bool SWAPPED>
+template <bool SWAPPED, typename Off = unsigned>
 __global__ void __launch_bounds__(BLOCK) k_aa_check32(const FlowArgs32 a)
 {
     const volatile FlowCtl *vc = a.ctl;
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(BLOCK) k_aa_check32(const FlowArgs32 a)
         const float *g = a.g0;
         float f[Q];
         if constexpr (SWAPPED) {
-            aa_gather_offsets(a, i, c, a.cmask[i], [&](int l, unsigned o) { f[l] = g[o]; });
+            aa_gather_offsets<Off>(a, i, c, a.cmask[i], [&](int l, Off o) { f[l] = g[o]; });
         } else {
 #pragma unroll
             for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * a.Nf + i];
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(BLOCK) k_aa_check32(const FlowArgs32 a)
 // Moments (FP64) of an AA buffer: natural order after an odd launch (SWAPPED = false), or
 // post-collision values in opposite slots after an even launch (SWAPPED = true, gathered as
 // the next odd launch would).
-template <bool SWAPPED>
+template <bool SWAPPED, typename Off = unsigned>
 __global__ void __launch_bounds__(BLOCK) k_aa_finalize32(const FlowArgs32 a)
 {
     // solid nodes: the outputs were zeroed by the host (the reference's zeros)
@@ -314,7 +317,7 @@ __global__ void __launch_bounds__(BLOCK) k_aa_finalize32(const FlowArgs32 a)
     const float *g = a.g0;
     float f[Q];
     if constexpr (SWAPPED) {
-        aa_gather_offsets(a, i, c, a.cmask[i], [&](int l, unsigned o) { f[l] = g[o]; });
+        aa_gather_offsets<Off>(a, i, c, a.cmask[i], [&](int l, Off o) { f[l] = g[o]; });
     } else {
 #pragma unroll
         for (int l = 0; l < Q; ++l) f[l] = g[(size_t)l * a.Nf + i];
@@ -487,7 +490,10 @@ static void aa_launch(const FlowArgs32 &a, bool odd, unsigned grid, cudaStream_t
 {
     // the loop variant is a separate instantiation: the control-block read costs the hot
     // fixed-step kernel ~2 % when it is only a run-time branch
-    if (a.ctl) {
+    if (odd && a.wide) {   // one variant: the tuner's choice applies to 32-bit offsets
+        if (a.ctl) k_aa32<true, FM, 4, true, true><<<grid, BLOCK, 0, s>>>(a);
+        else k_aa32<true, FM, 4, false, true><<<grid, BLOCK, 0, s>>>(a);
+    } else if (a.ctl) {
         if (odd) k_aa32<true, FM, MINB, true><<<grid, BLOCK, 0, s>>>(a);
         else k_aa32<false, FM, MINB, true><<<grid, BLOCK, 0, s>>>(a);
     } else {
@@ -517,7 +523,8 @@ cudaError_t launch_aa_step_f32(const FlowArgs32 &a, bool odd, cudaStream_t s)
 cudaError_t launch_aa_check_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s)
 {
     const unsigned grid = (a.Nf + BLOCK - 1) / BLOCK;
-    if (swapped) k_aa_check32<true><<<grid, BLOCK, 0, s>>>(a);
+    if (swapped && a.wide) k_aa_check32<true, unsigned long long><<<grid, BLOCK, 0, s>>>(a);
+    else if (swapped) k_aa_check32<true><<<grid, BLOCK, 0, s>>>(a);
     else k_aa_check32<false><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -538,7 +545,8 @@ cudaError_t launch_to_dev_compact32(const FlowArgs32 &a, const double *n, float 
 cudaError_t launch_aa_finalize_f32(const FlowArgs32 &a, bool swapped, cudaStream_t s)
 {
     const unsigned grid = (a.Nf + BLOCK - 1) / BLOCK;
-    if (swapped) k_aa_finalize32<true><<<grid, BLOCK, 0, s>>>(a);
+    if (swapped && a.wide) k_aa_finalize32<true, unsigned long long><<<grid, BLOCK, 0, s>>>(a);
+    else if (swapped) k_aa_finalize32<true><<<grid, BLOCK, 0, s>>>(a);
     else k_aa_finalize32<false><<<grid, BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }

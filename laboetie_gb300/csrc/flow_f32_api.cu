@@ -42,6 +42,7 @@ static void fill_args32(lbgpu_ctx *ctx, FlowArgs32 &a)
     a.minb_even = ctx->aa_minb[0];
     a.minb_odd = ctx->aa_minb[1];
     a.Nf = ctx->Nf;
+    a.wide = ctx->aa_wide;
     a.nw = ctx->nw;
     a.cpos = ctx->d_cpos;
     a.cmask = ctx->d_cmask;

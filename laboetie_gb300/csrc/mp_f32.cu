@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(MP_BLOCK, 5)
     const int tile = (int)blockIdx.x % nxy, chunk = (int)blockIdx.x / nxy;
     const int z0 = chunk * zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    mp_slab_sweep<true>(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
+    mp_slab_sweep<true, true>(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
                         sm4, vt, use_tma ? &tmV : nullptr, use_tma ? (par ? &tmP1 : &tmP0) : nullptr,
                         &a.ctl->status);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};

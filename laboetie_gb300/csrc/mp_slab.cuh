@@ -70,12 +70,14 @@ __device__ __forceinline__ float slab_cdot(const float4 &v)
 // (MP_BLOCK = 256 = 32 x 8) must call it.  AUX: the difference form of mp_f32.cu:k_mp32 with the
 // node's fixed (u*, D) from a.aux (18 scatterings per node and step); otherwise the flux form
 // P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings).
-// tmV / tmP (optional): tensor maps of V and of P(par) (mp32_tensor_map); a tile whose plane
-// with its halo lies inside the box (no periodic wrap in x or y) then stages each plane with two
-// bulk tensor copies issued by one thread and completed on the ring slot's mbarrier, instead of
-// 2 x 340 per-thread copies with wrap arithmetic; a wait that runs out of its bound sets
-// LBGPU_ERR_TIMEOUT in *status and the tile's nodes are left alone.
-template <bool AUX, typename Args>
+// TMA, with tmV / tmP the tensor maps of V and of P(par) (mp32_tensor_map; nullptr turns it off
+// at run time): a tile whose plane with its halo lies inside the box (no periodic wrap in x or y)
+// stages each plane with two bulk tensor copies issued by one thread and completed on the ring
+// slot's mbarrier, instead of 2 x 340 per-thread copies with wrap arithmetic; a wait that runs
+// out of its bound sets LBGPU_ERR_TIMEOUT in *status and the tile's nodes are left alone.
+// Without TMA none of that is compiled (the barriers, the 128-byte pad and the predicate cost a
+// caller 11 registers).
+template <bool AUX, bool TMA, typename Args>
 __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, int y0, int z0, int z1,
                                               float4 *sm_raw, float (&vt)[3],
                                               const CUtensorMap *tmV = nullptr,
@@ -85,13 +87,13 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
     // align the ring to 128 bytes by offsetting the shared-memory pointer itself (rounding its
     // generic address would hide from the compiler that it points to shared memory, and every
     // ring read would become a generic load)
-    float4 *sm = sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u;
+    float4 *sm = TMA ? sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u : sm_raw;
     float4 *sV = sm, *sP = sm + 4 * SPLP;
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 8 * SPLP);   // one per ring slot
     const int lx = a.lx, ly = a.ly, lz = a.lz;
     const float4 *__restrict__ Vg = a.V;
     const float4 *__restrict__ Pg = a.P[par];
-    const bool tma = tmV != nullptr && x0 >= 1 && x0 + MPS_TX + 1 <= lx && y0 >= 1 && y0 + MPS_TY + 1 <= ly;
+    const bool tma = TMA && tmV != nullptr && x0 >= 1 && x0 + MPS_TX + 1 <= lx && y0 >= 1 && y0 + MPS_TY + 1 <= ly;
     if (tma) {
         if (threadIdx.x == 0) {
             for (int q = 0; q < 4; ++q) mbar_init(&bars[q], 1);
@@ -143,7 +145,7 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
         if (col) ax_next = __ldg(a.aux + col0 + plane * z0);
     for (int z = z0; z < z1; ++z) {
         if (!tma) cp_async_wait0();
-        else if (ok) ok = wait_plane(z + 1);
+        else if (TMA && ok) ok = wait_plane(z + 1);
         __syncthreads();
         if (z + 2 <= z1) load_plane(z + 2);
         const size_t r = col0 + plane * z;
@@ -153,7 +155,7 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
             m_next = __ldg(a.mask + r + plane);
             if constexpr (AUX) ax_next = __ldg(a.aux + r + plane);
         }
-        if (ok && (m & FLUID_BIT)) {
+        if ((!TMA || ok) && (m & FLUID_BIT)) {
             const int c0 = (ty + 1) * SHX + (tx + 1);
             const int s0 = (z - z0 + 1) & 3;
             const float4 vr = sV[s0 * SPLP + c0];
@@ -207,7 +209,7 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
             __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
         }
     }
-    if (!ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
+    if (TMA && !ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
 }
 
 }  // namespace lbg

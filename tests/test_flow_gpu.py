@@ -252,6 +252,36 @@ def test_fp32_in_place_and_two_buffer_streaming_agree(monkeypatch):
             assert np.array_equal(ja[d], jb[d])
 
 
+def test_fp32_wide_gather_offsets_bit_identical(monkeypatch):
+    """64-bit slot offsets of the in-place layout (taken once 19 Nf reaches 2^32; LBGPU_AA_WIDE=1
+    forces them on any box) give the same bits as 32-bit ones: fixed steps, read back after odd
+    and even counts (swapped state), and the reference loop with its checks."""
+    nat = geo.porous_spheres(L=16, radius=3.0, porosity=0.65, seed=11)
+    out = {}
+    for wide in ("0", "1"):
+        monkeypatch.setenv("LBGPU_AA_WIDE", wide)
+        res = []
+        with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 2e-6, 0.0), precision=FP32_DEV) as box:
+            box.flow_init()
+            for k in (1, 6, 13):
+                box.flow_steps(k, force_on=True)
+                res.append(box.flow_get())
+        # the loop's checks on every step, stopped by the step cap (status kept, state readable)
+        with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 0.0, 0.0), target_error=1e-12,
+                 precision=FP32_DEV) as box:
+            box.flow_init()
+            steps, hist, rc = box.equilibration(max_steps=3001, hist_cap=3001, check=False)
+            res.append((steps, hist, rc, box.flow_get(populations=False)))
+        out[wide] = res
+    for (na, ra, ja), (nb, rb, jb) in zip(out["0"][:3], out["1"][:3]):
+        assert np.array_equal(na, nb) and np.array_equal(ra, rb)
+        for d in range(3):
+            assert np.array_equal(ja[d], jb[d])
+    (sa, ha, ca, (_, ra, ja)), (sb, hb, cb, (_, rb, jb)) = out["0"][3], out["1"][3]
+    assert sa == sb == 3001 and ca == cb != 0 and np.array_equal(ha, hb)
+    assert np.array_equal(ra, rb) and all(np.array_equal(ja[d], jb[d]) for d in range(3))
+
+
 @pytest.mark.parametrize("label,make", [(-1, lambda: geo.bulk(9, 9, 9)),
                                         (1, lambda: geo.slit(9, 7, 11))])
 def test_equilibration_compensated_force_bit_exact(oracle_mod, label, make):

@@ -9,6 +9,11 @@ seed 20261203; 4,245,990 fluid of 7,077,888 nodes), tau 0.8, f_ext (1e-6, 0, 0).
   number of steps (the in-place state is then in its swapped form).
 * FP32 mass conservation over 2000 steps: total mass within 1e-9 relative (the collision and the
   streaming conserve it exactly in exact arithmetic; the deviations keep the rounding small).
+
+And beyond 2^32 population slots: a cylinder (geometryLabel 2) in an 800 x 800 x 480 box,
+241 M fluid of 307 M nodes, 19 Nf = 4.6e9, where the in-place layout forms 64-bit slot offsets:
+its per-plane flux and density profiles along x, y and z equal the two-buffer layout's after an
+odd and an even number of steps (about 32 GB and 58 GB of device memory, one after the other).
 """
 import numpy as np
 import pytest
@@ -88,3 +93,25 @@ def test_fp32_mass_conservation_at_full_size(medium):
         _, rho, j = box.flow_get(populations=False)
     assert abs(rho.sum() - nf) <= 1e-9 * nf
     assert j[0].sum() > 0.0 and np.all(rho[medium == 1] == 0.0)
+
+
+def test_fp32_in_place_beyond_2_32_slots_equals_two_buffer(monkeypatch):
+    shape = (800, 800, 480)
+    out = {}
+    for mode in ("ab", "aa"):
+        monkeypatch.setenv("LBGPU_FP32_STREAMING", mode)
+        res = []
+        with Box.from_label(2, *shape, relaxation_time=TAU, f_ext=(0.0, 0.0, 1e-6),
+                            precision=FP32_DEV) as box:
+            nf = box.node_counts()["fluid"]
+            box.flow_init()
+            for k in (7, 5):   # 7 steps: swapped state; 12: natural order
+                box.flow_steps(k, force_on=True)
+                res.append([box.profiles(axis) for axis in range(3)])
+        out[mode] = (nf, res)
+    assert out["aa"][0] == out["ab"][0] and 19 * out["aa"][0] >= 2**32
+    for pa, pb in zip(out["ab"][1], out["aa"][1]):
+        for (fa, da), (fb, db) in zip(pa, pb):
+            assert np.array_equal(fa, fb) and np.array_equal(da, db)
+    flux_z = out["aa"][1][-1][2][0][:, 2]
+    assert np.all(flux_z > 0.0)
