@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_slab(const BatchInst *
     const int tile = t.start % nxy, chunk = t.start / nxy;
     const int z0 = chunk * I.zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    mp_slab_sweep<false, false>(I, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + I.zc, I.lz),
+    mp_slab_sweep(I, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + I.zc, I.lz),
                   sm4, vt);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     block_sum3(v);

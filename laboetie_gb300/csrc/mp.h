@@ -72,6 +72,7 @@ struct MpArgs32 {
     float ka, kd, one_minus_kd;
     float a1[3], lwh[3];
     int slab;                          // shared-memory slab step where the box allows it
+    unsigned slab_resident;            // slab blocks resident on the device at once
     // charged tracer: V.w holds the potential phi at every node; lambda*a0, tracer_z, 1/Pstat
     // and elec_slope for the per-link fermi factors (the grid-stride step is used)
     int charged;
@@ -80,15 +81,16 @@ struct MpArgs32 {
 
 // Shared-memory slab variant of the FP32 step (mp_f32.cu): 32 x 8 column tiles sweeping a chunk
 // of z planes.  Used when lx >= 32, ly >= 8 and lz >= 3.  Returns the grid (0: not eligible) and
-// the planes per block in *zc.
+// the planes per block in *zc.  A chunk reads two planes beyond its own, so the chunks are as long
+// as filling the device once allows (resident: blocks resident at once), and at least 8 planes.
 constexpr int MPS_TX = 32, MPS_TY = 8;
-inline unsigned mp32_slab_grid(int lx, int ly, int lz, int *zc)
+inline unsigned mp32_slab_grid(int lx, int ly, int lz, unsigned resident, int *zc)
 {
     if (lx < MPS_TX || ly < MPS_TY || lz < 3) return 0;
     const int nxy = ((lx + MPS_TX - 1) / MPS_TX) * ((ly + MPS_TY - 1) / MPS_TY);
-    int nz = 2432 / nxy;
+    int nz = (int)(resident / (unsigned)nxy);
+    if (nz > lz / 8) nz = lz / 8;
     if (nz < 1) nz = 1;
-    if (nz > lz) nz = lz;
     const int c = (lz + nz - 1) / nz;
     *zc = c;
     return (unsigned)(nxy * ((lz + c - 1) / c));
@@ -104,6 +106,8 @@ cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, const CUtensorM
 // tensor maps of a box's float4 field (V or P) for the slab step: dims (4 components, lx, ly, lz),
 // box (4, 34, 10, 1); false if the driver refuses them
 bool mp32_tensor_map(CUtensorMap *tm, const float4 *field, int lx, int ly, int lz);
+// blocks of the slab step resident on the current device at once (SMs x blocks per SM)
+unsigned mp32_slab_resident();
 cudaError_t launch_mp_init_f32(const MpArgs32 &a, float bw, unsigned grid, cudaStream_t s);
 
 }  // namespace lbg

@@ -201,7 +201,8 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
     a.pstat = Pstat;
     s->nblocks = (unsigned)((N + MP_BLOCK - 1) / MP_BLOCK);
     int zc = 0;
-    const unsigned slab = s->prec == LBGPU_FP64 ? 0u : mp32_slab_grid(a.lx, a.ly, a.lz, &zc);
+    const unsigned resident = s->prec == LBGPU_FP64 ? 0u : mp32_slab_resident();
+    const unsigned slab = s->prec == LBGPU_FP64 ? 0u : mp32_slab_grid(a.lx, a.ly, a.lz, resident, &zc);
     if ((rc = alloc_zero(ctx, s, &a.partial, 3 * (size_t)std::max(s->nblocks, slab)))) return rc;
     if ((rc = alloc_zero(ctx, s, &a.ctl, 1))) return rc;
 
@@ -238,6 +239,7 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
         // LBGPU_MP_SLAB=0: the grid-stride step everywhere (same per-node arithmetic)
         const char *slab_env = std::getenv("LBGPU_MP_SLAB");
         b.slab = !(slab_env && std::string(slab_env) == "0");
+        b.slab_resident = resident;
         b.ka = (float)tr->ka;
         b.kd = (float)tr->kd;
         b.one_minus_kd = (float)(1.0 - tr->kd);

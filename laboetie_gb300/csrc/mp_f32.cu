@@ -97,11 +97,12 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
         float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
         float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
         double dnet = 0.0;
+        // a step sums the links in mp_link_order (that of the slab step), the init in link order
         static_for<1, Q>([&](auto L) {
-            constexpr int l = decltype(L)::value;
+            constexpr int l = INIT ? decltype(L)::value : mp_link_order(decltype(L)::value);
             constexpr Vel c = vel(l);
             constexpr int w = wclass(l);
-            const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
+            const bool blocked = (m >> inv(l)) & 1u;  // r + c_l is solid
             const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
             const float4 vn = __ldg(V + rp);
             float lw_out = a.lwh[w], lw_in = a.lwh[w], emd = 1.0f;
@@ -111,11 +112,11 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                 const float fermi = 1.0f / (1.0f + e);
                 lw_out = a.lw[w] * fermi;
                 lw_in = a.lw[w] * (1.0f - fermi);
-                emd = on != 0.0f ? 1.0f / e : 0.0f;
+                emd = blocked ? 0.0f : 1.0f / e;
             }
-            const float spp = mp32_scatter(on, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), lw_in);
+            const float spp = mp32_scatter(blocked, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), lw_in);
             if constexpr (INIT) {
-                const float sp = mp32_scatter(on, a.a1[w], cdot<c.x, c.y, c.z>(vr), lw_out);
+                const float sp = mp32_scatter(blocked, a.a1[w], cdot<c.x, c.y, c.z>(vr), lw_out);
                 frac -= sp;
                 ux += c.x * sp;
                 uy += c.y * sp;
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
 // One tracer step of a box with V and P staged in shared memory (mp_slab.cuh): a block owns a
 // 32 x 8 column tile and a chunk of zc planes.  With use_tma, interior tiles stage their planes
 // by bulk tensor copies through the tensor maps of V and P[0], P[1] (kernel parameters).
-__global__ void __launch_bounds__(MP_BLOCK, 5)
+__global__ void __launch_bounds__(MP_BLOCK, 4)
     k_mp32_slab(const MpArgs32 a, int tiles_x, int tiles_y, int zc, const __grid_constant__ CUtensorMap tmV,
                 const __grid_constant__ CUtensorMap tmP0, const __grid_constant__ CUtensorMap tmP1, int use_tma)
 {
@@ -188,9 +189,8 @@ __global__ void __launch_bounds__(MP_BLOCK, 5)
     const int tile = (int)blockIdx.x % nxy, chunk = (int)blockIdx.x / nxy;
     const int z0 = chunk * zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    mp_slab_sweep<true, true>(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz),
-                        sm4, vt, use_tma ? &tmV : nullptr, use_tma ? (par ? &tmP1 : &tmP0) : nullptr,
-                        &a.ctl->status);
+    mp_slab_planes(a, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + zc, a.lz), sm4, vt,
+                   use_tma ? &tmV : nullptr, use_tma ? (par ? &tmP1 : &tmP0) : nullptr, &a.ctl->status);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     grid_sum3(v, a.partial, &a.ctl->blocks_done,
               [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });
@@ -246,10 +246,22 @@ bool mp32_tensor_map(CUtensorMap *tm, const float4 *field, int lx, int ly, int l
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+unsigned mp32_slab_resident()
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mp32_slab, MP_BLOCK, MPS_SMEM) != cudaSuccess) {
+        cudaGetLastError();
+        return 0u;
+    }
+    return (unsigned)(sms * per_sm);
+}
+
 cudaError_t launch_mp_step_f32(const MpArgs32 &a, unsigned grid, const CUtensorMap *tm, cudaStream_t s)
 {
     int zc = 0;
-    const unsigned sg = a.slab && !a.charged ? mp32_slab_grid(a.lx, a.ly, a.lz, &zc) : 0u;
+    const unsigned sg = a.slab && !a.charged ? mp32_slab_grid(a.lx, a.ly, a.lz, a.slab_resident, &zc) : 0u;
     if (sg) {
         const int tx = (a.lx + MPS_TX - 1) / MPS_TX, ty = (a.ly + MPS_TY - 1) / MPS_TY;
         CUtensorMap none;

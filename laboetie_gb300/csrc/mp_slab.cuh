@@ -1,16 +1,17 @@
 // mp_slab.cuh -- FP32 tracer step of a column tile with V and P staged in shared memory.
 //
-// The step of mp_f32.cu:k_mp32 (same operations in the same order, so P is bit-identical), for
-// the nodes (x0..x0+31, y0..y0+7, z0..z1-1) of a box with lx >= 32, ly >= 8, lz >= 3.  A ring
-// of 4 planes (z-1, z, z+1 and the one being fetched) of V and P with a one-node halo is filled
-// by asynchronous copies one plane ahead, so the neighbour reads are shared-memory reads and
-// every V and P value is fetched from L2/HBM about 1.3 times (halo) per step; the column's flag
-// word (and the node's fixed (u*, D)) is loaded into registers a plane ahead.  One block barrier
-// per plane: after it, plane z+1 is in shared memory and every thread is done with plane z-1, so
-// the fetch of plane z+2 may overwrite the slot of plane z-2.  The argument struct provides V,
-// P[2], A[2], mask, lx, ly, lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3] (and aux for the
-// difference form).
+// A block steps the nodes (x0..x0+31, y0..y0+7, z0..z1-1) of a box with lx >= 32, ly >= 8,
+// lz >= 3.  A ring of 4 planes of V and P with a one-node halo is filled by asynchronous copies
+// (or bulk tensor copies) ahead of use, so the neighbour reads are shared-memory reads and every
+// V and P value is fetched from L2/HBM about 1.3 times (halo) per step; the column's flag words
+// (and the node's fixed (u*, D)) are loaded into registers ahead of use.  One block barrier per
+// plane.  Two sweeps: mp_slab_planes, the difference form of mp_f32.cu:k_mp32 (same operations in
+// the same order, so P is bit-identical) visiting each plane once; mp_slab_sweep, the flux form
+// of the batched boxes, node by node.  The argument struct provides V, P[2], A[2], mask, lx, ly,
+// lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3] (and aux for the difference form).
 #pragma once
+
+#include <type_traits>
 
 #include "common.cuh"
 #include "cpasync.cuh"
@@ -28,11 +29,12 @@ constexpr unsigned MPS_TMA_BYTES = SPL * 16;                        // one plane
 // 4 planes of V and of P, 4 mbarriers, and slack to align the ring to 128 bytes
 constexpr size_t MPS_SMEM = 128 + sizeof(float4) * 8 * SPLP + 4 * sizeof(uint64_t);
 
-// Scattering probability of a link, on * (a1 (c.V) + lambda w / 2) (on = 0 across a
-// bounce-back link), rounded as written.
-__device__ __forceinline__ float mp32_scatter(float on, float a1, float cv, float lwh)
+// Scattering probability of a link, a1 (c.V) + lambda w / 2 rounded once, or 0 across a
+// bounce-back link (blocked).  The reference multiplies by a 0/1 factor instead; the sums it
+// enters are the same, as a product with -0 and with +0 adds nothing to a sum that is never -0.
+__device__ __forceinline__ float mp32_scatter(bool blocked, float a1, float cv, float lwh)
 {
-    return __fmul_rn(on, __fmaf_rn(a1, cv, lwh));
+    return blocked ? 0.0f : __fmaf_rn(a1, cv, lwh);
 }
 
 // One incoming link of an FP32 step: n += sp_in (P(r + c_l) - P(r)).
@@ -65,54 +67,22 @@ __device__ __forceinline__ float slab_cdot(const float4 &v)
     return s;
 }
 
-// Sweep of one tile: P(par) -> P(par^1) (and A) for its fluid nodes; vt += the nodes' VACF
-// terms (FP32, per thread).  sm: MPS_SMEM bytes of shared memory.  Every thread of the block
-// (MP_BLOCK = 256 = 32 x 8) must call it.  AUX: the difference form of mp_f32.cu:k_mp32 with the
-// node's fixed (u*, D) from a.aux (18 scatterings per node and step); otherwise the flux form
-// P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings).
-// TMA, with tmV / tmP the tensor maps of V and of P(par) (mp32_tensor_map; nullptr turns it off
-// at run time): a tile whose plane with its halo lies inside the box (no periodic wrap in x or y)
-// stages each plane with two bulk tensor copies issued by one thread and completed on the ring
-// slot's mbarrier, instead of 2 x 340 per-thread copies with wrap arithmetic; a wait that runs
-// out of its bound sets LBGPU_ERR_TIMEOUT in *status and the tile's nodes are left alone.
-// Without TMA none of that is compiled (the barriers, the 128-byte pad and the predicate cost a
-// caller 11 registers).
-template <bool AUX, bool TMA, typename Args>
+// Flux-form sweep of one tile (batched boxes): P(par) -> P(par^1) (and A) for its fluid nodes,
+// P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings per node); vt += the nodes'
+// VACF terms (FP32, per thread).  sm: MPS_SMEM bytes of shared memory.  Every thread of the block
+// (MP_BLOCK = 256 = 32 x 8) must call it.  Planes are staged by per-thread asynchronous copies.
+template <typename Args>
 __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, int y0, int z0, int z1,
-                                              float4 *sm_raw, float (&vt)[3],
-                                              const CUtensorMap *tmV = nullptr,
-                                              const CUtensorMap *tmP = nullptr,
-                                              unsigned *status = nullptr)
+                                              float4 *sm, float (&vt)[3])
 {
-    // align the ring to 128 bytes by offsetting the shared-memory pointer itself (rounding its
-    // generic address would hide from the compiler that it points to shared memory, and every
-    // ring read would become a generic load)
-    float4 *sm = TMA ? sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u : sm_raw;
     float4 *sV = sm, *sP = sm + 4 * SPLP;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 8 * SPLP);   // one per ring slot
     const int lx = a.lx, ly = a.ly, lz = a.lz;
     const float4 *__restrict__ Vg = a.V;
     const float4 *__restrict__ Pg = a.P[par];
-    const bool tma = TMA && tmV != nullptr && x0 >= 1 && x0 + MPS_TX + 1 <= lx && y0 >= 1 && y0 + MPS_TY + 1 <= ly;
-    if (tma) {
-        if (threadIdx.x == 0) {
-            for (int q = 0; q < 4; ++q) mbar_init(&bars[q], 1);
-            mbar_fence_init();
-        }
-        __syncthreads();
-    }
     auto load_plane = [&](int zz) {
         const int gz = zz < 0 ? zz + lz : (zz >= lz ? zz - lz : zz);
         const int slot = (zz - z0 + 1) & 3;
         float4 *dv = sV + slot * SPLP, *dp = sP + slot * SPLP;
-        if (tma) {
-            if (threadIdx.x == 0) {
-                mbar_arrive_expect_tx(&bars[slot], 2 * MPS_TMA_BYTES);
-                tma_load_4d(dv, tmV, 0, x0 - 1, y0 - 1, gz, &bars[slot]);
-                tma_load_4d(dp, tmP, 0, x0 - 1, y0 - 1, gz, &bars[slot]);
-            }
-            return;
-        }
         for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
             const int hx = k % SHX, hy = k / SHX;
             int gx = x0 + hx - 1, gy = y0 + hy - 1;
@@ -127,35 +97,21 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
     const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
     const int x = x0 + tx, y = y0 + ty;
     const bool col = x < lx && y < ly;
-    // the fill of plane zz is its slot's ((zz - z0 + 1) / 4)-th: the phase parity to wait for
-    auto wait_plane = [&](int zz) {
-        return mbar_wait(&bars[(zz - z0 + 1) & 3], (unsigned)(((zz - z0 + 1) >> 2) & 1));
-    };
     load_plane(z0 - 1);
     load_plane(z0);
     load_plane(z0 + 1);
-    bool ok = true;
-    if (tma) ok = wait_plane(z0 - 1) && wait_plane(z0);
-    // the column's flag word (and, AUX, fixed node data) of the next plane, loaded a plane ahead
-    // so that no plane starts on a global-memory round trip
+    // the column's flag word of the next plane, loaded a plane ahead so that no plane starts on a
+    // global-memory round trip
     const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
     uint32_t m_next = col ? __ldg(a.mask + col0 + plane * z0) : 0u;
-    float4 ax_next = make_float4(0.f, 0.f, 0.f, 0.f);
-    if constexpr (AUX)
-        if (col) ax_next = __ldg(a.aux + col0 + plane * z0);
     for (int z = z0; z < z1; ++z) {
-        if (!tma) cp_async_wait0();
-        else if (TMA && ok) ok = wait_plane(z + 1);
+        cp_async_wait0();
         __syncthreads();
         if (z + 2 <= z1) load_plane(z + 2);
         const size_t r = col0 + plane * z;
         const uint32_t m = m_next;
-        const float4 ax = ax_next;
-        if (col && z + 1 < z1) {
-            m_next = __ldg(a.mask + r + plane);
-            if constexpr (AUX) ax_next = __ldg(a.aux + r + plane);
-        }
-        if ((!TMA || ok) && (m & FLUID_BIT)) {
+        if (col && z + 1 < z1) m_next = __ldg(a.mask + r + plane);
+        if (m & FLUID_BIT) {
             const int c0 = (ty + 1) * SHX + (tx + 1);
             const int s0 = (z - z0 + 1) & 3;
             const float4 vr = sV[s0 * SPLP + c0];
@@ -170,33 +126,21 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
                 const int q = ((z + c.z - z0 + 1) & 3) * SPLP + c0 + c.y * SHX + c.x;
                 const float4 vn = sV[q];
                 const float4 pn = sP[q];
-                if constexpr (AUX) {
-                    mp32_link(mp32_scatter(on, a.a1[w], slab_cdot<-c.x, -c.y, -c.z>(vn), a.lwh[w]), pn, p,
-                              n0, n1, n2);
-                } else {
-                    const float sp = on * (a.a1[w] * slab_cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
-                    const float spp = on * (a.a1[w] * slab_cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
-                    ux += c.x * sp;
-                    uy += c.y * sp;
-                    uz += c.z * sp;
-                    n0 += pn.x * spp - p.x * sp;
-                    n1 += pn.y * spp - p.y * sp;
-                    n2 += pn.z * spp - p.z * sp;
-                }
+                const float sp = on * (a.a1[w] * slab_cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
+                const float spp = on * (a.a1[w] * slab_cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
+                ux += c.x * sp;
+                uy += c.y * sp;
+                uz += c.z * sp;
+                n0 += pn.x * spp - p.x * sp;
+                n1 += pn.y * spp - p.y * sp;
+                n2 += pn.z * spp - p.z * sp;
             });
-            if constexpr (AUX) {
-                vt[0] += p.x * ax.x;
-                vt[1] += p.y * ax.y;
-                vt[2] += p.z * ax.z;
-                mp32_finish(p, ax.w, n0, n1, n2);
-            } else {
-                vt[0] += p.x * ux;
-                vt[1] += p.y * uy;
-                vt[2] += p.z * uz;
-                n0 += p.x;
-                n1 += p.y;
-                n2 += p.z;
-            }
+            vt[0] += p.x * ux;
+            vt[1] += p.y * uy;
+            vt[2] += p.z * uz;
+            n0 += p.x;
+            n1 += p.y;
+            n2 += p.z;
             if (a.ads && (m & INTERFACIAL_BIT)) {
                 const float4 qa = a.A[par][r];
                 n0 += qa.x * a.kd - a.ka * p.x;
@@ -209,7 +153,232 @@ __device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, in
             __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
         }
     }
-    if (TMA && !ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
+}
+
+// Link of velocity (dx, dy, dz).
+__host__ __device__ constexpr int link_of(int dx, int dy, int dz)
+{
+    for (int l = 0; l < Q; ++l)
+        if (vel(l).x == dx && vel(l).y == dy && vel(l).z == dz) return l;
+    return -1;
+}
+
+// The nine points (dx, dy) of a column's neighbourhood in one plane, in the order the plane-wise
+// step visits them.  Restricted to the links of one z offset this is ascending link order.
+__host__ __device__ constexpr int pt_dx(int k) { return k == 1 || k == 5 || k == 7 ? 1 : (k == 2 || k == 6 || k == 8 ? -1 : 0); }
+__host__ __device__ constexpr int pt_dy(int k) { return k == 3 || k == 5 || k == 6 ? 1 : (k == 4 || k == 7 || k == 8 ? -1 : 0); }
+
+// The order in which a difference-form step sums a node's 18 incoming links (k = 1..18): the
+// links from the plane below (c.z = -1), from its own plane, then from the plane above, each
+// group in ascending link order.  Both FP32 tracer steps (mp_f32.cu) use it, so their P is
+// bit-identical.
+__host__ __device__ constexpr int mp_link_order(int k)
+{
+    int n = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int l = 1; l < Q; ++l)
+            if (vel(l).z == dz && ++n == k) return l;
+    return -1;
+}
+
+// visiting the nine points in order adds each node's links of one z offset in ascending order,
+// the offsets in the order -1, 0, +1: the sum order of mp_link_order
+__host__ __device__ constexpr bool plane_order_is_link_order()
+{
+    int k = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int p = 0; p < 9; ++p) {
+            const int l = link_of(pt_dx(p), pt_dy(p), dz);
+            if (l > 0 && l != mp_link_order(++k)) return false;
+        }
+    return k == Q - 1;
+}
+static_assert(plane_order_is_link_order(), "plane-wise visit order differs from mp_link_order");
+
+// Difference-form sweep of one tile (a box's FP32 step, mp_f32.cu:k_mp32's arithmetic in
+// mp_link_order): P(par) -> P(par^1) (and A) for its fluid nodes, P(r) + [sum_l sp_in(l)
+// (P(r+c_l) - P(r)) + D P(r)] with the node's fixed (u*, D) from a.aux; vt += the VACF terms.
+//
+// Plane-wise: each plane zz = z0-1 .. z1 is read once.  A thread reads the nine points
+// (x+dx, y+dy, zz) of its column's neighbourhood (V and P: 18 shared-memory reads instead of the
+// 37 a node-wise step makes) and adds each point's incoming links to the nodes of its column that
+// they reach: (dx, dy, -1) to node zz+1, (dx, dy, 0) to node zz, (dx, dy, +1) to node zz-1.  The
+// three nodes in flight keep their sums, P and flag words in registers; node zz-1 is complete
+// after plane zz and is written.  Ring of 4 plane slots: at step zz plane zz+1 has arrived (its
+// centre P enters the registers), and after the step's barrier the fetch of plane zz+3 reuses the
+// slot of plane zz-1, which no thread reads any more.
+// tmV / tmP (nullptr: per-thread copies everywhere): tensor maps of V and of P(par); a tile whose
+// plane with its halo lies inside the box (no periodic wrap in x or y) stages each plane with two
+// bulk tensor copies issued by one thread and completed on the ring slot's mbarrier; a wait that
+// runs out of its bound sets LBGPU_ERR_TIMEOUT in *status and the tile's nodes are left alone.
+template <typename Args>
+__device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, int y0, int z0, int z1,
+                                               float4 *sm_raw, float (&vt)[3], const CUtensorMap *tmV,
+                                               const CUtensorMap *tmP, unsigned *status)
+{
+    // align the ring to 128 bytes by offsetting the shared-memory pointer itself (rounding its
+    // generic address would hide from the compiler that it points to shared memory, and every
+    // ring read would become a generic load)
+    float4 *sm = sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u;
+    float4 *sV = sm, *sP = sm + 4 * SPLP;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 8 * SPLP);   // one per ring slot
+    const int lx = a.lx, ly = a.ly, lz = a.lz;
+    const float4 *__restrict__ Vg = a.V;
+    const float4 *__restrict__ Pg = a.P[par];
+    const bool tma = tmV != nullptr && x0 >= 1 && x0 + MPS_TX + 1 <= lx && y0 >= 1 && y0 + MPS_TY + 1 <= ly;
+    if (tma) {
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < 4; ++q) mbar_init(&bars[q], 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+    }
+    auto slot = [&](int zz) { return (zz - z0 + 1) & 3; };
+    // plane zz (<= z1) into its slot; per-thread copies commit one group per call (an empty one
+    // past z1), so that "plane zz+1 arrived" is always "all but the latest group complete"
+    auto load_plane = [&](int zz) {
+        if (zz <= z1) {
+            const int gz = zz < 0 ? zz + lz : (zz >= lz ? zz - lz : zz);
+            float4 *dv = sV + slot(zz) * SPLP, *dp = sP + slot(zz) * SPLP;
+            if (tma) {
+                if (threadIdx.x == 0) {
+                    mbar_arrive_expect_tx(&bars[slot(zz)], 2 * MPS_TMA_BYTES);
+                    tma_load_4d(dv, tmV, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
+                    tma_load_4d(dp, tmP, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
+                }
+            } else {
+                for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
+                    const int hx = k % SHX, hy = k / SHX;
+                    int gx = x0 + hx - 1, gy = y0 + hy - 1;
+                    gx = gx < 0 ? gx + lx : (gx >= lx ? gx - lx : gx);   // lx >= 32: one wrap at most
+                    gy = gy < 0 ? gy + ly : (gy >= ly ? gy - ly : gy);   // ly >= 8
+                    const size_t idx = (size_t)gx + (size_t)lx * ((size_t)gy + (size_t)ly * gz);
+                    cp_async16(dv + k, Vg + idx);
+                    cp_async16(dp + k, Pg + idx);
+                }
+            }
+        }
+        if (!tma) cp_async_commit();
+    };
+    // plane zz has arrived (this thread's view; the barrier that follows makes it everyone's); the
+    // fill of plane zz is its slot's ((zz - z0 + 1) / 4)-th: the phase parity to wait for
+    auto wait_plane = [&](int zz) {
+        if (!tma) {
+            cp_async_wait1();
+            return true;
+        }
+        return mbar_wait(&bars[slot(zz)], (unsigned)(((zz - z0 + 1) >> 2) & 1));
+    };
+    const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool col = x < lx && y < ly;
+    const int c0 = (ty + 1) * SHX + (tx + 1);
+    const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
+    // flag word of the column's node z; 0 (no fluid bit, no work) outside the tile's nodes
+    auto mask_at = [&](int z) { return (col && z >= z0 && z < z1) ? __ldg(a.mask + col0 + plane * z) : 0u; };
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool ok = true;   // false once a wait for a bulk copy ran out
+    // a node of the column in flight: P (also the centre point of its plane for the links of
+    // the nodes above and below), running sum, flag word, fixed (u*, D)
+    struct Node {
+        float4 p, n, ax;
+        uint32_t m;
+    };
+    Node S0, S1, S2;
+    S0.m = S1.m = S2.m = 0u;
+    S0.p = S1.p = S2.p = zero;
+    S0.n = S1.n = S2.n = zero;
+    S0.ax = S1.ax = S2.ax = zero;
+    uint32_t m_next = mask_at(z0);   // flag word of node zz+1 at the start of step zz
+    // Step zz with A = node zz-1, B = node zz, C = node zz+1 (DA, DB, DC: which of them can be
+    // nodes of the tile: the first step zz = z0-1 has only C, the last zz = z1 only A, and each
+    // computes only their links).
+    auto step = [&](auto DA, auto DB, auto DC, Node &A, Node &B, Node &C, int zz) {
+        constexpr bool da = decltype(DA)::value, db = decltype(DB)::value, dc = decltype(DC)::value;
+        if (dc && ok) ok = wait_plane(zz + 1);
+        __syncthreads();
+        load_plane(zz + 3);
+        if constexpr (dc) {   // node zz+1 enters; its centre P is the next step's centre point
+            C.m = m_next;
+            m_next = mask_at(zz + 2);
+            C.p = (ok && col) ? sP[slot(zz + 1) * SPLP + c0] : zero;
+            C.n = zero;
+        }
+        if constexpr (db)
+            if (B.m & FLUID_BIT) B.ax = __ldg(a.aux + col0 + plane * zz);   // used at step zz+1
+        const uint32_t any = (da ? A.m : 0u) | (db ? B.m : 0u) | (dc ? C.m : 0u);
+        if (ok && (any & FLUID_BIT)) {
+            const int s0 = slot(zz) * SPLP + c0;
+            static_for<0, 9>([&](auto K) {
+                constexpr int k = decltype(K)::value;
+                constexpr int dx = pt_dx(k), dy = pt_dy(k);
+                constexpr bool axis = dx * dx + dy * dy <= 1;   // links (dx, dy, -1) and (dx, dy, +1)
+                if constexpr ((dc && axis) || (db && (dx != 0 || dy != 0)) || (da && axis)) {
+                    const float4 vn = sV[s0 + dy * SHX + dx];
+                    float4 pn;
+                    if constexpr (dx == 0 && dy == 0) pn = B.p;
+                    else pn = sP[s0 + dy * SHX + dx];
+                    if constexpr (dc && axis) {   // link (dx, dy, -1) of node zz+1
+                        constexpr int l = link_of(dx, dy, -1);
+                        constexpr int w = wclass(l);
+                        mp32_link(mp32_scatter((C.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, 1>(vn), a.lwh[w]),
+                                  pn, C.p, C.n.x, C.n.y, C.n.z);
+                    }
+                    if constexpr (db && (dx != 0 || dy != 0)) {   // link (dx, dy, 0) of node zz
+                        constexpr int l = link_of(dx, dy, 0);
+                        constexpr int w = wclass(l);
+                        mp32_link(mp32_scatter((B.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, 0>(vn), a.lwh[w]),
+                                  pn, B.p, B.n.x, B.n.y, B.n.z);
+                    }
+                    if constexpr (da && axis) {   // link (dx, dy, +1) of node zz-1
+                        constexpr int l = link_of(dx, dy, 1);
+                        constexpr int w = wclass(l);
+                        mp32_link(mp32_scatter((A.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, -1>(vn), a.lwh[w]),
+                                  pn, A.p, A.n.x, A.n.y, A.n.z);
+                    }
+                }
+            });
+        }
+        if constexpr (da) {
+            if (ok && (A.m & FLUID_BIT)) {   // node zz-1 has all its links
+                const size_t r = col0 + plane * (zz - 1);
+                float4 n = A.n;
+                const float4 p = A.p, ax = A.ax;
+                vt[0] += p.x * ax.x;
+                vt[1] += p.y * ax.y;
+                vt[2] += p.z * ax.z;
+                mp32_finish(p, ax.w, n.x, n.y, n.z);
+                if (a.ads && (A.m & INTERFACIAL_BIT)) {
+                    const float4 qa = a.A[par][r];
+                    n.x += qa.x * a.kd - a.ka * p.x;
+                    n.y += qa.y * a.kd - a.ka * p.y;
+                    n.z += qa.z * a.kd - a.ka * p.z;
+                    a.A[par ^ 1][r] = make_float4(qa.x * a.one_minus_kd + p.x * a.ka,
+                                                  qa.y * a.one_minus_kd + p.y * a.ka,
+                                                  qa.z * a.one_minus_kd + p.z * a.ka, 0.0f);
+                }
+                __stcs(a.P[par ^ 1] + r, make_float4(n.x, n.y, n.z, 0.0f));
+            }
+        }
+    };
+    using T = std::true_type;
+    using F = std::false_type;
+    load_plane(z0 - 1);
+    load_plane(z0);
+    ok = wait_plane(z0 - 1);
+    load_plane(z0 + 1);
+    __syncthreads();
+    S0.p = (ok && col) ? sP[slot(z0 - 1) * SPLP + c0] : zero;   // centre P of plane z0-1
+    // S0, S1, S2 = nodes zz-1, zz, zz+1 at step zz (a loop unrolled by three to rotate the slots
+    // instead costs more in instruction fetch than the register moves it saves)
+    step(F{}, F{}, T{}, S2, S0, S1, z0 - 1);
+    for (int zz = z0; zz < z1; ++zz) {
+        step(T{}, T{}, T{}, S0, S1, S2, zz);
+        S0 = S1;
+        S1 = S2;
+    }
+    step(T{}, F{}, F{}, S0, S1, S2, z1);   // the last node's links from plane z1
+    if (!ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
 }
 
 }  // namespace lbg

@@ -165,9 +165,10 @@ def test_fp32_slab_bulk_tensor_copies_equal_per_thread_copies(monkeypatch):
     """The slab step stages interior tiles by bulk tensor copies (TMA) and edge tiles (periodic
     wrap) by per-thread copies; with LBGPU_MP_TMA=0 every tile uses per-thread copies and with
     LBGPU_MP_SLAB=0 the grid-stride kernel runs: P and P_ads bit-identical in all three.  100 x 40
-    x 12 has interior tiles in x (x0 = 32) and y (y0 = 8 .. 24) beside edge tiles."""
+    x 43 has interior tiles in x (x0 = 32) and y (y0 = 8 .. 24) beside edge tiles, and z chunks of
+    9, 9, 9, 9 and 7 planes (the first and the last reading across the periodic z boundary)."""
     rng = np.random.default_rng(11)
-    nat = (rng.random((12, 40, 100)) < 0.3).astype(np.int8)
+    nat = (rng.random((43, 40, 100)) < 0.3).astype(np.int8)
     rho = np.where(nat == 0, 1.0 + 1e-3 * rng.standard_normal(nat.shape), 0.0)
     j = [np.where(nat == 0, 1e-3 * rng.standard_normal(nat.shape), 0.0) for _ in range(3)]
     out = {}
