@@ -311,6 +311,9 @@ int lbgpu_batch_mp_start(lbgpu_batch *b, int id);
  * per-tile FP64 partials); D_eff = vacf0/2 + vacf_sum (Green-Kubo, unit time step). */
 int lbgpu_batch_mp_get(lbgpu_batch *b, int id, double vacf0[3], double vacf_sum[3],
                        double vacf_last[3], int *steps);
+/* Current P(3,lx,ly,lz) and adsorbed part (zeros when no adsorption) of a box in its tracer
+ * phase, as lbgpu_mp_get; either may be NULL. */
+int lbgpu_batch_mp_fields(lbgpu_batch *b, int id, double *P, double *P_ads);
 int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *smem_boxes,
                      size_t *bytes_used);
 

@@ -128,13 +128,16 @@ __device__ __forceinline__ float cdot(const float4 &v)
     return s;
 }
 
-// One tracer step at fluid node r, flux form of mp_f32.cu (module_moment_propagation.f90:207-253);
-// with INIT, P(t=1) and the node's VACF(0) term instead (module_moment_propagation.f90:112-136).
-// vt receives the node's VACF term (before the 1/Pstat factor for INIT).
+// One tracer step at fluid node r in the difference form of mp_f32.cu:k_mp32, with the same
+// operations in the same order (mp_slab.cuh helpers, mp_link_order), so a batched box's P is
+// bit-identical to a single box's; with INIT, P(t=1), the node's fixed (u*, D) in aux and its
+// VACF(0) term (before the 1/Pstat factor) instead (module_moment_propagation.f90:112-136).
+// vt receives the node's VACF term in FP32 (a thread's few nodes; FP64 across threads, as the
+// single box sums them).
 template <bool INIT>
 __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float4 *Pnext,
-                                        const float4 *An, float4 *Anext, unsigned r, int x, int y,
-                                        int z, uint32_t m, const BatchInst &I, double (&vt)[3],
+                                        const float4 *An, float4 *Anext, float4 *aux, unsigned r, int x,
+                                        int y, int z, uint32_t m, const BatchInst &I, float (&vt)[3],
                                         unsigned &bad)
 {
     const int lx = I.lx, ly = I.ly, lz = I.lz;
@@ -143,26 +146,31 @@ __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float
     const int X[3] = {wrap_minus(x, lx), x, wrap_plus(x, lx)};
     const int Y[3] = {wrap_minus(y, ly) * sy, y * sy, wrap_plus(y, ly) * sy};
     const int Z[3] = {wrap_minus(z, lz) * sz, z * sz, wrap_plus(z, lz) * sz};
-    const float4 vr = V[r];
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if constexpr (!INIT) p = Pn[r];
+    float4 vr = make_float4(0.f, 0.f, 0.f, 0.f), p = vr, ax = vr;
+    if constexpr (INIT) {
+        vr = V[r];
+    } else {
+        p = Pn[r];
+        ax = __ldg(aux + r);   // issued before the links, so that its latency overlaps them
+    }
     float frac = 1.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
     float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
     float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+    double dnet = 0.0;
     static_for<1, Q>([&](auto L) {
-        constexpr int l = decltype(L)::value;
+        constexpr int l = INIT ? decltype(L)::value : mp_link_order(decltype(L)::value);
         constexpr Vel c = vel(l);
         constexpr int w = wclass(l);
-        const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
+        const bool blocked = (m >> inv(l)) & 1u;  // r + c_l is solid
         const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
-        const float4 vn = V[rp];
-        const float sp = on * (I.a1[w] * cdot<c.x, c.y, c.z>(vr) + I.lwh[w]);
-        const float spp = on * (I.a1[w] * cdot<-c.x, -c.y, -c.z>(vn) + I.lwh[w]);
-        frac -= sp;
-        ux += c.x * sp;
-        uy += c.y * sp;
-        uz += c.z * sp;
+        const float spp = mp32_scatter(blocked, I.a1[w], cdot<-c.x, -c.y, -c.z>(V[rp]), I.lwh[w]);
         if constexpr (INIT) {
+            const float sp = mp32_scatter(blocked, I.a1[w], cdot<c.x, c.y, c.z>(vr), I.lwh[w]);
+            frac -= sp;
+            ux += c.x * sp;
+            uy += c.y * sp;
+            uz += c.z * sp;
+            dnet += (double)spp - (double)sp;
             v0 += c.x * c.x * sp;
             v1 += c.y * c.y * sp;
             v2 += c.z * c.z * sp;
@@ -170,34 +178,23 @@ __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float
             n1 -= c.y * spp;
             n2 -= c.z * spp;
         } else {
-            const float4 pn = Pn[rp];
-            n0 += pn.x * spp - p.x * sp;
-            n1 += pn.y * spp - p.y * sp;
-            n2 += pn.z * spp - p.z * sp;
+            mp32_link(spp, Pn[rp], p, n0, n1, n2);
         }
     });
     if constexpr (INIT) {
         Pnext[r] = make_float4(n0 * I.bw, n1 * I.bw, n2 * I.bw, 0.0f);
-        vt[0] += (double)v0;
-        vt[1] += (double)v1;
-        vt[2] += (double)v2;
+        aux[r] = make_float4(ux, uy, uz, (float)dnet);
+        vt[0] += v0;
+        vt[1] += v1;
+        vt[2] += v2;
         const float fr = (I.ads && (m & INTERFACIAL_BIT)) ? frac - I.ka : frac;
         if (fr < 1.1920929e-07f) bad = 1u;
     } else {
-        vt[0] += (double)(p.x * ux);
-        vt[1] += (double)(p.y * uy);
-        vt[2] += (double)(p.z * uz);
-        n0 += p.x;
-        n1 += p.y;
-        n2 += p.z;
-        if (I.ads && (m & INTERFACIAL_BIT)) {
-            const float4 q = An[r];
-            n0 += q.x * I.kd - I.ka * p.x;
-            n1 += q.y * I.kd - I.ka * p.y;
-            n2 += q.z * I.kd - I.ka * p.z;
-            Anext[r] = make_float4(q.x * I.one_minus_kd + p.x * I.ka, q.y * I.one_minus_kd + p.y * I.ka,
-                                   q.z * I.one_minus_kd + p.z * I.ka, 0.0f);
-        }
+        vt[0] += p.x * ax.x;
+        vt[1] += p.y * ax.y;
+        vt[2] += p.z * ax.z;
+        mp32_finish(p, ax.w, n0, n1, n2);
+        if (I.ads && (m & INTERFACIAL_BIT)) Anext[r] = mp32_adsorb(p, An[r], I.ka, I.kd, I.one_minus_kd, n0, n1, n2);
         Pnext[r] = make_float4(n0, n1, n2, 0.0f);
     }
 }
@@ -362,7 +359,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
     else t = tiles[blockIdx.x];
     const BatchInst &I = insts[t.inst];
     const unsigned k = (unsigned)t.start + threadIdx.x;   // node in the box's layout
-    double vt[3] = {0.0, 0.0, 0.0};
+    float vt32[3] = {0.0f, 0.0f, 0.0f};
     unsigned bad = 0;
     if (k < batch_units(I)) {
         uint32_t m;
@@ -377,10 +374,11 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
             lattice_xyz(I, r, x, y, z);
         }
         if (m & FLUID_BIT) {
-            if constexpr (INIT) mp_node<true>(I.V, nullptr, I.P[0], nullptr, nullptr, r, x, y, z, m, I, vt, bad);
-            else mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], r, x, y, z, m, I, vt, bad);
+            if constexpr (INIT) mp_node<true>(I.V, nullptr, I.P[0], nullptr, nullptr, I.aux, r, x, y, z, m, I, vt32, bad);
+            else mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], I.aux, r, x, y, z, m, I, vt32, bad);
         }
     }
+    double vt[3] = {(double)vt32[0], (double)vt32[1], (double)vt32[2]};
     block_sum3(vt);
     if (threadIdx.x == 0) {
         double *acc = I.tacc + (size_t)(t.start / BATCH_BLOCK) * BATCH_TACC;
@@ -404,7 +402,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
 
 // One tracer step of the slab tiles of boxes in the tracer phase (mp_slab.cuh); each tile keeps
 // its own running sums.
-__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_slab(const BatchInst *__restrict__ insts,
+__global__ void __launch_bounds__(BATCH_BLOCK, 4) k_batch_mp_slab(const BatchInst *__restrict__ insts,
                                                                const BatchTile *__restrict__ tiles, int par)
 {
     extern __shared__ float4 sm4[];
@@ -415,8 +413,8 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_slab(const BatchInst *
     const int tile = t.start % nxy, chunk = t.start / nxy;
     const int z0 = chunk * I.zc;
     float vt[3] = {0.0f, 0.0f, 0.0f};
-    mp_slab_sweep(I, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + I.zc, I.lz),
-                  sm4, vt);
+    mp_slab_planes(I, par, (tile % tiles_x) * MPS_TX, (tile / tiles_x) * MPS_TY, z0, min(z0 + I.zc, I.lz), sm4,
+                   vt, nullptr, nullptr, nullptr);
     double v[3] = {(double)vt[0], (double)vt[1], (double)vt[2]};
     block_sum3(v);
     if (threadIdx.x == 0) {
@@ -447,21 +445,23 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_v(const BatchInst *__r
     I.V[r] = make_float4(o[0], o[1], o[2], 0.0f);
 }
 
-// One block per small box, for all the steps of a call: load, nsteps steps of the box's phase
-// in shared memory, optional convergence check (flow), store.  nsteps is even, so a flow box
-// ends in natural order and a tracer box with P(now) in P[0].
+// One block per small box in the flow phase, for all the steps of a call: load, nsteps steps in
+// shared memory, optional convergence check, store.  nsteps is even, so a box ends in natural
+// order.  (The tracer phase is a kernel of its own, so that neither phase's register allocation
+// is set by the other's code.  A box's shared memory keeps one block per SM, so both kernels are
+// bounded for one resident block: the compiler may then use up to 128 registers for 512 threads,
+// which lets it issue more of a node's shared-memory reads ahead.)
 template <int MAXT>
-__global__ void __launch_bounds__(MAXT) k_batch_smem(const BatchInst *__restrict__ insts,
-                                                                   const int *__restrict__ list,
-                                                                   int nsteps, int check,
-                                                                   unsigned *du_out)
+__global__ void __launch_bounds__(MAXT, 1) k_batch_smem_flow(const BatchInst *__restrict__ insts,
+                                                          const int *__restrict__ list, int nsteps,
+                                                          int check, unsigned *du_out)
 {
     extern __shared__ float4 sm4[];
     const int id = list[blockIdx.x];
     const BatchInst &I = insts[id];
     const unsigned N = (unsigned)I.N;
     const unsigned T = blockDim.x;
-    if (I.phase == BATCH_FLOW) {
+    {
         float *g = reinterpret_cast<float *>(sm4);
         uint32_t *msk = reinterpret_cast<uint32_t *>(g + (size_t)Q * N);
         for (unsigned i = threadIdx.x; i < (unsigned)Q * N; i += T) g[i] = I.g[i];
@@ -485,9 +485,22 @@ __global__ void __launch_bounds__(MAXT) k_batch_smem(const BatchInst *__restrict
             if ((threadIdx.x & 31) == 0) atomicMax(du_out + id, du);
         }
         for (unsigned i = threadIdx.x; i < (unsigned)Q * N; i += T) I.g[i] = g[i];
-        return;
     }
-    // tracer phase
+}
+
+// One block per small box in the tracer phase, for all the steps of a call: load V, P (and A)
+// into shared memory, nsteps steps, store; nsteps is even, so P(now) ends in P[0].  The fixed
+// (u*, D) of the nodes stay in global memory (read once per node and step, from L2), which keeps
+// a 1 x 50 x 50 cell with adsorption within shared memory.
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) k_batch_smem_mp(const BatchInst *__restrict__ insts,
+                                                        const int *__restrict__ list, int nsteps)
+{
+    extern __shared__ float4 sm4[];
+    const int id = list[blockIdx.x];
+    const BatchInst &I = insts[id];
+    const unsigned N = (unsigned)I.N;
+    const unsigned T = blockDim.x;
     const int ads = I.ads;
     float4 *V = sm4, *P0 = sm4 + N, *P1 = sm4 + 2 * (size_t)N;
     float4 *A0 = ads ? sm4 + 3 * (size_t)N : nullptr, *A1 = ads ? sm4 + 4 * (size_t)N : nullptr;
@@ -510,12 +523,13 @@ __global__ void __launch_bounds__(MAXT) k_batch_smem(const BatchInst *__restrict
         const bool odd = s & 1;
         const float4 *Pn = odd ? P1 : P0, *An = odd ? A1 : A0;
         float4 *Px = odd ? P0 : P1, *Ax = odd ? A0 : A1;
-        double vt[3] = {0.0, 0.0, 0.0};
+        float vt32[3] = {0.0f, 0.0f, 0.0f};
         NodeWalk w(I, T);
         for (unsigned node = threadIdx.x; node < N; node += T, w.next()) {
             const uint32_t m = msk[node];
-            if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, node, w.x, w.y, w.z, m, I, vt, bad);
+            if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, I.aux, node, w.x, w.y, w.z, m, I, vt32, bad);
         }
+        double vt[3] = {(double)vt32[0], (double)vt32[1], (double)vt32[2]};
         block_sum3(vt);  // its barriers also separate this step from the next
         if (threadIdx.x == 0)
             for (int d = 0; d < 3; ++d) {
@@ -573,9 +587,13 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_moments(const BatchInst *
 
 cudaError_t batch_configure(int max_smem_bytes)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_batch_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_batch_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
+    const void *k[4] = {(const void *)k_batch_smem_flow<512>, (const void *)k_batch_smem_flow<1024>,
+                        (const void *)k_batch_smem_mp<512>, (const void *)k_batch_smem_mp<1024>};
+    for (const void *f : k) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 template <int MINB>
@@ -620,13 +638,20 @@ cudaError_t launch_batch_mp_start(const BatchInst *insts, int inst, unsigned uni
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist, int nsteps,
-                              bool check, unsigned *du, int smem_bytes, int threads, cudaStream_t s)
+cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nflow, int nmp, int nsteps,
+                              bool check, unsigned *du, int bytes_flow, int bytes_mp, int threads,
+                              cudaStream_t s)
 {
-    if (nlist <= 0) return cudaSuccess;
-    // up to 512 threads: the variant with up to 128 registers per thread; 1024: at most 64
-    if (threads <= 512) k_batch_smem<512><<<nlist, threads, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
-    else k_batch_smem<1024><<<nlist, 1024, smem_bytes, s>>>(insts, list, nsteps, check ? 1 : 0, du);
+    // up to 512 threads: the variants with up to 128 registers per thread; 1024: at most 64
+    const int c = check ? 1 : 0;
+    if (nflow > 0) {
+        if (threads <= 512) k_batch_smem_flow<512><<<nflow, threads, bytes_flow, s>>>(insts, list, nsteps, c, du);
+        else k_batch_smem_flow<1024><<<nflow, 1024, bytes_flow, s>>>(insts, list, nsteps, c, du);
+    }
+    if (nmp > 0) {
+        if (threads <= 512) k_batch_smem_mp<512><<<nmp, threads, bytes_mp, s>>>(insts, list + nflow, nsteps);
+        else k_batch_smem_mp<1024><<<nmp, 1024, bytes_mp, s>>>(insts, list + nflow, nsteps);
+    }
     return cudaGetLastError();
 }
 

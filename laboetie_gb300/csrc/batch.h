@@ -31,6 +31,7 @@ struct BatchInst {
     float4 *uprev;          // velocity at the previous convergence check
     float4 *V;              // tracer phase: (j + f_ext)/rho per node (0 on solid nodes)
     float4 *P[2], *A[2];    // propagated quantity / adsorbed part, by step parity
+    float4 *aux;            // per fluid node, fixed for the tracer phase: (u*, D) of mp_f32.cu
     double *tacc;           // BATCH_TACC doubles per tile of BATCH_BLOCK nodes, then a status word
     int lx, ly, lz, N;
     int phase, ads;
@@ -80,9 +81,11 @@ __host__ __device__ inline int batch_slab_tiles(int lx, int ly, int lz)
     if (lx < 32 || ly < 8 || lz < 3) return 0;
     return ((lx + 31) / 32) * ((ly + 7) / 8) * ((lz + BATCH_SLAB_ZC - 1) / BATCH_SLAB_ZC);
 }
-// du: one word per descriptor, max |u - u_prev| of the check as IEEE bits (non-negative)
-cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nlist, int nsteps,
-                              bool check, unsigned *du, int smem_bytes, int threads,
+// Shared-memory boxes: list holds nflow boxes in the flow phase, then nmp in the tracer phase,
+// each group with its own dynamic shared memory size.  du: one word per descriptor, max
+// |u - u_prev| of the flow check as IEEE bits (non-negative).
+cudaError_t launch_batch_smem(const BatchInst *insts, const int *list, int nflow, int nmp, int nsteps,
+                              bool check, unsigned *du, int bytes_flow, int bytes_mp, int threads,
                               cudaStream_t s);
 cudaError_t launch_batch_check(const BatchInst *insts, const BatchTile *tiles, int ntiles,
                                unsigned *du, cudaStream_t s);

@@ -63,9 +63,9 @@ bool tracer_ads(const lbgpu_tracer &t)
 // Byte layout of a slot's allocation: populations (g, over `units` nodes: lattice nodes, or
 // fluid nodes in the compact layout), lattice flags, previous velocity per unit, nature, the
 // compact tables (positions, flags, row table of `tab` entries) and the tracer buffers
-// (lattice-ordered V, P, A and per-tile VACF accumulators).
+// (lattice-ordered V, P, A, the fixed (u*, D) and per-tile VACF accumulators).
 struct Layout {
-    size_t g, mask, uprev, nature, cpos, cmask, rowtab, V, P0, P1, A0, A1, tacc, total;
+    size_t g, mask, uprev, nature, cpos, cmask, rowtab, V, P0, P1, A0, A1, aux, tacc, total;
 };
 
 Layout layout(long long N, long long units, long long tab, long long ntacc, bool compact, bool tracer,
@@ -91,6 +91,7 @@ Layout layout(long long N, long long units, long long tab, long long ntacc, bool
             L.A0 = o; o += f4;
             L.A1 = o; o += f4;
         }
+        L.aux = o; o += f4;
         L.tacc = o; o += up(sizeof(double) * ((size_t)ntacc * BATCH_TACC + 1));
     }
     L.total = o;
@@ -123,7 +124,9 @@ struct lbgpu_batch {
     BatchTile *d_tiles = nullptr;   // flow tiles, then tracer tiles, then tracer slab tiles
     int cap_tiles = 0, nflow = 0, nmp = 0, nslab = 0;
     int *d_smem = nullptr;
-    int cap_smem = 0, nsmem = 0, smem_bytes = 0, smem_threads = BATCH_SMEM_THREADS;
+    // shared-memory boxes: the flow-phase ones first (nsmem_flow), each phase with its bytes
+    int cap_smem = 0, nsmem = 0, nsmem_flow = 0, smem_bytes_flow = 0, smem_bytes_mp = 0;
+    int smem_threads = BATCH_SMEM_THREADS;
     unsigned *d_du = nullptr;
     int cap_du = 0;
     int aa_minb[2] = {4, 5};      // resident blocks per SM of the even / odd AA launches
@@ -204,9 +207,9 @@ int rebuild(lbgpu_batch *b)
     drop_graphs(b);
     std::vector<BatchInst> descs;
     std::vector<BatchTile> flow, mp, slab;
-    std::vector<int> smem;
+    std::vector<int> smem, smem_mp;
     b->desc_slot.clear();
-    int smem_bytes = 0;
+    int bytes_flow = 0, bytes_mp = 0;
     for (size_t k = 0; k < b->slots.size(); ++k) {
         const Slot &sl = b->slots[k];
         if (!sl.active) continue;
@@ -214,9 +217,13 @@ int rebuild(lbgpu_batch *b)
         descs.push_back(sl.d);
         b->desc_slot.push_back((int)k);
         if (sl.smem) {
-            smem.push_back(id);
-            smem_bytes = std::max(smem_bytes, sl.d.phase == BATCH_FLOW ? batch_smem_flow(sl.d.N)
-                                                                       : batch_smem_mp(sl.d.N, sl.d.ads));
+            if (sl.d.phase == BATCH_FLOW) {
+                smem.push_back(id);
+                bytes_flow = std::max(bytes_flow, batch_smem_flow(sl.d.N));
+            } else {
+                smem_mp.push_back(id);
+                bytes_mp = std::max(bytes_mp, batch_smem_mp(sl.d.N, sl.d.ads));
+            }
         } else if (sl.d.phase == BATCH_MP && sl.d.zc > 0) {
             const int n = batch_slab_tiles(sl.d.lx, sl.d.ly, sl.d.lz);
             for (int k = 0; k < n; ++k) slab.push_back({id, k});
@@ -226,6 +233,8 @@ int rebuild(lbgpu_batch *b)
             for (int st = 0; st < units; st += BATCH_BLOCK) list.push_back({id, st});
         }
     }
+    const int nsmem_flow = (int)smem.size();
+    smem.insert(smem.end(), smem_mp.begin(), smem_mp.end());
     std::vector<BatchTile> tiles(flow);
     tiles.insert(tiles.end(), mp.begin(), mp.end());
     tiles.insert(tiles.end(), slab.begin(), slab.end());
@@ -245,7 +254,9 @@ int rebuild(lbgpu_batch *b)
     b->nmp = (int)mp.size();
     b->nslab = (int)slab.size();
     b->nsmem = (int)smem.size();
-    b->smem_bytes = smem_bytes;
+    b->nsmem_flow = nsmem_flow;
+    b->smem_bytes_flow = bytes_flow;
+    b->smem_bytes_mp = bytes_mp;
     b->dirty = false;
     return LBGPU_OK;
 }
@@ -259,8 +270,8 @@ int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
     if (b->nsmem) {
         LBB_CK(cudaEventRecord(b->fork, s));
         LBB_CK(cudaStreamWaitEvent(b->side, b->fork, 0));
-        LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem, nsteps, check, b->d_du, b->smem_bytes,
-                                 b->smem_threads, b->side));
+        LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem_flow, b->nsmem - b->nsmem_flow, nsteps, check,
+                                 b->d_du, b->smem_bytes_flow, b->smem_bytes_mp, b->smem_threads, b->side));
         LBB_CK(cudaEventRecord(b->join, b->side));
     }
     for (int t = 0; t < nsteps; ++t) {
@@ -415,9 +426,11 @@ int tune_smem(lbgpu_batch *b)
     float best[2] = {1e30f, 1e30f};
     for (int rep = 0; rep < 2; ++rep)
         for (int k = 0; k < 2; ++k) {
-            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 2, false, nullptr, b->smem_bytes, cand[k], s));
+            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 0, 2, false, nullptr, b->smem_bytes_flow, 0,
+                                     cand[k], s));
             LBB_CK(cudaEventRecord(b->ev0, s));
-            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 20, false, nullptr, b->smem_bytes, cand[k], s));
+            LBB_CK(launch_batch_smem(d_tmp, b->d_smem, b->nsmem, 0, 20, false, nullptr, b->smem_bytes_flow, 0,
+                                     cand[k], s));
             LBB_CK(cudaEventRecord(b->ev1, s));
             LBB_CK(cudaEventSynchronize(b->ev1));
             float ms = 0.0f;
@@ -625,6 +638,7 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
             d.A[0] = reinterpret_cast<float4 *>(base + L.A0);
             d.A[1] = reinterpret_cast<float4 *>(base + L.A1);
         }
+        d.aux = reinterpret_cast<float4 *>(base + L.aux);
         d.tacc = reinterpret_cast<double *>(base + L.tacc);
     }
     LBB_CK(cudaMemsetAsync(sl.mem, 0, L.total, s));   // rest state rho = rho0, j = 0; P = A = V = 0
@@ -783,6 +797,32 @@ int lbgpu_batch_mp_get(lbgpu_batch *b, int id, double vacf0[3], double vacf_sum[
         }
     }
     if (steps) *steps = sl.mp_steps;
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_mp_fields(lbgpu_batch *b, int id, double *P, double *P_ads)
+{
+    if (!valid_slot(b, id)) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_fields: no such box");
+    const Slot &sl = b->slots[id];
+    if (sl.d.phase != BATCH_MP) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_mp_fields: no tracer phase");
+    const size_t N = (size_t)sl.d.N;
+    std::vector<float4> f(N);
+    double *outs[2] = {P, P_ads};
+    for (int q = 0; q < 2; ++q) {
+        if (!outs[q]) continue;
+        const float4 *src = q == 0 ? sl.d.P[0] : sl.d.A[0];   // a call runs an even number of steps
+        if (!src) {
+            std::memset(outs[q], 0, sizeof(double) * 3 * N);
+            continue;
+        }
+        LBB_CK(cudaMemcpyAsync(f.data(), src, sizeof(float4) * N, cudaMemcpyDeviceToHost, b->stream));
+        LBB_CK(cudaStreamSynchronize(b->stream));
+        for (size_t i = 0; i < N; ++i) {
+            outs[q][3 * i] = f[i].x;
+            outs[q][3 * i + 1] = f[i].y;
+            outs[q][3 * i + 2] = f[i].z;
+        }
+    }
     return LBGPU_OK;
 }
 

@@ -148,15 +148,8 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
             vt[1] += p.y * ax.y;
             vt[2] += p.z * ax.z;
             mp32_finish(p, ax.w, n0, n1, n2);
-            if (a.ads && (m & INTERFACIAL_BIT)) {
-                const float4 q = a.A[par][r];
-                n0 += q.x * a.kd - a.ka * p.x;
-                n1 += q.y * a.kd - a.ka * p.y;
-                n2 += q.z * a.kd - a.ka * p.z;
-                a.A[par ^ 1][r] = make_float4(q.x * a.one_minus_kd + p.x * a.ka,
-                                              q.y * a.one_minus_kd + p.y * a.ka,
-                                              q.z * a.one_minus_kd + p.z * a.ka, 0.0f);
-            }
+            if (a.ads && (m & INTERFACIAL_BIT))
+                a.A[par ^ 1][r] = mp32_adsorb(p, a.A[par][r], a.ka, a.kd, a.one_minus_kd, n0, n1, n2);
             __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
         }
     }

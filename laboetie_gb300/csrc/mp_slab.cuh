@@ -5,10 +5,10 @@
 // (or bulk tensor copies) ahead of use, so the neighbour reads are shared-memory reads and every
 // V and P value is fetched from L2/HBM about 1.3 times (halo) per step; the column's flag words
 // (and the node's fixed (u*, D)) are loaded into registers ahead of use.  One block barrier per
-// plane.  Two sweeps: mp_slab_planes, the difference form of mp_f32.cu:k_mp32 (same operations in
-// the same order, so P is bit-identical) visiting each plane once; mp_slab_sweep, the flux form
-// of the batched boxes, node by node.  The argument struct provides V, P[2], A[2], mask, lx, ly,
-// lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3] (and aux for the difference form).
+// plane.  mp_slab_planes is the difference form of mp_f32.cu:k_mp32 (same operations in the same
+// order, so P is bit-identical) visiting each plane once, for single boxes and batched ones alike.
+// The argument struct provides V, P[2], A[2], aux, mask, lx, ly, lz, ads, ka, kd, one_minus_kd,
+// a1[3], lwh[3].
 #pragma once
 
 #include <type_traits>
@@ -54,6 +54,20 @@ __device__ __forceinline__ void mp32_finish(const float4 &p, float D, float &n0,
     n2 = __fadd_rn(p.z, __fmaf_rn(D, p.z, n2));
 }
 
+// Adsorption exchange at an interfacial fluid node (module_moment_propagation.f90:239-246), after
+// mp32_finish: n += kd A - ka P; returns A_next = (1 - kd) A + ka P.  Fused operations in a fixed
+// order, so every kernel that calls it rounds alike.
+__device__ __forceinline__ float4 mp32_adsorb(const float4 &p, const float4 &qa, float ka, float kd,
+                                              float one_minus_kd, float &n0, float &n1, float &n2)
+{
+    n0 = __fmaf_rn(qa.x, kd, __fmaf_rn(-ka, p.x, n0));
+    n1 = __fmaf_rn(qa.y, kd, __fmaf_rn(-ka, p.y, n1));
+    n2 = __fmaf_rn(qa.z, kd, __fmaf_rn(-ka, p.z, n2));
+    return make_float4(__fmaf_rn(p.x, ka, __fmul_rn(qa.x, one_minus_kd)),
+                       __fmaf_rn(p.y, ka, __fmul_rn(qa.y, one_minus_kd)),
+                       __fmaf_rn(p.z, ka, __fmul_rn(qa.z, one_minus_kd)), 0.0f);
+}
+
 template <int CX, int CY, int CZ>
 __device__ __forceinline__ float slab_cdot(const float4 &v)
 {
@@ -65,94 +79,6 @@ __device__ __forceinline__ float slab_cdot(const float4 &v)
     if constexpr (CZ > 0) s += v.z;
     if constexpr (CZ < 0) s -= v.z;
     return s;
-}
-
-// Flux-form sweep of one tile (batched boxes): P(par) -> P(par^1) (and A) for its fluid nodes,
-// P(r) + sum_l [P(r+c_l) sp_in(l) - P(r) sp_out(l)] (36 scatterings per node); vt += the nodes'
-// VACF terms (FP32, per thread).  sm: MPS_SMEM bytes of shared memory.  Every thread of the block
-// (MP_BLOCK = 256 = 32 x 8) must call it.  Planes are staged by per-thread asynchronous copies.
-template <typename Args>
-__device__ __forceinline__ void mp_slab_sweep(const Args &a, int par, int x0, int y0, int z0, int z1,
-                                              float4 *sm, float (&vt)[3])
-{
-    float4 *sV = sm, *sP = sm + 4 * SPLP;
-    const int lx = a.lx, ly = a.ly, lz = a.lz;
-    const float4 *__restrict__ Vg = a.V;
-    const float4 *__restrict__ Pg = a.P[par];
-    auto load_plane = [&](int zz) {
-        const int gz = zz < 0 ? zz + lz : (zz >= lz ? zz - lz : zz);
-        const int slot = (zz - z0 + 1) & 3;
-        float4 *dv = sV + slot * SPLP, *dp = sP + slot * SPLP;
-        for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
-            const int hx = k % SHX, hy = k / SHX;
-            int gx = x0 + hx - 1, gy = y0 + hy - 1;
-            gx = gx < 0 ? gx + lx : (gx >= lx ? gx - lx : gx);   // lx >= 32: one wrap at most
-            gy = gy < 0 ? gy + ly : (gy >= ly ? gy - ly : gy);   // ly >= 8
-            const size_t idx = (size_t)gx + (size_t)lx * ((size_t)gy + (size_t)ly * gz);
-            cp_async16(dv + k, Vg + idx);
-            cp_async16(dp + k, Pg + idx);
-        }
-        cp_async_commit();
-    };
-    const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool col = x < lx && y < ly;
-    load_plane(z0 - 1);
-    load_plane(z0);
-    load_plane(z0 + 1);
-    // the column's flag word of the next plane, loaded a plane ahead so that no plane starts on a
-    // global-memory round trip
-    const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
-    uint32_t m_next = col ? __ldg(a.mask + col0 + plane * z0) : 0u;
-    for (int z = z0; z < z1; ++z) {
-        cp_async_wait0();
-        __syncthreads();
-        if (z + 2 <= z1) load_plane(z + 2);
-        const size_t r = col0 + plane * z;
-        const uint32_t m = m_next;
-        if (col && z + 1 < z1) m_next = __ldg(a.mask + r + plane);
-        if (m & FLUID_BIT) {
-            const int c0 = (ty + 1) * SHX + (tx + 1);
-            const int s0 = (z - z0 + 1) & 3;
-            const float4 vr = sV[s0 * SPLP + c0];
-            const float4 p = sP[s0 * SPLP + c0];
-            float ux = 0.0f, uy = 0.0f, uz = 0.0f;
-            float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
-            static_for<1, Q>([&](auto L) {
-                constexpr int l = decltype(L)::value;
-                constexpr Vel c = vel(l);
-                constexpr int w = wclass(l);
-                const float on = ((m >> inv(l)) & 1u) ? 0.0f : 1.0f;  // r + c_l is fluid
-                const int q = ((z + c.z - z0 + 1) & 3) * SPLP + c0 + c.y * SHX + c.x;
-                const float4 vn = sV[q];
-                const float4 pn = sP[q];
-                const float sp = on * (a.a1[w] * slab_cdot<c.x, c.y, c.z>(vr) + a.lwh[w]);
-                const float spp = on * (a.a1[w] * slab_cdot<-c.x, -c.y, -c.z>(vn) + a.lwh[w]);
-                ux += c.x * sp;
-                uy += c.y * sp;
-                uz += c.z * sp;
-                n0 += pn.x * spp - p.x * sp;
-                n1 += pn.y * spp - p.y * sp;
-                n2 += pn.z * spp - p.z * sp;
-            });
-            vt[0] += p.x * ux;
-            vt[1] += p.y * uy;
-            vt[2] += p.z * uz;
-            n0 += p.x;
-            n1 += p.y;
-            n2 += p.z;
-            if (a.ads && (m & INTERFACIAL_BIT)) {
-                const float4 qa = a.A[par][r];
-                n0 += qa.x * a.kd - a.ka * p.x;
-                n1 += qa.y * a.kd - a.ka * p.y;
-                n2 += qa.z * a.kd - a.ka * p.z;
-                a.A[par ^ 1][r] = make_float4(qa.x * a.one_minus_kd + p.x * a.ka,
-                                              qa.y * a.one_minus_kd + p.y * a.ka,
-                                              qa.z * a.one_minus_kd + p.z * a.ka, 0.0f);
-            }
-            __stcs(a.P[par ^ 1] + r, make_float4(n0, n1, n2, 0.0f));
-        }
-    }
 }
 
 // Link of velocity (dx, dy, dz).
@@ -348,15 +274,8 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
                 vt[1] += p.y * ax.y;
                 vt[2] += p.z * ax.z;
                 mp32_finish(p, ax.w, n.x, n.y, n.z);
-                if (a.ads && (A.m & INTERFACIAL_BIT)) {
-                    const float4 qa = a.A[par][r];
-                    n.x += qa.x * a.kd - a.ka * p.x;
-                    n.y += qa.y * a.kd - a.ka * p.y;
-                    n.z += qa.z * a.kd - a.ka * p.z;
-                    a.A[par ^ 1][r] = make_float4(qa.x * a.one_minus_kd + p.x * a.ka,
-                                                  qa.y * a.one_minus_kd + p.y * a.ka,
-                                                  qa.z * a.one_minus_kd + p.z * a.ka, 0.0f);
-                }
+                if (a.ads && (A.m & INTERFACIAL_BIT))
+                    a.A[par ^ 1][r] = mp32_adsorb(p, a.A[par][r], a.ka, a.kd, a.one_minus_kd, n.x, n.y, n.z);
                 __stcs(a.P[par ^ 1] + r, make_float4(n.x, n.y, n.z, 0.0f));
             }
         }

@@ -511,6 +511,7 @@ def _batch_lib():
         ("lbgpu_batch_moments", [vp, i, vp, vp, vp, vp], C.c_int),
         ("lbgpu_batch_mp_start", [vp, i], C.c_int),
         ("lbgpu_batch_mp_get", [vp, i, vp, vp, vp, pi], C.c_int),
+        ("lbgpu_batch_mp_fields", [vp, i, vp, vp], C.c_int),
         ("lbgpu_batch_info", [vp, pi, C.POINTER(C.c_longlong), pi, C.POINTER(C.c_size_t)], C.c_int),
         ("lbgpu_serve", [vp, vp, i, d, i, vp], C.c_int),
     ):
@@ -626,6 +627,13 @@ class Batch:
         self._chk(self.L.lbgpu_batch_mp_get(self.b, box, *(_ptr(x) for x in v), C.byref(st)),
                   "batch_mp_get")
         return v[0], v[1], v[2], st.value
+
+    def mp_fields(self, box: int):
+        """(P, P_ads) of a box in its tracer phase, shape (lz, ly, lx, 3), as Box.mp_get."""
+        shape = self._shapes[box] + (3,)
+        P, A = np.zeros(shape), np.zeros(shape)
+        self._chk(self.L.lbgpu_batch_mp_fields(self.b, box, _ptr(P), _ptr(A)), "batch_mp_fields")
+        return P, A
 
     def info(self):
         a, sm = C.c_int(0), C.c_int(0)

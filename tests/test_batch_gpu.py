@@ -31,7 +31,7 @@ def _cells():
 
 
 def _run(cells, idx, flow_steps, mp_steps):
-    """Run the cells idx together; returns {i: (rho, j, mp_get)}."""
+    """Run the cells idx together; returns {i: (rho, j, mp_get, mp_fields)}."""
     out = {}
     with Batch() as b:
         ids = {i: b.add(cells[i][0], relaxation_time=1.0, f_ext=cells[i][1],
@@ -42,18 +42,19 @@ def _run(cells, idx, flow_steps, mp_steps):
             b.mp_start(ids[i])
         b.steps(mp_steps)
         for i in idx:
-            out[i] = mom[i] + (b.mp_get(ids[i]),)
+            out[i] = mom[i] + (b.mp_get(ids[i]), b.mp_fields(ids[i]))
     return out
 
 
 def _same(a, b):
-    (ra, ja, ma), (rb, jb, mb) = a, b
+    (ra, ja, ma, fa), (rb, jb, mb, fb) = a, b
     assert np.array_equal(ra, rb)
     for d in range(3):
         assert np.array_equal(ja[d], jb[d])
     for x, y in zip(ma[:3], mb[:3]):
         assert np.array_equal(x, y)
     assert ma[3] == mb[3]
+    assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1])
 
 
 def test_batch_box_alone_equals_box_in_mix():
@@ -66,7 +67,9 @@ def test_batch_box_alone_equals_box_in_mix():
 
 def test_batch_shared_memory_and_tiled_paths_agree(monkeypatch):
     """The shared-memory and the tiled kernels do the same per-node arithmetic: the flow state
-    is bit-identical; the VACF sums differ only by the order of their FP64 additions."""
+    and the tracer's P and P_ads are bit-identical.  The VACF terms are summed per thread in FP32
+    (over a thread's few nodes of the box in shared memory, one node per thread in a tile) before
+    the FP64 sums, so the VACF sums differ by that grouping: 1e-6 relative."""
     cells = _cells()[:3]
     res = {}
     for mode in ("1", "0"):
@@ -77,12 +80,13 @@ def test_batch_shared_memory_and_tiled_paths_agree(monkeypatch):
         res[mode] = _run(cells, range(3), 200, 100)
     assert res["1info"] == 3 and res["0info"] == 0
     for i in range(3):
-        (ra, ja, ma), (rb, jb, mb) = res["1"][i], res["0"][i]
+        (ra, ja, ma, fa), (rb, jb, mb, fb) = res["1"][i], res["0"][i]
         assert np.array_equal(ra, rb)
         for d in range(3):
             assert np.array_equal(ja[d], jb[d])
+        assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1]) and np.abs(fa[0]).max() > 0
         for x, y in zip(ma[:3], mb[:3]):
-            assert np.allclose(x, y, rtol=1e-12, atol=1e-15 * np.abs(ma[0]).max())
+            assert np.allclose(x, y, rtol=1e-6, atol=1e-9 * np.abs(ma[0]).max())
 
 
 def test_batch_flow_reaches_the_fp64_steady_state(oracle_mod):
@@ -107,13 +111,15 @@ def test_batch_flow_reaches_the_fp64_steady_state(oracle_mod):
 @pytest.mark.parametrize("make,fe", [
     (lambda: geo.slit(4, 4, 34), (1e-5, 0.0, 0.0)),                                   # shared memory
     (lambda: geo.modulated_tube(48, n=32, r_mean=10.0, r_amp=4.0), (0.0, 0.0, 1e-5)),  # slab tiles
+    (lambda: geo.modulated_tube(40, n=16, r_mean=5.0, r_amp=2.0), (0.0, 0.0, 1e-5)),   # node tiles
 ])
 def test_batch_tracer_matches_single_box_fp32(make, fe):
-    """Given the batch's own flow moments, the single-box FP32 propagation computes the same V
-    and P step for step.  VACF(0) agrees to 1e-12 relative (FP64 sums of the same per-node
-    terms in another order); the per-step VACF is summed per thread in FP32 over a few nodes
-    before the FP64 sums, and the kernels group the nodes differently, so the VACF sums agree to
-    1e-6 of the summed magnitudes."""
+    """Given the batch's own flow moments, the single-box FP32 propagation computes the same V,
+    (u*, D) and P step for step: P and P_ads bit-identical after K steps (the batch's node, slab
+    and shared-memory kernels do the single box's operations in its order).  VACF(0) agrees to
+    1e-12 relative (FP64 sums of the same per-node terms in another order); the per-step VACF is
+    summed per thread in FP32 over a few nodes before the FP64 sums, and the kernels group the
+    nodes differently, so the VACF sums agree to 1e-6 of the summed magnitudes."""
     nat = make()
     K = 400
     with Batch() as b:
@@ -123,11 +129,14 @@ def test_batch_tracer_matches_single_box_fp32(make, fe):
         b.mp_start(box)
         b.steps(K)
         v0, vs, vl, steps = b.mp_get(box)
+        bP, bA = b.mp_fields(box)
     assert steps == K
     with Box(nat, relaxation_time=1.0, f_ext=fe, precision=FP32_DEV) as sb:
         s0 = sb.mp_init(moments=(rho, j), f_ext=fe, **TR)
         vac, _ = sb.mp_propagate(K)
+        sP, sA = sb.mp_get()
     assert len(vac) == K
+    assert np.array_equal(bP, sP) and np.array_equal(bA, sA) and np.abs(sP).max() > 0
     scale = np.abs(s0).max()
     assert np.max(np.abs(v0 - s0)) <= 1e-12 * scale
     assert np.all(np.abs(vs - vac.sum(axis=0)) <= 1e-6 * np.abs(vac).sum(axis=0))

@@ -75,8 +75,8 @@ def test_no_gpu_means_a_loud_failure_not_a_cpu_fallback():
 def test_batch_footprint_and_struct_layout():
     """lbgpu_batch_footprint is host logic, an upper bound over both layouts: populations, flags,
     previous velocity and the nature byte per node, the compact-layout positions, flags and row
-    table (256-byte aligned parts), plus the tracer buffers when Db > 0 (two more float4 records
-    per node with adsorption)."""
+    table (256-byte aligned parts), plus the tracer buffers when Db > 0 (V, P twice and the fixed
+    (u*, D): four float4 records per node, two more with adsorption)."""
     from laboetie_gb300.lbgpu import Cell, Request, RequestResult, footprint, make_cell
 
     assert (ctypes.sizeof(Cell), ctypes.sizeof(Request), ctypes.sizeof(RequestResult)) == (144, 200, 88)
@@ -85,7 +85,7 @@ def test_batch_footprint_and_struct_layout():
     base = up(76 * N) + up(4 * N) + up(16 * N) + up(N) + 2 * up(4 * N) + up(8 * 50 * 50)
     assert footprint(make_cell((1, 50, 50))) == base
     tiles = (N + 255) // 256
-    mp = 3 * up(16 * N) + up(8 * (9 * tiles + 1))
+    mp = 4 * up(16 * N) + up(8 * (9 * tiles + 1))
     assert footprint(make_cell((1, 50, 50), tracer=dict(Db=0.01))) == base + mp
     ads = footprint(make_cell((1, 50, 50), tracer=dict(Db=0.01, ka=0.02, kd=0.01)))
     assert ads == base + mp + 2 * up(16 * N)

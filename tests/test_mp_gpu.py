@@ -141,8 +141,10 @@ def test_mp_fp32_tracks_fp64(oracle_mod):
 
 def test_mp_fp32_slab_and_grid_stride_steps_agree(monkeypatch):
     """The shared-memory slab step (boxes with lx >= 32, ly >= 8) and the grid-stride step do
-    the same per-node arithmetic: P and P_ads are bit-identical after any number of steps; the
-    VACF differs only in the order of its node sums (1e-12 of |VACF(0)|)."""
+    the same per-node arithmetic: P and P_ads are bit-identical after any number of steps.  The
+    VACF terms are summed per thread in FP32 before the FP64 sums, over the nodes of a column's
+    z-chunk (slab) or a grid-stride walk, so the per-step VACF differs by that grouping: 1e-9 of
+    |VACF(0)| (observed ~1e-12)."""
     nat = geo.porous_spheres(L=40, radius=5.0, porosity=0.6, seed=3)
     rng = np.random.default_rng(5)
     rho = np.where(nat == 0, 1.0 + 1e-3 * rng.standard_normal(nat.shape), 0.0)
@@ -158,7 +160,7 @@ def test_mp_fp32_slab_and_grid_stride_steps_agree(monkeypatch):
     a, b = out["1"], out["0"]
     assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
     assert len(a[1]) == len(b[1]) == 37
-    assert np.max(np.abs(a[1] - b[1])) <= 1e-12 * np.abs(a[0]).max()
+    assert np.max(np.abs(a[1] - b[1])) <= 1e-9 * np.abs(a[0]).max()
 
 
 def test_fp32_slab_bulk_tensor_copies_equal_per_thread_copies(monkeypatch):
