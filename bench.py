@@ -583,6 +583,10 @@ def main():
         cpu = {"value": round(mlups_cpu, 4), "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": f"{steps_cpu} flow steps of the full 192^3 box by the C restatement of "
                          "the reference (FP64, OpenMP streaming as the reference)"}
+        if threads > 1:   # the same on one host thread (the reference without OpenMP)
+            mlups_1, steps_1, _, _ = cpu_oracle_mlups(nature, min(a.cpu_seconds, 5.0), 1)
+            cpu["single_thread"] = {"value": round(mlups_1, 4), "unit": "MLUPS", "cores": 1,
+                                    "sample": f"{steps_1} flow step(s) of the full box"}
 
     if rank != 0:
         return
