@@ -196,7 +196,9 @@ int lbgpu_time_flow_steps(lbgpu_ctx *ctx, int nsteps, int force_on, float *ms);
 int lbgpu_sync(lbgpu_ctx *ctx);
 
 /* Page-lock (pin) an existing host array so that the copies of the calls above run at full
- * host<->device bandwidth, e.g. the Fortran host's n(:,:,:,:).  Unregister before freeing it. */
+ * host<->device bandwidth, e.g. the Fortran host's n(:,:,:,:).  Unregister before freeing it.
+ * An FP32 context's lbgpu_flow_set reads populations that lie inside one registered range in
+ * place (the device converts them straight from host memory, no device copy of the FP64 array). */
 int lbgpu_host_register(void *ptr, size_t bytes);
 int lbgpu_host_unregister(void *ptr);
 

@@ -6,9 +6,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ctx.h"
@@ -112,6 +115,32 @@ namespace lbg {
 int geometry_build(int label, int lx, int ly, int lz, const double *params, int8_t *d_nature,
                    long long *nfluid, cudaStream_t s, std::string &err);
 int geometry_check(int label, int lx, int ly, int lz, const double *params, std::string &err);
+}  // namespace lbg
+
+namespace lbg {
+// Host ranges page-locked through lbgpu_host_register: [begin, end).
+std::mutex g_pinned_mutex;
+std::vector<std::pair<uintptr_t, uintptr_t>> g_pinned;
+
+const void *pinned_device_view(const void *p, size_t bytes)
+{
+    const uintptr_t b = reinterpret_cast<uintptr_t>(p), e = b + bytes;
+    bool inside = false;
+    {
+        std::lock_guard<std::mutex> lock(g_pinned_mutex);
+        for (const auto &r : g_pinned)
+            if (r.first <= b && e <= r.second) {
+                inside = true;
+                break;
+            }
+    }
+    void *d = nullptr;
+    if (!inside || cudaHostGetDevicePointer(&d, const_cast<void *>(p), 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return d;
+}
 }  // namespace lbg
 
 extern "C" {
@@ -256,12 +285,23 @@ int lbgpu_host_register(void *ptr, size_t bytes)
     if (!ptr || !bytes) return fail_global(LBGPU_ERR_INVALID, "lbgpu_host_register: empty range");
     cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
     if (e != cudaSuccess) return fail_global(LBGPU_ERR_CUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lock(lbg::g_pinned_mutex);
+    lbg::g_pinned.emplace_back(reinterpret_cast<uintptr_t>(ptr), reinterpret_cast<uintptr_t>(ptr) + bytes);
     return LBGPU_OK;
 }
 
 int lbgpu_host_unregister(void *ptr)
 {
     if (!ptr) return LBGPU_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lock(lbg::g_pinned_mutex);
+        auto &v = lbg::g_pinned;
+        for (size_t k = 0; k < v.size(); ++k)
+            if (v[k].first == reinterpret_cast<uintptr_t>(ptr)) {
+                v.erase(v.begin() + (long)k);
+                break;
+            }
+    }
     cudaError_t e = cudaHostUnregister(ptr);
     if (e != cudaSuccess) return fail_global(LBGPU_ERR_CUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
     return LBGPU_OK;

@@ -103,6 +103,9 @@ void mp_release(lbgpu_ctx *ctx);
 void pnp_release(lbgpu_ctx *ctx);
 // device potential phi of the Poisson-Nernst-Planck state (N doubles), or null without one
 const double *pnp_potential(const lbgpu_ctx *ctx);
+// The device address of the host range [p, p + bytes) if it lies inside one range page-locked by
+// lbgpu_host_register (kernels may then read it in place), else null.
+const void *pinned_device_view(const void *p, size_t bytes);
 
 #define LBG_CK(ctx, call)                                                   \
     do {                                                                    \

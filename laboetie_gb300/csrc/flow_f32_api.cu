@@ -87,12 +87,18 @@ int f32_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const d
     cudaStream_t s = ctx->stream;
     FlowArgs32 a;
     fill_args32(ctx, a);
+    // populations page-locked by lbgpu_host_register are read in place by the conversion kernel
+    // (no device copy of the FP64 array); others are staged through device memory
     double *tmp = nullptr;
-    LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
-    LBG_CK(ctx, cudaMemcpyAsync(tmp, n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
-    if (ctx->aa) LBG_CK(ctx, launch_to_dev_compact32(a, tmp, ctx->d_g[0], s));
-    else LBG_CK(ctx, launch_to_dev32(a, tmp, ctx->d_g[1], s));
-    LBG_CK(ctx, cudaFreeAsync(tmp, s));
+    const double *src = static_cast<const double *>(pinned_device_view(n, sizeof(double) * Q * N));
+    if (!src) {
+        LBG_CK(ctx, cudaMallocAsync(&tmp, sizeof(double) * Q * N, s));
+        LBG_CK(ctx, cudaMemcpyAsync(tmp, n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
+        src = tmp;
+    }
+    if (ctx->aa) LBG_CK(ctx, launch_to_dev_compact32(a, src, ctx->d_g[0], s));
+    else LBG_CK(ctx, launch_to_dev32(a, src, ctx->d_g[1], s));
+    if (tmp) LBG_CK(ctx, cudaFreeAsync(tmp, s));
     if (ctx->aa) {
         // AA: the populations are the natural-order state; the next launch collides them with
         // the current phase's force.  density and j are implied by n.

@@ -252,6 +252,38 @@ def test_fp32_in_place_and_two_buffer_streaming_agree(monkeypatch):
             assert np.array_equal(ja[d], jb[d])
 
 
+def test_fp32_flow_set_from_registered_host_memory():
+    """lbgpu_flow_set on an FP32 context converts populations page-locked by lbgpu_host_register
+    straight from host memory; the state is bit-identical to the one staged from pageable memory,
+    after the upload and after steps."""
+    from laboetie_gb300 import library
+
+    L = library()
+    nat = geo.porous_spheres(L=24, radius=3.0, porosity=0.6, seed=5)
+    with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 0.0, 0.0)) as b64:
+        b64.flow_init()
+        b64.flow_steps(30, force_on=True)
+        n0, rho0, j0 = b64.flow_get()
+    out = {}
+    for pinned in (False, True):
+        n = n0.copy()
+        if pinned:
+            assert L.lbgpu_host_register(n.ctypes.data, n.nbytes) == 0
+        try:
+            with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 0.0, 0.0), precision=FP32_DEV) as box:
+                box.flow_init()
+                box.flow_set(n, rho0, j0)
+                first = box.flow_get()
+                box.flow_steps(7, force_on=True)
+                out[pinned] = (first, box.flow_get())
+        finally:
+            if pinned:
+                L.lbgpu_host_unregister(n.ctypes.data)
+    for (na, ra, ja), (nb, rb, jb) in zip(out[False], out[True]):
+        assert np.array_equal(na, nb) and np.array_equal(ra, rb)
+        assert all(np.array_equal(ja[d], jb[d]) for d in range(3))
+
+
 def test_fp32_wide_gather_offsets_bit_identical(monkeypatch):
     """64-bit slot offsets of the in-place layout (taken once 19 Nf reaches 2^32; LBGPU_AA_WIDE=1
     forces them on any box) give the same bits as 32-bit ones: fixed steps, read back after odd
