@@ -1,8 +1,8 @@
 """Generates the fixtures of tests/golden/ from the CPU oracle.
 
 The reference (Fortran) ships no golden vectors and no Fortran compiler is available where this
-project is built, so these fixtures record the oracle's outputs on the BASELINE configs[0] slit
-(4x4x34, tau 1, f_ext (1e-5,0,0), target 1e-10; tracer Db 0.01 with and without adsorption,
+project is built, so these fixtures record the oracle's outputs on the Poiseuille slit of the
+reference's small case (4x4x34, tau 1, f_ext (1e-5,0,0), target 1e-10; tracer Db 0.01 with and without adsorption,
 K = e with kd 0.01).  They pin the oracle against regressions and give the GPU tests fixed
 expected values; they are not outputs of the reference itself.
 

@@ -141,7 +141,7 @@ def test_fused_fixed_steps_bit_exact(oracle_mod, f_ext):
 
 
 def test_equilibration_c1_bit_exact(oracle_mod):
-    """BASELINE configs[0] flow phase: slit 4x4x34, tau 1, f_ext (1e-5,0,0), target 1e-10."""
+    """Flow phase of the small slit case: slit 4x4x34, tau 1, f_ext (1e-5,0,0), target 1e-10."""
     nat = geo.slit(4, 4, 34)
     ref = oracle_mod.equilibration(nat, tau=1.0, target_error=1e-10, f_ext=(1e-5, 0, 0),
                                    max_steps=100000)

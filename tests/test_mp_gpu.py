@@ -44,7 +44,7 @@ def oracle_mp(oracle, nat, rho, j, f_ext, steps, **tr):
 
 @pytest.mark.parametrize("adsorb", [False, True])
 def test_mp_c1_fp64(oracle_mod, adsorb):
-    """BASELINE configs[0]: slit 4x4x34, tau 1, f_ext (1e-5,0,0), Db 0.01, K = e with kd 0.01."""
+    """The small slit case: slit 4x4x34, tau 1, f_ext (1e-5,0,0), Db 0.01, K = e with kd 0.01."""
     nat = geo.slit(4, 4, 34)
     f_ext = (1e-5, 0.0, 0.0)
     rho, j = converged_flow(oracle_mod, nat, 1.0, f_ext)
