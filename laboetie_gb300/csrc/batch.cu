@@ -115,19 +115,6 @@ __device__ __forceinline__ void aa_node_compact(const BatchInst &I, unsigned i, 
     }
 }
 
-template <int CX, int CY, int CZ>
-__device__ __forceinline__ float cdot(const float4 &v)
-{
-    float s = 0.0f;
-    if constexpr (CX > 0) s += v.x;
-    if constexpr (CX < 0) s -= v.x;
-    if constexpr (CY > 0) s += v.y;
-    if constexpr (CY < 0) s -= v.y;
-    if constexpr (CZ > 0) s += v.z;
-    if constexpr (CZ < 0) s -= v.z;
-    return s;
-}
-
 // One tracer step at fluid node r in the difference form of mp_f32.cu:k_mp32, with the same
 // operations in the same order (mp_slab.cuh helpers, mp_link_order), so a batched box's P is
 // bit-identical to a single box's; with INIT, P(t=1), the node's fixed (u*, D) in aux and its
@@ -163,9 +150,9 @@ __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float
         constexpr int w = wclass(l);
         const bool blocked = (m >> inv(l)) & 1u;  // r + c_l is solid
         const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
-        const float spp = mp32_scatter(blocked, I.a1[w], cdot<-c.x, -c.y, -c.z>(V[rp]), I.lwh[w]);
+        const float spp = mp32_scatter(blocked, I.a1[w], mp32_cdot<-c.x, -c.y, -c.z>(V[rp]), I.lwh[w]);
         if constexpr (INIT) {
-            const float sp = mp32_scatter(blocked, I.a1[w], cdot<c.x, c.y, c.z>(vr), I.lwh[w]);
+            const float sp = mp32_scatter(blocked, I.a1[w], mp32_cdot<c.x, c.y, c.z>(vr), I.lwh[w]);
             frac -= sp;
             ux += c.x * sp;
             uy += c.y * sp;

@@ -25,19 +25,6 @@
 namespace lbg {
 namespace {
 
-template <int CX, int CY, int CZ>
-__device__ __forceinline__ float cdot(const float4 &v)
-{
-    float s = 0.0f;
-    if constexpr (CX > 0) s += v.x;
-    if constexpr (CX < 0) s -= v.x;
-    if constexpr (CY > 0) s += v.y;
-    if constexpr (CY < 0) s -= v.y;
-    if constexpr (CZ > 0) s += v.z;
-    if constexpr (CZ < 0) s -= v.z;
-    return s;
-}
-
 // INIT: P(t=1) and VACF(0) (module_moment_propagation.f90:112-136), and the node's fixed
 // aux = (u*, D); else one step (module_moment_propagation.f90:207-253) in difference form:
 //   P_next(r) = P(r) + [sum_l sp_in(l) (P(r+c_l) - P(r)) + D P(r)]   (+ adsorption terms)
@@ -114,9 +101,9 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
                 lw_in = a.lw[w] * (1.0f - fermi);
                 emd = blocked ? 0.0f : 1.0f / e;
             }
-            const float spp = mp32_scatter(blocked, a.a1[w], cdot<-c.x, -c.y, -c.z>(vn), lw_in);
+            const float spp = mp32_scatter(blocked, a.a1[w], mp32_cdot<-c.x, -c.y, -c.z>(vn), lw_in);
             if constexpr (INIT) {
-                const float sp = mp32_scatter(blocked, a.a1[w], cdot<c.x, c.y, c.z>(vr), lw_out);
+                const float sp = mp32_scatter(blocked, a.a1[w], mp32_cdot<c.x, c.y, c.z>(vr), lw_out);
                 frac -= sp;
                 ux += c.x * sp;
                 uy += c.y * sp;

@@ -68,8 +68,10 @@ __device__ __forceinline__ float4 mp32_adsorb(const float4 &p, const float4 &qa,
                        __fmaf_rn(p.z, ka, __fmul_rn(qa.z, one_minus_kd)), 0.0f);
 }
 
+// c.V of a link (x, y, z summed in that order, signs folded): the one definition every FP32 tracer
+// kernel uses, so that their scattering probabilities round alike.
 template <int CX, int CY, int CZ>
-__device__ __forceinline__ float slab_cdot(const float4 &v)
+__device__ __forceinline__ float mp32_cdot(const float4 &v)
 {
     float s = 0.0f;
     if constexpr (CX > 0) s += v.x;
@@ -247,19 +249,19 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
                     if constexpr (dc && axis) {   // link (dx, dy, -1) of node zz+1
                         constexpr int l = link_of(dx, dy, -1);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((C.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, 1>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter((C.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, 1>(vn), a.lwh[w]),
                                   pn, C.p, C.n.x, C.n.y, C.n.z);
                     }
                     if constexpr (db && (dx != 0 || dy != 0)) {   // link (dx, dy, 0) of node zz
                         constexpr int l = link_of(dx, dy, 0);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((B.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, 0>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter((B.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, 0>(vn), a.lwh[w]),
                                   pn, B.p, B.n.x, B.n.y, B.n.z);
                     }
                     if constexpr (da && axis) {   // link (dx, dy, +1) of node zz-1
                         constexpr int l = link_of(dx, dy, 1);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((A.m >> inv(l)) & 1u, a.a1[w], slab_cdot<-dx, -dy, -1>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter((A.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, -1>(vn), a.lwh[w]),
                                   pn, A.p, A.n.x, A.n.y, A.n.z);
                     }
                 }
