@@ -9,7 +9,9 @@
 // memory, runs all the steps of a call there with a block barrier between steps, and writes it
 // back: HBM is touched twice per call instead of twice per step.  Every box is updated by its
 // own threads only and its arithmetic does not depend on which other boxes share the launch,
-// so a box gives the same result alone and in any mix, and in either path.
+// so a box gives the same result alone and in any mix, and in either path.  The tracer is the
+// single box's FP32 difference form (mp_f32.cu) with the same helpers and link order in every
+// path, so a batched box's P is bit-identical to a single box's on the same flow moments.
 #include <cfloat>
 
 #include "batch.h"
