@@ -267,9 +267,11 @@ int lbgpu_mp_release(lbgpu_ctx *ctx);
 int lbgpu_time_mp_steps(lbgpu_ctx *ctx, int nsteps, float *ms);
 
 /* ---------------------------------------------------------------- batches of boxes, serving
+ * No counterpart in the reference, which runs one lb.in per process.
  * Many independent boxes (cells) of any size stepped together in FP32 deviations with in-place
  * streaming, each in one of two phases: flow, then (optionally) the moment propagation of a
- * neutral tracer in the box's final flow field.  Large boxes are stepped by one tiled launch
+ * neutral tracer in the box's final flow field (the single box's FP32 tracer arithmetic: given
+ * the same flow moments, P is bit-identical to lbgpu_mp_get's).  Large boxes are stepped by one tiled launch
  * per step and phase, boxes of up to ~2,700 nodes by one block each that keeps the box in
  * shared memory for all the steps of a call; one call's launches run as a CUDA graph.  The
  * force acts from the first step on (a steady-state solve, no two-phase loop); the convergence
