@@ -67,7 +67,7 @@ typedef struct {
     double relaxation_time;      /* lb.in relaxation_time (module_collision.f90:38), > 0.5 */
     double target_error;         /* lb.in target_error (equilibration.f90:57), default 1e-10 */
     double f_ext[3];             /* lb.in f_ext (equilibration.f90:379, drop_tracers.f90:92) */
-    double rho0;                 /* lb.in initialSolventDensity (init_simu.f90:283) */
+    double rho0;                 /* lb.in initialSolventDensity (init_simu.f90:31) */
     int device;                  /* CUDA device ordinal */
 } lbgpu_params;
 
@@ -112,7 +112,7 @@ int lbgpu_create_label(const lbgpu_params *p, int label, const double *params, l
 
 /* ---------------------------------------------------------------- flow: state transfer */
 
-/* init_simu.f90:283-291 on the device: density = rho0 on fluid, 0 on solid; n_l = w_l*density;
+/* init_simu.f90:31-39 on the device: density = rho0 on fluid, 0 on solid; n_l = w_l*density;
  * j = 0 and the force field = 0 (equilibration.f90:75-80,94-96). */
 int lbgpu_flow_init(lbgpu_ctx *ctx);
 
@@ -138,8 +138,9 @@ int lbgpu_collide(lbgpu_ctx *ctx, double *n, const double *density, const double
 int lbgpu_bounce_back_stream(lbgpu_ctx *ctx, double *n);
 
 /* equilibration.f90:248,254,266-268,293-300,339-343: density = SUM(n,4);
- * j = f_ext/2 + sum_l n_l c_l; *l2err = max|j - j_old| with j_old read from jx/jy/jz on entry.
- * Returns LBGPU_ERR_NEGATIVE_POPULATION if any n < 0 (results are still written). */
+ * j = f_ext/2 + sum_l n_l c_l; *l2err = max|j - j_old| with j_old read from jx/jy/jz on entry
+ * (a NaN difference makes l2err NaN).  Returns LBGPU_ERR_NEGATIVE_POPULATION if any n < 0 and
+ * LBGPU_ERR_NONFINITE if any n is NaN or infinite (results are still written). */
 int lbgpu_moments(lbgpu_ctx *ctx, const double *n, const double *f_ext_x,
                   const double *f_ext_y, const double *f_ext_z, double *density, double *jx,
                   double *jy, double *jz, double *l2err);
@@ -207,11 +208,13 @@ int lbgpu_host_unregister(void *ptr);
  * memory (their populations already live on the GPU under their own allocator, or their loop
  * runs under a fixed device-memory budget): the moments of lbgpu_moments on caller-owned
  * device arrays, with no context and no cudaMalloc.  d_n is n(lx,ly,lz,19); d_jx/d_jy/d_jz hold
- * j_old on entry and j on exit; *l2err (host, optional) = max|j - j_old|.  Boxes of more than
+ * j_old on entry and j on exit; *l2err (host, optional) = max|j - j_old|.  Outputs and status
+ * bits are those of lbgpu_moments, non-finite input included.  Boxes of more than
  * 16,777,216 nodes (256^3) are rejected (LBGPU_ERR_INVALID): the reduction scratch is a fixed
  * ~1 MiB device array per GPU, shared by all calls, so calls that overlap on the GPU race.  The
  * first call on each device looks up that array's address; make it before any stream capture.
- * stream: a cudaStream_t, or NULL for the default stream.  The call waits for its stream. */
+ * stream: a cudaStream_t, or NULL for the default stream.  Every call ends by waiting for its
+ * stream. */
 int lbgpu_moments_noalloc(int lx, int ly, int lz, const double *d_n, const double *d_fx,
                           const double *d_fy, const double *d_fz, double *d_density,
                           double *d_jx, double *d_jy, double *d_jz, double *l2err, void *stream);

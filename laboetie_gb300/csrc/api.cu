@@ -45,6 +45,15 @@ int ctx_cuda(lbgpu_ctx *ctx, cudaError_t e, const char *what)
     return ctx_fail(ctx, LBGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+int moments_status(lbgpu_ctx *ctx, unsigned raised)
+{
+    const int bad = (int)(raised & (LBGPU_ERR_NEGATIVE_POPULATION | LBGPU_ERR_NONFINITE));
+    if (!bad) return LBGPU_OK;
+    if (bad & LBGPU_ERR_NEGATIVE_POPULATION)
+        return ctx_fail(ctx, bad, "In equilibration, the population n(x,y,z,vel) < 0");
+    return ctx_fail(ctx, bad, "moments: a population is not finite (NaN or Inf)");
+}
+
 // module_lbmodel.f90:127-147 and module_collision.f90:28,99-103, evaluated as the reference
 // does (every operation separately rounded).
 LbConst64 make_const64(double tau)

@@ -107,6 +107,16 @@ struct FlowCtl {
     int exit_phase;         // AA phase of the state the loop exited on
 };
 
+// Maximum of two values that are each non-negative or a NaN with the sign bit clear (what fabs
+// returns), taken on their IEEE bit patterns: the order of non-negative doubles is the order of
+// their bits, and a NaN's bits lie above +Inf's, so a NaN is never dropped as fmax drops it.
+__device__ __forceinline__ double max_nonneg(double a, double b)
+{
+    const unsigned long long ia = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ib = (unsigned long long)__double_as_longlong(b);
+    return __longlong_as_double((long long)(ia > ib ? ia : ib));
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v)
 {
     // IEEE-754 ordering of non-negative doubles equals the ordering of their bit patterns.

@@ -93,6 +93,9 @@ namespace lbg {
 
 int ctx_fail(lbgpu_ctx *ctx, int code, const std::string &msg);
 int ctx_cuda(lbgpu_ctx *ctx, cudaError_t e, const char *what);
+// The status of a moments operator from the bits its kernel raised: LBGPU_ERR_NEGATIVE_POPULATION
+// (the reference's stop, equilibration.f90:248) and/or LBGPU_ERR_NONFINITE, with their message.
+int moments_status(lbgpu_ctx *ctx, unsigned raised);
 int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature);
 void ctx_release_device(lbgpu_ctx *ctx);
 LbConst64 make_const64(double tau);

@@ -76,7 +76,7 @@ cudaError_t launch_stream_f64(const FlowArgs64 &a, cudaStream_t s);
 cudaError_t launch_moments_f64(const FlowArgs64 &a, bool field, cudaStream_t s);
 // pull from buffer (parity) + moments, writing n_t (if nout), rho and j for all nodes
 cudaError_t launch_finalize_f64(const FlowArgs64 &a, bool field, cudaStream_t s);
-// init_simu.f90:283-291: raw n = w*rho0 into buffer (parity), rho, j = 0
+// init_simu.f90:31-39: raw n = w*rho0 into buffer (parity), rho, j = 0
 cudaError_t launch_init_f64(const FlowArgs64 &a, double rho0, cudaStream_t s);
 
 // FP32 deviation ------------------------------------------------------------------------

@@ -416,10 +416,7 @@ int lbgpu_moments(lbgpu_ctx *ctx, const double *n, const double *f_ext_x, const 
     Scratch sc;
     if ((rc = read_scratch(ctx, sc))) return rc;
     if (l2err) std::memcpy(l2err, &sc.err_bits, sizeof(double));
-    if (sc.status & LBGPU_ERR_NEGATIVE_POPULATION)
-        return ctx_fail(ctx, LBGPU_ERR_NEGATIVE_POPULATION,
-                        "In equilibration, the population n(x,y,z,vel) < 0");
-    return LBGPU_OK;
+    return moments_status(ctx, sc.status);
 }
 
 int lbgpu_equilibration(lbgpu_ctx *ctx, int max_steps, double *l2err_hist, int hist_cap,

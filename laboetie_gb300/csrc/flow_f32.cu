@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(BLOCK) k_to_dev_compact32(const FlowArgs32 a, 
     out[t] = (float)(n[(size_t)l * (size_t)a.N + lattice_of(a, a.cpos[i])] - a.w64[wclass(l)] * a.rho0d);
 }
 
-// Zero deviations: the rest state rho = rho0, j = 0 (init_simu.f90:283-291 on fluid nodes).
+// Zero deviations: the rest state rho = rho0, j = 0 (init_simu.f90:31-39 on fluid nodes).
 __global__ void __launch_bounds__(BLOCK) k_init32(const FlowArgs32 a)
 {
     const size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x;

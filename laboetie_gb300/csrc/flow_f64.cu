@@ -195,7 +195,7 @@ __device__ __forceinline__ unsigned check19(const double (&n)[Q])
 __device__ __forceinline__ double warp_max(double v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = max_nonneg(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
 __device__ __forceinline__ unsigned warp_or(unsigned v)
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(BLOCK) k_flow_step(const FlowArgs64 a)
             else moments19(n, 0.0, 0.0, 0.0, rho, jx, jy, jz);
             if constexpr (CHECK) {
                 const double ox = a.jx[node], oy = a.jy[node], oz = a.jz[node];
-                err = fmax(fmax(fabs(jx - ox), fabs(jy - oy)), fabs(jz - oz));
+                err = max_nonneg(max_nonneg(fabs(jx - ox), fabs(jy - oy)), fabs(jz - oz));
                 a.jx[node] = jx;
                 a.jy[node] = jy;
                 a.jz[node] = jz;
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(BLOCK) k_moments(const FlowArgs64 a)
         double rho, jx, jy, jz;
         moments19(n, fx / 2.0, fy / 2.0, fz / 2.0, rho, jx, jy, jz);
         const double ox = a.jx[node], oy = a.jy[node], oz = a.jz[node];
-        err = fmax(fmax(fabs(jx - ox), fabs(jy - oy)), fabs(jz - oz));
+        err = max_nonneg(max_nonneg(fabs(jx - ox), fabs(jy - oy)), fabs(jz - oz));
         a.rho[node] = rho;
         a.jx[node] = jx;
         a.jy[node] = jy;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(BLOCK) k_moments(const FlowArgs64 a)
     }
 }
 
-// init_simu.f90:283-291 and equilibration.f90:75-80: raw n = w_l*rho into buffer `parity`.
+// init_simu.f90:31-39 and equilibration.f90:75-80: raw n = w_l*rho into buffer `parity`.
 __global__ void __launch_bounds__(BLOCK) k_init(const FlowArgs64 a, const double rho0)
 {
     double *__restrict__ dst = a.parity ? a.f1 : a.f0;

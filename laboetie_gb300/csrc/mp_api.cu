@@ -347,7 +347,7 @@ static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done,
                 rc = ctx_cuda(ctx, e, "moment propagation");
                 break;
             }
-            if (c.done) break;
+            if (c.done || (c.status & LBGPU_ERR_TIMEOUT)) break;
         }
     }
     cudaGraphExecDestroy(exec);

@@ -20,7 +20,13 @@
 //
 // The host side needs the device address of the array.  The first call on each device looks
 // it up (cudaGetSymbolAddress, with that device current) and caches it; that first call should
-// therefore be made before any stream capture the caller might begin.
+// therefore be made before any stream capture the caller might begin.  Every call ends by
+// copying l2err back and waiting for its stream.
+//
+// Results match lbgpu_moments bit for bit, including on non-finite input: l2err is a maximum
+// over IEEE bit patterns (a NaN difference gives a NaN l2err), and a NaN or infinite population
+// is reported as LBGPU_ERR_NONFINITE, a negative one as LBGPU_ERR_NEGATIVE_POPULATION (the
+// outputs are written either way).
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -39,7 +45,7 @@ constexpr long long NA_MAX_NODES = (long long)NA_MAX_BLOCKS * NA_BLOCK;
 constexpr int NA_MAX_DEVICES = 64;
 
 struct __align__(16) NaPartial {
-    double max_dj;    // max over the block's nodes of |j - j_old| (all three components)
+    double max_dj;    // max over the block's nodes of |j - j_old| (all three components; NaN wins)
     unsigned status;  // lbgpu_status bits raised by the block
     unsigned pad;
 };
@@ -83,7 +89,7 @@ k_na_moments(const double *__restrict__ n, const double *__restrict__ fx,
             if constexpr (c.z > 0) Z = Z + f[l];
             if constexpr (c.z < 0) Z = Z - f[l];
         });
-        err = fmax(fmax(fabs(X - jx[node]), fabs(Y - jy[node])), fabs(Z - jz[node]));
+        err = lbg::max_nonneg(lbg::max_nonneg(fabs(X - jx[node]), fabs(Y - jy[node])), fabs(Z - jz[node]));
         rho[node] = r;
         jx[node] = X;
         jy[node] = Y;
@@ -93,7 +99,7 @@ k_na_moments(const double *__restrict__ n, const double *__restrict__ fx,
     __shared__ double se[NA_BLOCK / 32];
     __shared__ unsigned sb[NA_BLOCK / 32];
     for (int o = 16; o > 0; o >>= 1) {
-        err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+        err = lbg::max_nonneg(err, __shfl_xor_sync(0xffffffffu, err, o));
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -106,7 +112,7 @@ k_na_moments(const double *__restrict__ n, const double *__restrict__ fx,
         double e = se[0];
         unsigned b = sb[0];
         for (int w = 1; w < NA_BLOCK / 32; ++w) {
-            e = fmax(e, se[w]);
+            e = lbg::max_nonneg(e, se[w]);
             b |= sb[w];
         }
         part[blockIdx.x].max_dj = e;
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(NA_BLOCK) k_na_reduce(NaPartial *part, unsigne
     double e = 0.0;
     unsigned b = 0;
     for (unsigned i = threadIdx.x; i < nb; i += NA_BLOCK) {
-        e = fmax(e, part[i].max_dj);
+        e = lbg::max_nonneg(e, part[i].max_dj);
         b |= part[i].status;
     }
     __shared__ double se[NA_BLOCK];
@@ -130,7 +136,7 @@ __global__ void __launch_bounds__(NA_BLOCK) k_na_reduce(NaPartial *part, unsigne
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int t = 1; t < NA_BLOCK; ++t) {
-            e = fmax(e, se[t]);
+            e = lbg::max_nonneg(e, se[t]);
             b |= sb[t];
         }
         part[NA_MAX_BLOCKS].max_dj = e;
@@ -192,8 +198,5 @@ extern "C" int lbgpu_moments_noalloc(int lx, int ly, int lz, const double *d_n,
     if (e != cudaSuccess)
         return lbg::ctx_fail(nullptr, LBGPU_ERR_CUDA, std::string("lbgpu_moments_noalloc: ") + cudaGetErrorString(e));
     if (l2err) *l2err = res.max_dj;
-    if (res.status & LBGPU_ERR_NEGATIVE_POPULATION)
-        return lbg::ctx_fail(nullptr, LBGPU_ERR_NEGATIVE_POPULATION,
-                             "In equilibration, the population n(x,y,z,vel) < 0");
-    return LBGPU_OK;
+    return lbg::moments_status(nullptr, res.status);
 }

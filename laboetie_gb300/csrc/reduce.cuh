@@ -105,6 +105,8 @@ __device__ __forceinline__ void mp_control(MpCtl *c, double *hist, const double 
         c->done = 1;
     }
     if (it >= c->max_it) c->done = 1;
+    // a block's bounded wait ran out (its tile was left alone): no further step is meaningful
+    if (atomicOr(&c->status, 0u) & LBGPU_ERR_TIMEOUT) c->done = 1;
 }
 
 }  // namespace lbg

@@ -25,6 +25,7 @@ STATUS = {
     1 << 9: "unsupported", 1 << 10: "device wait timed out",
 }
 ERR_NEGATIVE_POPULATION = 1 << 2
+ERR_NONFINITE = 1 << 3
 ERR_FRACTION = 1 << 4
 ERR_STEP_CAP = 1 << 5
 ERR_OOM = 1 << 6
@@ -271,7 +272,7 @@ class Box:
         err = C.c_double(0)
         rc = self.L.lbgpu_moments(self.ctx, _ptr(n), *(_ptr(x) for x in f), _ptr(rho),
                                   *(_ptr(x) for x in j), C.byref(err))
-        if rc and rc != ERR_NEGATIVE_POPULATION:
+        if rc & ~(ERR_NEGATIVE_POPULATION | ERR_NONFINITE):
             self._chk(rc, "moments")
         return rc, rho, tuple(j), err.value
 

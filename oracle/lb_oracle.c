@@ -113,7 +113,7 @@ void orc_detect_interfacial(int lx, int ly, int lz, const int8_t *nature, uint8_
             }
 }
 
-/* init_simu.f90:283-291 */
+/* init_simu.f90:31-39 */
 void orc_init_populations(int lx, int ly, int lz, const int8_t *nature, double svden,
                           double *n, double *density)
 {

@@ -42,7 +42,7 @@ void orc_lbm_tables(int c[19][3], int inv[19], double a0[19], double a1[19], dou
 /* supercell_definition.f90:115-147 (detectInterfacialNodes) */
 void orc_detect_interfacial(int lx, int ly, int lz, const int8_t *nature, uint8_t *interfacial);
 
-/* init_simu.f90:283-291: density = svden on non-solid, 0 on solid; n(:,:,:,l) = density*a0(l) */
+/* init_simu.f90:31-39: density = svden on non-solid, 0 on solid; n(:,:,:,l) = density*a0(l) */
 void orc_init_populations(int lx, int ly, int lz, const int8_t *nature, double svden,
                           double *n, double *density);
 

@@ -46,7 +46,7 @@ def test_default_params_are_the_reference_defaults():
     assert (p.lx, p.ly, p.lz) == (4, 5, 6)
     assert p.relaxation_time == 1.0      # module_collision.f90:38
     assert p.target_error == 1e-10       # equilibration.f90:57
-    assert p.rho0 == 1.0                 # init_simu.f90:283
+    assert p.rho0 == 1.0                 # init_simu.f90:31
     assert list(p.f_ext) == [0.0, 0.0, 0.0]
 
 

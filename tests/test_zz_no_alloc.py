@@ -62,6 +62,36 @@ def test_noalloc_moments_match_the_context_entry_point_on_two_calls():
         assert err == err_r
 
 
+def test_noalloc_moments_match_the_context_entry_point_on_non_finite_input():
+    """A NaN population and an infinite one: both entry points raise LBGPU_ERR_NONFINITE, write
+    the same (partly non-finite) moments and return the same l2err -- NaN for the NaN (a maximum
+    over bit patterns keeps the NaN that fmax would drop), +Inf for the infinity; then a finite
+    call on the same scratch is clean again."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device visible to torch")
+    nonfinite = 1 << 3
+    for bad in (np.nan, np.inf):
+        nat, n, f, jold = _case((6, 5, 7), 3)
+        n[4, 2, 3, 1] = bad
+        rc, rho, j, err = _noalloc(torch, n, f, jold)
+        with Box(nat) as box:
+            st, rho_r, j_r, err_r = box.moments(n, f, jold)
+        assert rc == st == nonfinite
+        assert np.array_equal(rho, rho_r, equal_nan=True) and not np.isfinite(rho[2, 3, 1])
+        for d in range(3):
+            assert np.array_equal(j[d], j_r[d], equal_nan=True)
+        if np.isnan(bad):
+            assert np.isnan(err) and np.isnan(err_r)
+        else:
+            assert err == err_r == np.inf
+    nat, n, f, jold = _case((6, 5, 7), 4)
+    rc, rho, j, err = _noalloc(torch, n, f, jold)
+    with Box(nat) as box:
+        st, rho_r, j_r, err_r = box.moments(n, f, jold)
+    assert rc == st == 0 and np.isfinite(err) and err == err_r
+
+
 def test_noalloc_moments_reject_boxes_beyond_the_scratch():
     L = library()
     one = ctypes.c_void_p(1)  # never dereferenced: the size check comes first
