@@ -1,0 +1,311 @@
+"""A second CPU restatement of laboetie's hot path, in numpy -- TEST INFRASTRUCTURE ONLY.
+
+Written from the Fortran sources of the reference, independently of ``lb_oracle.c``, so that a
+misreading of the Fortran in one restatement shows up as a difference between the two
+(``tests/test_oracle_np.py`` compares them bit for bit).  Only ``tests/`` use it.
+
+How the Fortran's arithmetic is reproduced: every expression is transcribed with the Fortran's
+own grouping (left to right within a sum or product, as gfortran evaluates them without
+``-ffast-math``); numpy evaluates each elementwise operation as one correctly rounded IEEE
+double operation and never fuses a multiply with an add, so a transcription vectorised over the
+nodes gives, node by node, the same bits as the scalar Fortran loop.  Whole-array ``SUM`` and the
+running sums of the reference's loops are formed sequentially in the reference's element order
+(``np.add.accumulate`` is sequential).  Where the reference multiplies by a velocity component
+(an integer 0 or +-1 converted to real) the product is formed as well, not skipped.
+
+Arrays: a field f(lx,ly,lz) is a numpy array of shape (lz, ly, lx) (x fastest, the Fortran
+element order); flow populations n(lx,ly,lz,19) are (19, lz, ly, lx); tracer populations
+n(19,lx,ly,lz) are (lz, ly, lx, 19); P(3,lx,ly,lz) is (lz, ly, lx, 3).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+FLUID, SOLID = 0, 1
+
+# module_lbmodel.f90:67-86 (D3Q19 velocities, l = 1..19 here 0..18) and 123-147 (weights).
+C = np.array([[0, 0, 0], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+              [1, 1, 0], [-1, 1, 0], [1, -1, 0], [-1, -1, 0], [1, 0, 1], [-1, 0, 1], [1, 0, -1],
+              [-1, 0, -1], [0, 1, 1], [0, -1, 1], [0, 1, -1], [0, -1, -1]], dtype=np.int64)
+CSQ = 1.0 / 3.0
+_A00, _A01, _A02 = 1.0 / 3.0, 1.0 / 18.0, 1.0 / 36.0
+_A1 = (_A00 / CSQ, _A01 / CSQ, _A02 / CSQ)
+_A2 = (_A00 / (2 * (CSQ * CSQ)), _A01 / (2 * (CSQ * CSQ)), _A02 / (2 * (CSQ * CSQ)))
+_CLASS = [0] + [1] * 6 + [2] * 12
+A0 = np.array([(_A00, _A01, _A02)[k] for k in _CLASS])
+A1 = np.array([_A1[k] for k in _CLASS])
+A2 = np.array([_A2[k] for k in _CLASS])
+# module_lbmodel.f90:156-162: inv(l) is the velocity with coo = -coo(l)
+INV = np.array([next(m for m in range(19) if (C[m] == -C[l]).all()) for l in range(19)])
+KBT = 1.0 / 3.0                     # module_system.f90:94
+PI = math.acos(-1.0)                # module_constants.f90:19
+EPS_DP = float(np.finfo(np.float64).eps)
+
+
+def _shift(a, c):
+    """a(x - c) for every node x of a periodic field shaped (lz, ly, lx): np.roll by +c."""
+    return np.roll(a, shift=(int(c[2]), int(c[1]), int(c[0])), axis=(0, 1, 2))
+
+
+def _at_plus(a, c):
+    """a(x + c) (module_system.f90:99-112 pbc, one step across the boundary)."""
+    return np.roll(a, shift=(-int(c[2]), -int(c[1]), -int(c[0])), axis=(0, 1, 2))
+
+
+def _seq_sum(a):
+    """Fortran SUM of an array: a single accumulator in array element order."""
+    flat = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    return float(np.add.accumulate(flat)[-1]) if flat.size else 0.0
+
+
+# ----------------------------------------------------------------------------------------- flow
+
+def init_populations(nature, svden=1.0):
+    """init_simu.f90:31-39: density = svden off the solid, 0 on it; n(:,:,:,l) = density*a0(l)."""
+    rho = np.where(nature != SOLID, svden, 0.0)
+    return np.stack([rho * A0[l] for l in range(19)]), rho
+
+
+def collide(nature, tau, n, rho, jx, jy, jz, fx, fy, fz):
+    """module_collision.f90:62-108 (second order; first_order_only has no defined result)."""
+    fl = nature == FLUID
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ux = np.where(fl, jx / rho, 0.0)
+        uy = np.where(fl, jy / rho, 0.0)
+        uz = np.where(fl, jz / rho, 0.0)
+    out = n.copy()
+    for l in range(19):
+        cx, cy, cz = (float(v) for v in C[l])
+        a0, a1, a2 = A0[l], A1[l], A2[l]
+        neq = a0 * rho \
+            + a1 * (cx * jx + cy * jy + cz * jz) \
+            + a2 * (jx * ux * (cx ** 2 - CSQ) + jx * uy * cx * cy + jx * uz * cx * cz
+                    + jy * ux * cy * cx + jy * uy * (cy ** 2 - CSQ) + jy * uz * cy * cz
+                    + jz * ux * cz * cx + jz * uy * cz * cy + jz * uz * (cz ** 2 - CSQ))
+        new = (1.0 - 1.0 / tau) * n[l] \
+            + (1.0 / tau) * neq \
+            + (1.0 - 1.0 / (2.0 * tau)) * (
+                a1 * ((cx - ux) * fx + (cy - uy) * fy + (cz - uz) * fz)
+                + 2.0 * a2 * (cx * ux + cy * uy + cz * uz) * (cx * fx + cy * fy + cz * fz))
+        out[l] = np.where(fl, new, n[l])
+    return out
+
+
+def bounce_back_stream(nature, n):
+    """equilibration.f90:204-243: for l = 1, 3, ..., 19 (Fortran numbering) swap n(x,l) with
+    n(x+c_l, inv l) where the two natures differ; then n(x+c_l, l) = n_old(x, l) for every l."""
+    n = n.copy()
+    for l in range(0, 19, 2):            # Fortran l = 1, 3, ..., 19
+        c, li = C[l], INV[l]
+        diff = nature != _at_plus(nature, c)
+        mine = n[l].copy()
+        theirs = _at_plus(n[li], c)      # n(x+c_l, inv l) seen from x
+        n[l] = np.where(diff, theirs, mine)
+        # the partner entries n(x+c, inv l) receive n(x, l): written back at x+c
+        back = _shift(np.where(diff, mine, theirs), c)
+        n[li] = np.where(_shift(diff, c), back, n[li])
+    return np.stack([_shift(n[l], C[l]) for l in range(19)])
+
+
+def moments(n, fx, fy, fz, jx_old, jy_old, jz_old):
+    """equilibration.f90:248-343: (any n<0, density = SUM(n,4), j = f/2 + sum_l n_l c_l, l2err)."""
+    negative = bool((n < 0).any())
+    rho = n[0].copy()
+    for l in range(1, 19):
+        rho = rho + n[l]
+    jx, jy, jz = fx / 2.0, fy / 2.0, fz / 2.0
+    for l in range(19):
+        cx, cy, cz = (float(v) for v in C[l])
+        jx = jx + n[l] * cx
+        jy = jy + n[l] * cy
+        jz = jz + n[l] * cz
+    l2err = max(np.abs(jx - jx_old).max(), np.abs(jy - jy_old).max(), np.abs(jz - jz_old).max())
+    return negative, rho, (jx, jy, jz), float(l2err)
+
+
+def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), svden=1.0,
+                  max_steps=100000):
+    """The time loop of equilibration.f90:143-491 with the uniform force (no compensate_f_ext):
+    collide, bounce-back, streaming, moments, l2err, and the two-phase force machine (f_ext on
+    fluid nodes from the step after the first convergence, exit at the second)."""
+    n, rho = init_populations(nature, svden)
+    z = np.zeros(nature.shape)
+    jx, jy, jz = z.copy(), z.copy(), z.copy()
+    fx, fy, fz = z.copy(), z.copy(), z.copy()
+    without = with_ = False
+    hist = []
+    for t in range(1, max_steps + 1):
+        n = collide(nature, tau, n, rho, jx, jy, jz, fx, fy, fz)
+        n = bounce_back_stream(nature, n)
+        negative, rho, (jx2, jy2, jz2), l2err = moments(n, fx, fy, fz, jx, jy, jz)
+        if negative:
+            raise RuntimeError("In equilibration, the population n(x,y,z,vel) < 0")
+        jx, jy, jz = jx2, jy2, jz2
+        hist.append(l2err)
+        converged = l2err <= target_error and t > 2
+        if converged:
+            if not without:
+                without = True
+            else:
+                with_ = True
+            if without and with_ and t > 2:
+                return dict(n=n, rho=rho, j=(jx, jy, jz), steps=t, l2err=np.array(hist))
+            fl = nature == FLUID
+            fx = np.where(fl, f_ext[0], fx)
+            fy = np.where(fl, f_ext[1], fy)
+            fz = np.where(fl, f_ext[2], fz)
+    return dict(n=n, rho=rho, j=(jx, jy, jz), steps=max_steps, l2err=np.array(hist), capped=True)
+
+
+# ------------------------------------------------------------------------ moment propagation
+
+def detect_interfacial(nature):
+    """supercell_definition.f90:115-147: a node is interfacial if any of its 18 periodic
+    neighbours has another nature."""
+    out = np.zeros(nature.shape, dtype=bool)
+    for l in range(1, 19):
+        out |= nature != _at_plus(nature, C[l])
+    return out
+
+
+def update_tracer_population(nature, rho, j, f_ext, q=0.0, D=0.0, elec_slope=(0.0, 0.0, 0.0)):
+    """drop_tracers.f90:94-105: n(l,x) = a0 rho + a1 sum(coo*(flux + f_ext - rho q D E)) on fluid
+    nodes, a0 rho + a1 sum(coo*flux) elsewhere.  Returns shape (lz, ly, lx, 19)."""
+    fl = nature == FLUID
+    out = np.empty(nature.shape + (19,))
+    for l in range(19):
+        cf = [float(v) for v in C[l]]
+        fluid_terms = [cf[d] * (j[d] + f_ext[d] - rho * q * D * elec_slope[d]) for d in range(3)]
+        solid_terms = [cf[d] * j[d] for d in range(3)]
+        nf = A0[l] * rho + A1[l] * (fluid_terms[0] + fluid_terms[1] + fluid_terms[2])
+        ns = A0[l] * rho + A1[l] * (solid_terms[0] + solid_terms[1] + solid_terms[2])
+        out[..., l] = np.where(fl, nf, ns)
+    return out
+
+
+def _scattprop(n, rho, w, lam, fermi):
+    """module_moment_propagation.f90:341-346: n/rho - w + lambda*w*fermi."""
+    with np.errstate(divide="ignore", invalid="ignore"):   # solid nodes (rho = 0) are masked
+        return n / rho - w + lam * w * fermi
+
+
+class MomentPropagation:
+    """module_moment_propagation.f90 init (30-160) and propagate (164-289) for a neutral tracer
+    (the reference stops on a charged one, :71-79): exp_dphi = 1, fermi = 1/2."""
+
+    def __init__(self, nature, rho, n_mp, ka=0.0, kd=0.0, Db=0.01):
+        self.nature = nature
+        self.fl = nature == FLUID
+        self.inter = detect_interfacial(nature)
+        self.rho = rho
+        self.n = n_mp
+        eps = EPS_DP
+        self.ka, self.kd = ka, kd
+        K = 0.0 if abs(kd) <= eps else ka / kd
+        self.ads = abs(K) > eps
+        self.lam = 4.0 * Db / KBT                                  # calc_lambda, :331-337
+        self.Db = Db
+        nf = int(self.fl.sum())
+        nfi = int((self.fl & self.inter).sum())
+        pstat = float(nf) + K * float(nfi)                         # :97
+        bw = 1.0 / pstat
+        fermi = 1.0 / (1.0 + 1.0)
+        exp_min_dphi = 1.0 / 1.0
+        vacf0 = [0.0, 0.0, 0.0]
+        P = np.zeros(nature.shape + (3,))
+        # the init loop, DO CONCURRENT over fluid nodes and l = 2..19 (:105-136); the vacf sum
+        # runs over nodes in array element order, l inner
+        terms = []
+        for l in range(1, 19):
+            c = C[l]
+            nbr_fluid = _at_plus(self.fl, c)
+            on = self.fl & nbr_fluid
+            sp = _scattprop(self.n[..., l], rho, A0[l], self.lam, fermi)
+            li = INV[l]
+            sp_p = _scattprop(_at_plus(self.n[..., li], c), _at_plus(rho, c), A0[li], self.lam,
+                              1.0 - fermi)
+            for d in range(3):
+                term = exp_min_dphi * sp_p * float(C[li][d]) * bw
+                P[..., d] = np.where(on, P[..., d] + term, P[..., d])
+            terms.append([np.where(on, bw * sp * float(c[d]) ** 2, 0.0) for d in range(3)])
+        for d in range(3):
+            # node-major, l-minor order of the reference's nested loops
+            t = np.stack([terms[k][d] for k in range(18)], axis=-1)
+            on_all = np.stack([self.fl & _at_plus(self.fl, C[l]) for l in range(1, 19)], axis=-1)
+            vacf0[d] = _seq_sum(np.where(on_all, t, 0.0)[on_all])
+        self.vacf0 = np.array(vacf0)
+        self.P = P
+        self.A = np.zeros_like(P) if self.ads else None
+        self.fermi = fermi
+
+    def propagate(self, it):
+        """One step: returns (vacf(it), is_converged); raises if a remaining fraction < eps."""
+        fl, rho, lam, fermi = self.fl, self.rho, self.lam, self.fermi
+        Pn = self.P
+        Pnext = np.zeros_like(Pn)
+        frac = np.ones(fl.shape)
+        us = [np.zeros(fl.shape) for _ in range(3)]
+        for l in range(1, 19):               # Fortran l = 2..19
+            c, li = C[l], INV[l]
+            on = fl & _at_plus(fl, c)
+            sp = _scattprop(self.n[..., l], rho, A0[l], lam, fermi)
+            frac = np.where(on, frac - sp, frac)
+            for d in range(3):
+                us[d] = np.where(on, us[d] + sp * float(c[d]), us[d])
+            sp_p = _scattprop(_at_plus(self.n[..., li], c), _at_plus(rho, c), A0[li], lam,
+                              1.0 - fermi)
+            for d in range(3):
+                Pnext[..., d] = np.where(on, Pnext[..., d] + _at_plus(Pn[..., d], c) * sp_p,
+                                         Pnext[..., d])
+        vacf = np.array([_seq_sum(np.where(fl, Pn[..., d] * us[d], 0.0)[fl]) for d in range(3)])
+        bulk = fl & ~(self.inter & self.ads) if self.ads else fl
+        for d in range(3):
+            Pnext[..., d] = np.where(bulk, Pnext[..., d] + frac * Pn[..., d], Pnext[..., d])
+        if self.ads:
+            site = fl & self.inter
+            frac = np.where(site, frac - self.ka, frac)
+            An = self.A
+            Anext = np.zeros_like(An)
+            for d in range(3):
+                Pnext[..., d] = np.where(site, Pnext[..., d] + frac * Pn[..., d]
+                                         + An[..., d] * self.kd, Pnext[..., d])
+                Anext[..., d] = np.where(site, An[..., d] * (1.0 - self.kd)
+                                         + Pn[..., d] * self.ka, Anext[..., d])
+            self.A = Anext
+        if (frac[fl] < EPS_DP).any():
+            raise RuntimeError("somewhere restpart is negative")
+        self.P = Pnext
+        lx, ly, lz = fl.shape[2], fl.shape[1], fl.shape[0]
+        thr = 1.0 / (2.0 * lx * ly * lz / self.Db)
+        conv = it > 2 and bool((np.abs(vacf) < thr).all() and (np.abs(vacf) < float(np.float32(1.e-12))).all())
+        return vacf, conv
+
+
+# ---------------------------------------------------------------------------------- Poisson
+
+def sor(nature, sigma, bjl, c_plus, c_minus, phi, anormf0, maxiter=500000):
+    """sor.f90:7-91: over-relaxed Jacobi (omega 1.4) over every node, phi* = sum_l a0(l)
+    phi(x - c_l) + 4 pi bjl kBT/2 (c+ - c-), stop when sum|phi* - phi| <= 1e-5 anormf0 (the
+    sum over i outer, j, k inner); then anormf0 = SUM(|phi|).  Returns (phi, anormf0, iter-1)."""
+    if sigma == 0.0:
+        return np.zeros(nature.shape), anormf0, 0
+    eps = float(np.float32(1.0e-5))
+    omega = 1.4
+    factor = 4.0 * PI * bjl * KBT / 2.0
+    phi = phi.copy()
+    rhs = factor * (c_plus - c_minus)
+    for it in range(1, maxiter + 1):
+        phistar = np.zeros(nature.shape)
+        for l in range(19):
+            phistar = phistar + A0[l] * _shift(phi, C[l])
+        phistar = phistar + rhs
+        phitmp = omega * phistar + (1.0 - omega) * phi
+        anorm = _seq_sum(np.transpose(np.abs(phistar - phi), (2, 1, 0)))   # k fastest
+        phi = phitmp
+        if anorm <= eps * anormf0:
+            break
+    else:
+        raise RuntimeError("maximum iterations 500 000 reached without convergence in sor")
+    return phi, _seq_sum(np.abs(phi)), it - 1

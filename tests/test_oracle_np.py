@@ -1,0 +1,148 @@
+"""Two independent restatements of the reference agree bit for bit.
+
+oracle/lb_oracle.c (C) and oracle/np_oracle.py (numpy) were each written from the Fortran
+sources of the reference.  The reference cannot be compiled here (no Fortran compiler), so its
+own outputs are not available; two restatements that agree to the last bit on the collision,
+the bounce-back + streaming, the moments, the whole flow loop, the tracer init and propagation
+and the Poisson sweeps make a misreading of the Fortran by either one visible.  Sums that the
+reference itself forms in an unspecified order (OpenMP reductions of the VACF) are compared to
+1e-12 of |VACF(0)|.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import np_oracle as npo
+from laboetie_gb300 import geometry as geo
+
+
+def _random_nature(shape, frac, seed):
+    rng = np.random.default_rng(seed)
+    nat = (rng.random(shape) < frac).astype(np.int8)
+    nat.flat[0] = 0
+    return nat
+
+
+def _random_state(nature, seed, amp=0.02):
+    rng = np.random.default_rng(seed)
+    n = npo.A0[:, None, None, None] * (1.0 + amp * rng.standard_normal((19,) + nature.shape))
+    rho = n.sum(axis=0)
+    j = [(n * npo.C[:, d][:, None, None, None]).sum(axis=0) + amp * rng.standard_normal(nature.shape)
+         for d in range(3)]
+    f = [1e-4 * rng.standard_normal(nature.shape) for _ in range(3)]
+    return n, rho, j, f
+
+
+BOXES = [
+    ("slit-c1", lambda: geo.slit(4, 4, 34)),
+    ("cc8", lambda: geo.cc(8, 8, 8)),
+    ("random-6x5x7", lambda: _random_nature((7, 5, 6), 0.3, 1)),
+    ("thin-x", lambda: _random_nature((9, 8, 1), 0.25, 2)),
+    ("thin-2", lambda: _random_nature((2, 3, 2), 0.3, 3)),
+    ("line-z", lambda: _random_nature((11, 1, 1), 0.3, 4)),
+    ("cylinder", lambda: geo.cylinder(9, 9, 5)),
+]
+
+
+def test_tables_agree(oracle_mod):
+    c, inv, a0, a1, a2, _ = oracle_mod.tables()
+    assert np.array_equal(c, npo.C) and np.array_equal(inv, npo.INV)
+    assert np.array_equal(a0, npo.A0) and np.array_equal(a1, npo.A1) and np.array_equal(a2, npo.A2)
+
+
+@pytest.mark.parametrize("name,make", BOXES)
+def test_interfacial_agrees(oracle_mod, name, make):
+    nat = make()
+    assert np.array_equal(oracle_mod.detect_interfacial(nat).astype(bool), npo.detect_interfacial(nat))
+
+
+@pytest.mark.parametrize("tau", [0.6, 0.8, 1.0, 1.7])
+@pytest.mark.parametrize("name,make", BOXES)
+def test_collide_bit_exact(oracle_mod, name, make, tau):
+    nat = make()
+    n, rho, j, f = _random_state(nat, 11)
+    want = oracle_mod.collide(nat, tau, n, rho, j, f)
+    got = npo.collide(nat, tau, n, rho, *j, *f)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("name,make", BOXES)
+def test_bounce_back_stream_bit_exact(oracle_mod, name, make):
+    nat = make()
+    n, _, _, _ = _random_state(nat, 12)
+    assert np.array_equal(npo.bounce_back_stream(nat, n), oracle_mod.bounce_back_stream(nat, n))
+
+
+@pytest.mark.parametrize("name,make", BOXES)
+def test_moments_bit_exact(oracle_mod, name, make):
+    nat = make()
+    n, _, j, f = _random_state(nat, 13)
+    rc, rho, jj, err = oracle_mod.moments(nat, n, f, j)
+    neg, rho2, jj2, err2 = npo.moments(n, *f, *j)
+    assert (rc != 0) == neg
+    assert np.array_equal(rho2, rho) and all(np.array_equal(a, b) for a, b in zip(jj2, jj))
+    assert err2 == err
+
+
+@pytest.mark.parametrize("name,make,tau,f_ext,target", [
+    ("slit-c1", lambda: geo.slit(4, 4, 34), 1.0, (1e-5, 0.0, 0.0), 1e-10),
+    ("cc8", lambda: geo.cc(8, 8, 8), 0.8, (2e-5, 0.0, 0.0), 1e-9),
+    ("random", lambda: _random_nature((5, 6, 7), 0.25, 5), 1.3, (0.0, 1e-5, 3e-6), 1e-9),
+])
+def test_flow_loop_bit_exact(oracle_mod, name, make, tau, f_ext, target):
+    nat = make()
+    ref = oracle_mod.equilibration(nat, tau=tau, target_error=target, f_ext=f_ext,
+                                   max_steps=20000, check=False)
+    got = npo.equilibration(nat, tau=tau, target_error=target, f_ext=f_ext, max_steps=20000)
+    assert got["steps"] == ref["steps"]
+    assert np.array_equal(got["l2err"], ref["l2err"])
+    assert np.array_equal(got["n"], ref["n"]) and np.array_equal(got["rho"], ref["rho"])
+    assert all(np.array_equal(a, b) for a, b in zip(got["j"], ref["j"]))
+
+
+@pytest.mark.parametrize("adsorb", [False, True])
+@pytest.mark.parametrize("name,make,tau,f_ext", [
+    ("slit-c1", lambda: geo.slit(4, 4, 34), 1.0, (1e-5, 0.0, 0.0)),
+    ("cc8", lambda: geo.cc(8, 8, 8), 0.8, (2e-5, 0.0, 0.0)),
+])
+def test_tracer_bit_exact(oracle_mod, name, make, tau, f_ext, adsorb):
+    nat = make()
+    ref = oracle_mod.equilibration(nat, tau=tau, target_error=1e-9, f_ext=f_ext, max_steps=50000)
+    rho, j = ref["rho"], ref["j"]
+    ka, kd = (0.01 * math.e, 0.01) if adsorb else (0.0, 0.0)
+    nmp = oracle_mod.update_tracer_population(nat, rho, j, f_ext, 0.0, 0.01)
+    nmp2 = npo.update_tracer_population(nat, rho, j, f_ext)
+    assert np.array_equal(nmp2, nmp.reshape(nmp2.shape))
+    mp = oracle_mod.MomentPropagation(nat, oracle_mod.detect_interfacial(nat), rho, nmp,
+                                      ka=ka, kd=kd, Db=0.01)
+    mp2 = npo.MomentPropagation(nat, rho, nmp2, ka=ka, kd=kd, Db=0.01)
+    scale = np.abs(mp.vacf0).max()
+    assert np.max(np.abs(mp2.vacf0 - mp.vacf0)) <= 1e-12 * scale
+    assert np.array_equal(mp2.P, mp.P().reshape(mp2.P.shape))
+    for it in range(1, 301):
+        v, conv = mp.propagate(it)
+        v2, conv2 = mp2.propagate(it)
+        assert conv2 == conv
+        assert np.max(np.abs(v2 - v)) <= 1e-12 * scale
+        if conv:
+            break
+    assert np.array_equal(mp2.P, mp.P().reshape(mp2.P.shape))
+    if adsorb:
+        assert np.array_equal(mp2.A, mp.Pads().reshape(mp2.A.shape))
+    mp.close()
+
+
+@pytest.mark.parametrize("name,make", [("slit64", lambda: geo.slit(1, 1, 64)),
+                                       ("cc8", lambda: geo.cc(8, 8, 8)),
+                                       ("cyl", lambda: geo.cylinder(9, 9, 4))])
+def test_poisson_sweeps_bit_exact(oracle_mod, name, make):
+    nat = make()
+    inter = oracle_mod.detect_interfacial(nat)
+    sigma = -0.01 * int(((nat == 1) & (inter == 1)).sum())
+    cp, cm, phi, an, _ = oracle_mod.charges_init(nat, inter, 0.4, sigma, 4.0)
+    phi_o, an_o, it_o = oracle_mod.sor(nat, sigma, 0.4, cp, cm, phi, an)
+    phi_n, an_n, it_n = npo.sor(nat, sigma, 0.4, cp, cm, phi, an)
+    assert it_n == it_o
+    assert np.array_equal(phi_n, phi_o)
+    assert an_n == an_o
