@@ -23,6 +23,7 @@
 #include "ctx.h"
 #include "lbgpu.h"
 #include "trace.h"
+#include "pnp.h"
 #include "reduce.cuh"
 
 namespace lbg {
@@ -31,31 +32,6 @@ namespace {
 constexpr int PB = MP_BLOCK;
 constexpr double PI_D = 3.141592653589793;   // acos(-1.0_dp), module_constants.f90:19
 }
-
-struct PnpCtl {
-    int iter, done, converged, parity;
-    int max_iter;
-    unsigned blocks_done;
-    double anorm, limit;  // stop when anorm <= limit
-};
-
-struct PnpState {
-    lbgpu_pnp_params p{};
-    double *phi[2] = {nullptr, nullptr};
-    double *cp = nullptr, *cm = nullptr;
-    double *fp = nullptr, *fm = nullptr;    // flux_site_plus / flux_site_minus
-    double *bak[3] = {nullptr, nullptr, nullptr};  // phi_old, c_plus_old, c_minus_old
-    double *partial = nullptr;              // 4 per block
-    double *result = nullptr;               // 4 reduced sums
-    PnpCtl *ctl = nullptr;
-    int par = 0;                            // buffer holding phi
-    double anormf0 = 0.0, rho_ch = 0.0;
-    bool charged = false;
-    std::vector<void *> allocs;
-    // CUDA graphs of 8 and of 64 sweeps, captured at the first solve and replayed by every later
-    // one (their arguments are fixed until the state is released)
-    cudaGraphExec_t sor_exec[2] = {nullptr, nullptr};
-};
 
 const double *pnp_potential(const lbgpu_ctx *ctx)
 {

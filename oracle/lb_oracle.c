@@ -1124,3 +1124,223 @@ int orc_geometry(int label, int lx, int ly, int lz, const double *params, int8_t
         if (nature[q] == 0) return 0;
     return 4;
 }
+
+/* ------------------------------------------------------------ coupled electrokinetics */
+
+/* electrostatic_pot.f90:7-21 */
+void orc_electrostatic_pot(int lx, int ly, int lz, const double *phi, const double es[3],
+                           double *phi_tot)
+{
+    const long N = (long)lx * ly * lz;
+    if (es[0] == 0.0 && es[1] == 0.0 && es[2] == 0.0) {
+        for (long r = 0; r < N; ++r) phi_tot[r] = phi[r];
+        return;
+    }
+    for (int k = 0; k < lz; ++k)
+        for (int j = 0; j < ly; ++j)
+            for (int i = 0; i < lx; ++i) {
+                /* sum(elec_slope * real([i,j,k],dp)): one accumulator from 0, x then y then z */
+                double s = 0.0;
+                s = s + es[0] * (double)(i + 1);
+                s = s + es[1] * (double)(j + 1);
+                s = s + es[2] * (double)(k + 1);
+                const long r = nid(i, j, k, lx, ly);
+                phi_tot[r] = phi[r] + s;
+            }
+}
+
+/* comp_j.f90:14-27 */
+void orc_comp_j(int lx, int ly, int lz, const double *n, double *jx, double *jy, double *jz)
+{
+    init_tables();
+    const long N = (long)lx * ly * lz;
+    double *j[3] = {jx, jy, jz};
+    for (long r = 0; r < N; ++r)
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;   /* sum(n(i,j,k,:)*coo(d)) over l = 1..19 */
+            for (int l = 0; l < Q; ++l) s = s + n[(long)l * N + r] * (double)VC[l][d];
+            j[d][r] = 0.5 * (j[d][r] + s);
+        }
+}
+
+/* smolu.f90:1-144 */
+int orc_smolu(int lx, int ly, int lz, const int8_t *nature, const double *phi_tot,
+              double *c_plus, double *c_minus, double D_plus, double D_minus, int time,
+              int D_iter, const double es[3], const double ls[3], double el_curr[3],
+              double ion_curr[3], double *sf)
+{
+    init_tables();
+    const long N = (long)lx * ly * lz;
+    const double kBT = 1.0 / 3.0;
+    const double dit = (double)D_iter;
+    double *fp = (double *)calloc((size_t)N, sizeof(double));
+    double *fm = (double *)calloc((size_t)N, sizeof(double));
+    for (int i = 0; i < lx; ++i)
+        for (int j = 0; j < ly; ++j)
+            for (int k = 0; k < lz; ++k) {
+                const long r = nid(i, j, k, lx, ly);
+                for (int l = 1; l < Q; ++l) {
+                    const int ip = pbc0(i + VC[l][0], lx), jp = pbc0(j + VC[l][1], ly),
+                              kp = pbc0(k + VC[l][2], lz);
+                    const long rp = nid(ip, jp, kp, lx, ly);
+                    const double cx = (double)VC[l][0], cy = (double)VC[l][1], cz = (double)VC[l][2];
+                    if (nature[r] == 0 && nature[rp] == 0) {
+                        double e = exp(phi_tot[rp] - phi_tot[r]);
+                        /* smolu.f90:46-51: every matching case applies, in this order */
+                        if (i == lx - 1 && ip == 0) e = e * exp(es[0] * (double)lx);
+                        if (j == ly - 1 && jp == 0) e = e * exp(es[1] * (double)ly);
+                        if (k == lz - 1 && kp == 0) e = e * exp(es[2] * (double)lz);
+                        if (i == 0 && ip == lx - 1) e = e * exp(-(es[0] * (double)lx));
+                        if (j == 0 && jp == ly - 1) e = e * exp(-(es[1] * (double)ly));
+                        if (k == 0 && kp == lz - 1) e = e * exp(-(es[2] * (double)lz));
+                        const double em = 1.0 / e;
+                        double sl = 0.0;
+                        sl = sl + ls[0] * cx;
+                        sl = sl + ls[1] * cy;
+                        sl = sl + ls[2] * cz;
+                        const double edl = exp(sl);
+                        const double emdl = 1.0 / edl;
+                        double flp = 0.5 * (1.0 + em * emdl) * (c_plus[rp] * e * edl - c_plus[r]);
+                        double flm = 0.5 * (1.0 + e * emdl) * (c_minus[rp] * em * edl - c_minus[r]);
+                        const double elc = flp * D_plus - flm * D_minus;
+                        const double ionc = flp * D_plus + flm * D_minus;
+                        const double f_plus = 0.5 * (1.0 + em) * (c_plus[rp] * e - c_plus[r]);
+                        const double f_minus = 0.5 * (1.0 + e) * (c_minus[rp] * em - c_minus[r]);
+                        double fmi = kBT * (f_plus + f_minus);
+                        fmi = fmi - kBT * (c_plus[rp] - c_plus[r] + c_minus[rp] - c_minus[r]);
+                        flp = flp * (D_plus / DELTA[l]);
+                        flm = flm * (D_minus / DELTA[l]);
+                        fp[r] = fp[r] + flp;
+                        fm[r] = fm[r] + flm;
+                        el_curr[0] = el_curr[0] + W1[l] * cx * elc / dit;
+                        el_curr[1] = el_curr[1] + W1[l] * cy * elc / dit;
+                        el_curr[2] = el_curr[2] + W1[l] * cz * elc / dit;
+                        ion_curr[0] = ion_curr[0] + W1[l] * cx * ionc / dit;
+                        ion_curr[1] = ion_curr[1] + W1[l] * cy * ionc / dit;
+                        ion_curr[2] = ion_curr[2] + W1[l] * cz * ionc / dit;
+                        sf[r] = sf[r] + W1[l] * cx * fmi / dit;
+                        sf[r + N] = sf[r + N] + W1[l] * cy * fmi / dit;
+                        sf[r + 2 * N] = sf[r + 2 * N] + W1[l] * cz * fmi / dit;
+                    } else if (nature[r] == 0 && nature[rp] == 1) {
+                        const double e = exp(phi_tot[rp] - phi_tot[r]);
+                        const double em = 1.0 / e;
+                        const double f_plus = c_plus[r] * (1.0 - em);
+                        const double f_minus = c_minus[r] * (1.0 - e);
+                        const double fmi = kBT * (f_plus + f_minus);
+                        sf[r] = sf[r] + W1[l] * cx * fmi / dit;
+                        sf[r + N] = sf[r + N] + W1[l] * cy * fmi / dit;
+                        sf[r + 2 * N] = sf[r + 2 * N] + W1[l] * cz * fmi / dit;
+                    }
+                }
+            }
+    for (long r = 0; r < N; ++r)
+        if (nature[r] == 0) {
+            c_plus[r] = c_plus[r] + fp[r];
+            c_minus[r] = c_minus[r] + fm[r];
+        }
+    if (time > 0) {
+        /* n_fluidsites = sum(node%nature, mask=node%nature==fluid): fluid is 0, so the sum is 0
+         * and the currents are divided by zero (smolu.f90:126-134) */
+        long nfs = 0;
+        for (long r = 0; r < N; ++r)
+            if (nature[r] == 0) nfs += nature[r];
+        const double d = (double)nfs;
+        for (int q = 0; q < 3; ++q) {
+            el_curr[q] = el_curr[q] / d;
+            ion_curr[q] = ion_curr[q] / d;
+        }
+    }
+    double sp = 0.0, sm = 0.0;
+    for (long r = 0; r < N; ++r)
+        if (nature[r] == 0) {
+            sp = sp + fp[r];
+            sm = sm + fm[r];
+        }
+    free(fp);
+    free(fm);
+    if (fabs(sp) > (double)1.0e-12f || fabs(sm) > (double)1.0e-12f) return ORC_ERR_FLUX_SUM;
+    return ORC_OK;
+}
+
+/* advect.f90:2-116 */
+int orc_advect(int lx, int ly, int lz, const int8_t *nature, const double *jx, const double *jy,
+               const double *jz, double *c_plus, double *c_minus, double *fp, double *fm,
+               double el_curr[3], double ion_curr[3])
+{
+    const long N = (long)lx * ly * lz;
+    const double eps = 2.220446049250313e-16;   /* epsilon(1._dp) */
+    const double *J[3] = {jx, jy, jz};
+    int all_zero = 1, all_diff0 = 1, all_sum0 = 1;
+    for (long r = 0; r < N; ++r) {
+        if (!(fabs(c_plus[r]) <= eps && fabs(c_minus[r]) <= eps)) all_zero = 0;
+        if (!(fabs(c_plus[r] - c_minus[r]) <= eps)) all_diff0 = 0;
+        if (!(fabs(c_plus[r] + c_minus[r]) <= eps)) all_sum0 = 0;
+    }
+    if (all_zero) return ORC_OK;   /* advect.f90:32-34: no charge, nothing to advect */
+    if (all_diff0) {
+        el_curr[0] = el_curr[1] = el_curr[2] = 0.0;
+    } else {
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (long r = 0; r < N; ++r)
+                if (nature[r] == 0) s = s + J[d][r] * (c_plus[r] - c_minus[r]);
+            el_curr[d] = -s;
+        }
+    }
+    if (all_sum0) {   /* advect.f90:46-49 sets el_curr here, not ion_curr */
+        el_curr[0] = el_curr[1] = el_curr[2] = 0.0;
+    } else {
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (long r = 0; r < N; ++r)
+                if (nature[r] == 0) s = s + J[d][r] * (c_plus[r] + c_minus[r]);
+            ion_curr[d] = -s;
+        }
+    }
+    double cp_old = 0.0, cm_old = 0.0;
+    for (long r = 0; r < N; ++r) cp_old = cp_old + c_plus[r];
+    for (long r = 0; r < N; ++r) cm_old = cm_old + c_minus[r];
+    for (int i = 0; i < lx; ++i)
+        for (int j = 0; j < ly; ++j)
+            for (int k = 0; k < lz; ++k) {
+                const long r = nid(i, j, k, lx, ly);
+                if (fabs(c_plus[r]) <= eps && fabs(c_minus[r]) <= eps) continue;
+                const double vx = jx[r], vy = jy[r], vz = jz[r];
+                for (int ix = -1; ix <= 1; ++ix) {
+                    double ax = vx * (double)ix;
+                    for (int iy = -1; iy <= 1; ++iy) {
+                        double ay = vy * (double)iy;
+                        for (int iz = -1; iz <= 1; ++iz) {
+                            const long rp = nid(pbc0(i + ix, lx), pbc0(j + iy, ly), pbc0(k + iz, lz), lx, ly);
+                            double az = vz * (double)iz;
+                            double flp, flm;
+                            if (ax >= 0.0 && ay >= 0.0 && az >= 0.0 && nature[r] == nature[rp]) {
+                                if (ix == 0) ax = 1.0 - fabs(vx);
+                                if (iy == 0) ay = 1.0 - fabs(vy);
+                                if (iz == 0) az = 1.0 - fabs(vz);
+                                flp = ax * ay * az * c_plus[r];
+                                flm = ax * ay * az * c_minus[r];
+                            } else {
+                                flp = 0.0;
+                                flm = 0.0;
+                            }
+                            fm[r] = fm[r] - flm;
+                            fm[rp] = fm[rp] + flm;
+                            fp[r] = fp[r] - flp;
+                            fp[rp] = fp[rp] + flp;
+                        }
+                    }
+                }
+            }
+    for (long r = 0; r < N; ++r)
+        if (nature[r] == 0) {
+            c_minus[r] = c_minus[r] + fm[r];
+            c_plus[r] = c_plus[r] + fp[r];
+        }
+    double cm_new = 0.0, cp_new = 0.0;
+    for (long r = 0; r < N; ++r) cm_new = cm_new + c_minus[r];
+    for (long r = 0; r < N; ++r) cp_new = cp_new + c_plus[r];
+    if (fabs(cm_new - cm_old) > (double)1.e-8f || fabs(cp_new - cp_old) > (double)1.e-8f)
+        return ORC_ERR_CHARGE;
+    return ORC_OK;
+}

@@ -165,6 +165,36 @@ int orc_pnp(int lx, int ly, int lz, const int8_t *nature, double bjl, double sig
             double *c_minus, double *phi, double *anormf0, int max_outer, int *outer_out,
             int *sor_iters_total);
 
+/* ----------------------------------------------------------- coupled electrokinetics
+ * The operators of the reference's coupled loop (src/trash/equilibration_without_constraint.f90:
+ * 26-34, a driver that no longer builds), each restated as the subroutine it is. */
+
+/* electrostatic_pot.f90:7-21: phi_tot = phi, or phi + sum(elec_slope*[i,j,k]) (1-based i,j,k)
+ * when elec_slope is not all zero. */
+void orc_electrostatic_pot(int lx, int ly, int lz, const double *phi, const double elec_slope[3],
+                           double *phi_tot);
+
+/* comp_j.f90:14-27: solventFlux = 0.5*(solventFlux + sum_l n(:,:,:,l)*c_l) at every node. */
+void orc_comp_j(int lx, int ly, int lz, const double *n, double *jx, double *jy, double *jz);
+
+/* smolu.f90:1-144: link fluxes from phi_tot, c+ and c- (fluid-fluid links, with the elec_slope
+ * and lncb_slope corrections), c+- += the site fluxes on fluid nodes, the currents el_curr and
+ * ion_curr (in/out, accumulated, divided by n_fluidsites when time > 0) and solute_force
+ * (lx,ly,lz,3, in/out, accumulated).  ORC_ERR_FLUX_SUM if a flux sum exceeds 1.0e-12. */
+int orc_smolu(int lx, int ly, int lz, const int8_t *nature, const double *phi_tot,
+              double *c_plus, double *c_minus, double D_plus, double D_minus, int time,
+              int D_iter, const double elec_slope[3], const double lncb_slope[3],
+              double el_curr[3], double ion_curr[3], double *solute_force);
+
+/* advect.f90:2-116 with the solvent flux j: the volumetric advection of c+ and c- (flux_site
+ * arrays fp, fm are the reference's module variables, kept by the caller across calls), the
+ * currents (in/out).  The reference indexes ip_all(3) with ix = -1, 0, 1 (advect.f90:57-66), an
+ * undefined result for -1 and 0; this restatement takes the neighbour pbc(i + ix) that the code
+ * around it intends.  ORC_ERR_CHARGE if a total concentration changes by more than 1.e-8. */
+int orc_advect(int lx, int ly, int lz, const int8_t *nature, const double *jx, const double *jy,
+               const double *jz, double *c_plus, double *c_minus, double *fp, double *fm,
+               double el_curr[3], double ion_curr[3]);
+
 /* equilibration.f90:159-175, 504-516: mass-flux and mean-density profiles along an axis. */
 void orc_profiles(int lx, int ly, int lz, const double *density, const double *jx,
                   const double *jy, const double *jz, int axis, double *flux, double *mean_density);
