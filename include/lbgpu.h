@@ -396,6 +396,46 @@ int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *
  * sigma and -sigma by more than 1e-10. */
 int lbgpu_charge_test(lbgpu_ctx *ctx, double *solid_charge, double *fluid_charge);
 
+/* ---------------------------------------------------------------- coupled electrokinetics
+ * The operators of the reference's coupled electrokinetic time loop (its only driver,
+ * src/trash/equilibration_without_constraint.f90:26-34, no longer builds), one call per
+ * subroutine, on the context's charged-solute state (after lbgpu_pnp_init or lbgpu_pnp_set):
+ * the potential phi, the ion densities c+ and c-, and the reference's module variables phi_tot,
+ * solute_force(lx,ly,lz,3) (accumulated over lbgpu_smolu calls, zero at the first) and advect's
+ * flux_site arrays (accumulated over lbgpu_advect calls: the reference allocates them once and
+ * never resets them).  Host arrays jx/jy/jz are node%solventFlux(x:z). */
+
+/* electrostatic_pot.f90:7-21: phi_tot = phi + sum(elec_slope*[i,j,k]) (1-based node indices),
+ * or phi when elec_slope is all zero. */
+int lbgpu_electrostatic_pot(lbgpu_ctx *ctx, const double elec_slope[3]);
+
+/* comp_j.f90:14-27: j = 0.5*(j + sum_l n(:,:,:,l)*c_l) at every node (n(lx,ly,lz,19) host
+ * array; jx, jy, jz updated in place). */
+int lbgpu_comp_j(lbgpu_ctx *ctx, const double *n, double *jx, double *jy, double *jz);
+
+/* smolu.f90:1-144 with phi_tot (lbgpu_electrostatic_pot first): the fluid-fluid link fluxes of
+ * c+ and c- (with the elec_slope correction of links across the periodic boundary and the
+ * lncb_slope salt gradient), c+- += the site fluxes on fluid nodes, solute_force += the force of
+ * the solutes on the fluid, el_curr / ion_curr (in/out) += the currents divided by D_iter, then,
+ * when time > 0, divided by n_fluidsites = sum(node%nature, mask=fluid), which is 0 in the
+ * reference (so the currents become +-Inf or NaN there and here).  LBGPU_ERR_FLUX_SUM with the
+ * reference's message if a site-flux sum exceeds 1.0e-12 (the densities are updated first). */
+int lbgpu_smolu(lbgpu_ctx *ctx, int time, int D_iter, const double elec_slope[3],
+                const double lncb_slope[3], double el_curr[3], double ion_curr[3]);
+
+/* advect.f90:2-116: volumetric advection of c+ and c- by the solvent flux j; el_curr / ion_curr
+ * (in/out) as the reference sets them (its branch for c+ + c- = 0 zeroes el_curr).  The
+ * reference reads ip_all(ix) of an array declared ip_all(3) with ix = -1, 0, 1 (advect.f90:57-66),
+ * which has no defined result for -1 and 0; the library takes the neighbour pbc(i + ix) that
+ * the code around it intends.  LBGPU_ERR_CHARGE with the reference's message if a total
+ * concentration changes by more than 1.e-8 (the densities are updated first). */
+int lbgpu_advect(lbgpu_ctx *ctx, const double *jx, const double *jy, const double *jz,
+                 double el_curr[3], double ion_curr[3]);
+
+/* phi_tot(lx,ly,lz) and solute_force(lx,ly,lz,3) (zeros before the first lbgpu_smolu); either
+ * may be NULL. */
+int lbgpu_ek_get(lbgpu_ctx *ctx, double *phi_tot, double *solute_force);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
           "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 # translation units whose FP64 arithmetic must match the reference operation for operation
-STRICT = {"flow_f64.cu", "mp_f64.cu", "pnp.cu", "noalloc_moments.cu", "profiles.cu", "geometry_build.cu"}
+STRICT = {"flow_f64.cu", "mp_f64.cu", "pnp.cu", "ek.cu", "noalloc_moments.cu", "profiles.cu",
+          "geometry_build.cu"}
 
 
 def nvcc() -> str:

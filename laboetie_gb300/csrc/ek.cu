@@ -14,6 +14,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -452,7 +453,7 @@ int lbgpu_smolu(lbgpu_ctx *ctx, int time, int D_iter, const double elec_slope[3]
     if (time > 0) {
         // n_fluidsites = sum(node%nature, mask=node%nature==fluid) (smolu.f90:125): the natures
         // of fluid nodes are 0, so the reference divides the currents by zero
-        const double n_fluidsites = 0.0;
+        volatile double n_fluidsites = 0.0;
         for (int d = 0; d < 3; ++d) {
             el_curr[d] = el_curr[d] / n_fluidsites;
             ion_curr[d] = ion_curr[d] / n_fluidsites;

@@ -119,6 +119,11 @@ def library():
         ("lbgpu_just_eq_smolu", [vp, pi]),
         ("lbgpu_poisson_nernst_planck", [vp, i, pi, pi]),
         ("lbgpu_charge_test", [vp, C.POINTER(d), C.POINTER(d)]),
+        ("lbgpu_electrostatic_pot", [vp, vp]),
+        ("lbgpu_comp_j", [vp, vp, vp, vp, vp]),
+        ("lbgpu_smolu", [vp, i, i, vp, vp, vp, vp]),
+        ("lbgpu_advect", [vp, vp, vp, vp, vp, vp]),
+        ("lbgpu_ek_get", [vp, vp, vp]),
         ("lbgpu_moments_noalloc", [i, i, i] + [vp] * 8 + [C.POINTER(d), vp]),
         ("lbgpu_compensated_force_field", [vp, i, vp, i, vp, vp, vp]),
         ("lbgpu_set_force_field", [vp, vp, vp, vp]),
@@ -413,6 +418,60 @@ def _charge_test(self):
     return rc, s.value, f.value
 
 
+def _electrostatic_pot(self, elec_slope=(0.0, 0.0, 0.0)):
+    """electrostatic_pot.f90: phi_tot from the box's phi and elec_slope (kept on the device)."""
+    self._chk(self.L.lbgpu_electrostatic_pot(self.ctx, (C.c_double * 3)(*elec_slope)),
+              "electrostatic_pot")
+
+
+def _comp_j(self, n, j):
+    """comp_j.f90: returns j = 0.5*(j + sum_l n_l c_l)."""
+    n = _f64(n, (19,) + self.shape)
+    jj = [np.array(x, dtype=np.float64, order="C").reshape(self.shape) for x in j]
+    self._chk(self.L.lbgpu_comp_j(self.ctx, _ptr(n), *(_ptr(x) for x in jj)), "comp_j")
+    return tuple(jj)
+
+
+def _smolu(self, time=0, D_iter=-1, elec_slope=(0.0, 0.0, 0.0), lncb_slope=(0.0, 0.0, 0.0),
+           el_curr=(0.0, 0.0, 0.0), ion_curr=(0.0, 0.0, 0.0), check=True):
+    """smolu.f90 on the box's c+, c-, phi_tot; returns (el_curr, ion_curr), or
+    (el_curr, ion_curr, status) when check is False."""
+    el, io = (C.c_double * 3)(*el_curr), (C.c_double * 3)(*ion_curr)
+    rc = self.L.lbgpu_smolu(self.ctx, int(time), int(D_iter), (C.c_double * 3)(*elec_slope),
+                            (C.c_double * 3)(*lncb_slope), el, io)
+    out = (np.array(list(el)), np.array(list(io)))
+    if not check:
+        return out + (rc,)
+    self._chk(rc, "smolu")
+    return out
+
+
+def _advect(self, j, el_curr=(0.0, 0.0, 0.0), ion_curr=(0.0, 0.0, 0.0), check=True):
+    """advect.f90 of the box's c+, c- by the solvent flux j; returns (el_curr, ion_curr), or
+    (el_curr, ion_curr, status) when check is False."""
+    jj = [_f64(x, self.shape) for x in j]
+    el, io = (C.c_double * 3)(*el_curr), (C.c_double * 3)(*ion_curr)
+    rc = self.L.lbgpu_advect(self.ctx, *(_ptr(x) for x in jj), el, io)
+    out = (np.array(list(el)), np.array(list(io)))
+    if not check:
+        return out + (rc,)
+    self._chk(rc, "advect")
+    return out
+
+
+def _ek_get(self):
+    """(phi_tot, solute_force shaped (3, lz, ly, lx))."""
+    phi_tot = np.zeros(self.shape)
+    sf = np.zeros((3,) + self.shape)
+    self._chk(self.L.lbgpu_ek_get(self.ctx, _ptr(phi_tot), _ptr(sf)), "ek_get")
+    return phi_tot, sf
+
+
+Box.electrostatic_pot = _electrostatic_pot
+Box.comp_j = _comp_j
+Box.smolu = _smolu
+Box.advect = _advect
+Box.ek_get = _ek_get
 Box.pnp_init = _pnp_init
 Box.pnp_get = _pnp_get
 Box.pnp_set = _pnp_set

@@ -112,6 +112,13 @@ def lib():
         L.orc_profiles.argtypes = [_int, _int, _int] + [_dp] * 4 + [_int, _dp, _dp]
         L.orc_geometry.argtypes = [_int, _int, _int, _int, _vp, _vp]
         L.orc_profiles.restype = None
+        L.orc_electrostatic_pot.argtypes = [_int, _int, _int, _dp, _vp, _dp]
+        L.orc_electrostatic_pot.restype = None
+        L.orc_comp_j.argtypes = [_int, _int, _int] + [_dp] * 4
+        L.orc_comp_j.restype = None
+        L.orc_smolu.argtypes = [_int, _int, _int, _i8, _dp, _dp, _dp, _d, _d, _int, _int, _vp,
+                                _vp, _vp, _vp, _dp]
+        L.orc_advect.argtypes = [_int, _int, _int, _i8] + [_dp] * 7 + [_vp, _vp]
         _lib = L
     return _lib
 
@@ -331,6 +338,49 @@ def pnp(nature, bjl, sigma, D_plus, D_minus, rho_ch, cp, cm, phi, anormf0, loop_
         _chk(rc, "pnp")
     return dict(c_plus=cp, c_minus=cm, phi=phi, anormf0=an.value, outer=outer.value,
                 sor_iters=tot.value, status=rc)
+
+
+def electrostatic_pot(phi, elec_slope):
+    lz, ly, lx = phi.shape
+    out = np.zeros(phi.shape)
+    lib().orc_electrostatic_pot(lx, ly, lz, np.ascontiguousarray(phi, dtype=np.float64),
+                                (C.c_double * 3)(*elec_slope), out)
+    return out
+
+
+def comp_j(n, j):
+    lz, ly, lx = n.shape[1:]
+    jj = [np.array(x, dtype=np.float64, order="C") for x in j]
+    lib().orc_comp_j(lx, ly, lz, np.ascontiguousarray(n, dtype=np.float64), *jj)
+    return tuple(jj)
+
+
+def smolu(nature, phi_tot, cp, cm, D_plus, D_minus, time, D_iter, elec_slope, lncb_slope,
+          el_curr, ion_curr, solute_force):
+    """smolu.f90; returns (status, c+, c-, el_curr, ion_curr, solute_force)."""
+    nature = np.ascontiguousarray(nature, dtype=np.int8)
+    cp = np.array(cp, dtype=np.float64, order="C")
+    cm = np.array(cm, dtype=np.float64, order="C")
+    el = (C.c_double * 3)(*el_curr)
+    io = (C.c_double * 3)(*ion_curr)
+    sf = np.array(solute_force, dtype=np.float64, order="C")
+    rc = lib().orc_smolu(*_dims(nature), nature, np.ascontiguousarray(phi_tot), cp, cm, D_plus,
+                         D_minus, time, D_iter, (C.c_double * 3)(*elec_slope),
+                         (C.c_double * 3)(*lncb_slope), el, io, sf)
+    return rc, cp, cm, np.array(list(el)), np.array(list(io)), sf
+
+
+def advect(nature, j, cp, cm, fp, fm, el_curr, ion_curr):
+    """advect.f90; fp, fm: the flux_site arrays carried between calls (updated in place).
+    Returns (status, c+, c-, el_curr, ion_curr)."""
+    nature = np.ascontiguousarray(nature, dtype=np.int8)
+    cp = np.array(cp, dtype=np.float64, order="C")
+    cm = np.array(cm, dtype=np.float64, order="C")
+    el = (C.c_double * 3)(*el_curr)
+    io = (C.c_double * 3)(*ion_curr)
+    jx, jy, jz = (np.ascontiguousarray(x, dtype=np.float64) for x in j)
+    rc = lib().orc_advect(*_dims(nature), nature, jx, jy, jz, cp, cm, fp, fm, el, io)
+    return rc, cp, cm, np.array(list(el)), np.array(list(io))
 
 
 def profiles(nature, rho, j, axis):

@@ -309,3 +309,163 @@ def sor(nature, sigma, bjl, c_plus, c_minus, phi, anormf0, maxiter=500000):
     else:
         raise RuntimeError("maximum iterations 500 000 reached without convergence in sor")
     return phi, _seq_sum(np.abs(phi)), it - 1
+
+
+# --------------------------------------------------------------- coupled electrokinetics
+
+_exp = np.vectorize(math.exp, otypes=[np.float64])   # the C library's exp, as the C oracle's
+
+
+def electrostatic_pot(phi, elec_slope):
+    """electrostatic_pot.f90:7-21."""
+    if all(e == 0.0 for e in elec_slope):
+        return phi.copy()
+    lz, ly, lx = phi.shape
+    k, j, i = np.meshgrid(np.arange(1, lz + 1), np.arange(1, ly + 1), np.arange(1, lx + 1),
+                          indexing="ij")
+    s = np.zeros(phi.shape)
+    s = s + elec_slope[0] * i.astype(np.float64)
+    s = s + elec_slope[1] * j.astype(np.float64)
+    s = s + elec_slope[2] * k.astype(np.float64)
+    return phi + s
+
+
+def comp_j(n, j):
+    """comp_j.f90:14-27: j = 0.5*(j + sum(n(:,:,:,l)*coo(l))), the sum from 0 over l."""
+    out = []
+    for d in range(3):
+        s = np.zeros(n.shape[1:])
+        for l in range(19):
+            s = s + n[l] * float(C[l][d])
+        out.append(0.5 * (j[d] + s))
+    return tuple(out)
+
+
+def smolu(nature, phi_tot, cp, cm, D_plus, D_minus, time, D_iter, elec_slope, lncb_slope,
+          el_curr, ion_curr, solute_force):
+    """smolu.f90:1-144.  Returns (flux sums ok, c+, c-, el_curr, ion_curr, solute_force)."""
+    lz, ly, lx = nature.shape
+    fl = nature == FLUID
+    dit = float(D_iter)
+    fp, fm = np.zeros(nature.shape), np.zeros(nature.shape)
+    sf = [solute_force[d].copy() for d in range(3)]
+    k, jj, i = np.meshgrid(np.arange(lz), np.arange(ly), np.arange(lx), indexing="ij")
+    terms = []   # per link, the six current terms at every node (summed below in loop order)
+    for l in range(1, 19):
+        c = C[l]
+        cx, cy, cz = (float(v) for v in c)
+        a1 = A1[l]
+        fl_p = _at_plus(fl, c)
+        both = fl & fl_p
+        sol = fl & ~fl_p
+        php, cpp, cmp_ = _at_plus(phi_tot, c), _at_plus(cp, c), _at_plus(cm, c)
+        e = _exp(php - phi_tot)
+        ip, jp, kp = (i + c[0]) % lx, (jj + c[1]) % ly, (k + c[2]) % lz
+        for cond, fac in (((i == lx - 1) & (ip == 0), math.exp(elec_slope[0] * lx)),
+                          ((jj == ly - 1) & (jp == 0), math.exp(elec_slope[1] * ly)),
+                          ((k == lz - 1) & (kp == 0), math.exp(elec_slope[2] * lz)),
+                          ((i == 0) & (ip == lx - 1), math.exp(-(elec_slope[0] * lx))),
+                          ((jj == 0) & (jp == ly - 1), math.exp(-(elec_slope[1] * ly))),
+                          ((k == 0) & (kp == lz - 1), math.exp(-(elec_slope[2] * lz)))):
+            e = np.where(cond, e * fac, e)
+        em = 1.0 / e
+        sl = 0.0
+        sl = sl + lncb_slope[0] * cx
+        sl = sl + lncb_slope[1] * cy
+        sl = sl + lncb_slope[2] * cz
+        edl = math.exp(sl)
+        emdl = 1.0 / edl
+        flp = 0.5 * (1.0 + em * emdl) * (cpp * e * edl - cp)
+        flm = 0.5 * (1.0 + e * emdl) * (cmp_ * em * edl - cm)
+        elc = flp * D_plus - flm * D_minus
+        ionc = flp * D_plus + flm * D_minus
+        fpl = 0.5 * (1.0 + em) * (cpp * e - cp)
+        fmi = 0.5 * (1.0 + e) * (cmp_ * em - cm)
+        fmic = KBT * (fpl + fmi)
+        fmic = fmic - KBT * (cpp - cp + cmp_ - cm)
+        delta = 1.0 if l < 7 else math.sqrt(2.0)
+        flp = flp * (D_plus / delta)
+        flm = flm * (D_minus / delta)
+        fp = np.where(both, fp + flp, fp)
+        fm = np.where(both, fm + flm, fm)
+        terms.append([np.where(both, a1 * cd * x / dit, np.nan) for x in (elc, ionc)
+                      for cd in (cx, cy, cz)])
+        # the force on the solid across a fluid-solid link
+        es_ = _exp(php - phi_tot)
+        ems = 1.0 / es_
+        fmis = KBT * (cp * (1.0 - ems) + cm * (1.0 - es_))
+        for d, cd in enumerate((cx, cy, cz)):
+            sf[d] = np.where(both, sf[d] + a1 * cd * fmic / dit,
+                             np.where(sol, sf[d] + a1 * cd * fmis / dit, sf[d]))
+    # the currents, summed over nodes (i outer, j, k inner) and their links in l order
+    el, io = list(el_curr), list(ion_curr)
+    stack = [np.stack([terms[l][q] for l in range(18)], axis=-1) for q in range(6)]
+    order = np.transpose(np.arange(lx * ly * lz).reshape(lz, ly, lx), (2, 1, 0)).ravel()
+    for q in range(6):
+        t = stack[q].reshape(-1, 18)[order].ravel()
+        t = t[~np.isnan(t)]
+        acc = el[q] if q < 3 else io[q - 3]
+        acc = float(np.add.accumulate(np.concatenate([[acc], t]))[-1]) if t.size else acc
+        if q < 3:
+            el[q] = acc
+        else:
+            io[q - 3] = acc
+    cp2 = np.where(fl, cp + fp, cp)
+    cm2 = np.where(fl, cm + fm, cm)
+    if time > 0:
+        with np.errstate(divide="ignore", invalid="ignore"):
+            el = [v / np.float64(0.0) for v in el]
+            io = [v / np.float64(0.0) for v in io]
+    ok = not (abs(_seq_sum(fp[fl])) > float(np.float32(1.0e-12))
+              or abs(_seq_sum(fm[fl])) > float(np.float32(1.0e-12)))
+    return ok, cp2, cm2, np.array(el, dtype=float), np.array(io, dtype=float), np.stack(sf)
+
+
+def advect(nature, j, cp, cm, fp, fm, el_curr, ion_curr):
+    """advect.f90:2-116 as a literal loop (small boxes), the neighbour of link (ix, iy, iz) taken
+    as pbc(i + ix) where the reference's ip_all(ix) has no defined result.  fp, fm: flux_site
+    arrays carried between calls (updated in place).  Returns (ok, c+, c-, el_curr, ion_curr)."""
+    lz, ly, lx = nature.shape
+    eps = EPS_DP
+    cp, cm = cp.copy(), cm.copy()
+    el, io = [float(v) for v in el_curr], [float(v) for v in ion_curr]
+    fl = nature == FLUID
+    if (np.abs(cp) <= eps).all() and (np.abs(cm) <= eps).all():
+        return True, cp, cm, np.array(el), np.array(io)
+    if (np.abs(cp - cm) <= eps).all():
+        el = [0.0, 0.0, 0.0]
+    else:
+        el = [-_seq_sum((j[d] * (cp - cm))[fl]) for d in range(3)]
+    if (np.abs(cp + cm) <= eps).all():
+        el = [0.0, 0.0, 0.0]
+    else:
+        io = [-_seq_sum((j[d] * (cp + cm))[fl]) for d in range(3)]
+    cp_old, cm_old = _seq_sum(cp), _seq_sum(cm)
+    for i in range(lx):
+        for jj in range(ly):
+            for k in range(lz):
+                if abs(cp[k, jj, i]) <= eps and abs(cm[k, jj, i]) <= eps:
+                    continue
+                vx, vy, vz = (float(j[d][k, jj, i]) for d in range(3))
+                for ix in (-1, 0, 1):
+                    for iy in (-1, 0, 1):
+                        for iz in (-1, 0, 1):
+                            ip, jp, kp = (i + ix) % lx, (jj + iy) % ly, (k + iz) % lz
+                            ax, ay, az = vx * ix, vy * iy, vz * iz
+                            if ax >= 0 and ay >= 0 and az >= 0 and nature[k, jj, i] == nature[kp, jp, ip]:
+                                fx = 1.0 - abs(vx) if ix == 0 else ax
+                                fy = 1.0 - abs(vy) if iy == 0 else ay
+                                fz = 1.0 - abs(vz) if iz == 0 else az
+                                flp = fx * fy * fz * float(cp[k, jj, i])
+                                flm = fx * fy * fz * float(cm[k, jj, i])
+                            else:
+                                flp = flm = 0.0
+                            fm[k, jj, i] = fm[k, jj, i] - flm
+                            fm[kp, jp, ip] = fm[kp, jp, ip] + flm
+                            fp[k, jj, i] = fp[k, jj, i] - flp
+                            fp[kp, jp, ip] = fp[kp, jp, ip] + flp
+    cm = np.where(fl, cm + fm, cm)
+    cp = np.where(fl, cp + fp, cp)
+    ok = not (abs(_seq_sum(cm) - cm_old) > float(np.float32(1.e-8))
+              or abs(_seq_sum(cp) - cp_old) > float(np.float32(1.e-8)))
+    return ok, cp, cm, np.array(el), np.array(io)
