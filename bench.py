@@ -85,6 +85,43 @@ def args_():
     return ap.parse_args()
 
 
+def config_of(world, nature):
+    """The workload identity both arms print (the driver compares the two dicts)."""
+    return {"workload": WORKLOAD, "boxes": world, "fluid_nodes": int((nature == 0).sum()),
+            "nodes": int(nature.size)}
+
+
+def fp64_pipe(profile_name):
+    """FP64 instructions per fluid node of the fused FP64 step, from its committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", profile_name)
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"fp64_instructions_per_fluid_node:\s*([0-9.eE+-]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def fp64_roofline(dp_per_node, nodes_per_s, clocks, nfluid, hbm, ms_step):
+    """The FP64 step is bound by GB300's FP64 pipe (2 FP64 lanes per SM and clock, 152 SMs): the
+    fraction is the FP64 instructions the step issues per second (per fluid node, from the ncu
+    summary) over that pipe's peak at the SM clock sampled during the run."""
+    bytes_gbs = BYTES_F64 * nfluid / (ms_step * 1e-3) / 1e9
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = 152 * 2 * mhz * 1e6
+    out = {"bound": "fp64 pipe", "unit": "FP64 inst/s", "peak": peak,
+           "peak_kind": "152 SMs x 2 FP64 lanes x sampled SM clock",
+           "hbm_gbs": round(bytes_gbs, 1), "hbm_frac": round(bytes_gbs / hbm, 4),
+           "algorithmic_bytes_per_fluid_node": BYTES_F64}
+    if dp_per_node:
+        ach = dp_per_node * nodes_per_s
+        out.update({"achieved": ach, "frac": round(ach / peak, 4),
+                    "fp64_instructions_per_fluid_node": dp_per_node})
+    else:
+        out.update({"achieved": None, "frac": None})
+    return out
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -488,7 +525,7 @@ def run_reference(a):
         "unit": "MLUPS", "n_gpus": a.gpus, "steps": steps, "warmup": 1,
         "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded porous medium)",
-        "config": {"workload": WORKLOAD, "boxes": 1, "parallelism": "openmp"},
+        "config": config_of(1, nature), "parallelism": "openmp",
         "cpu_baseline": {"value": round(mlups, 4), "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"{steps} reference flow steps of the full 192^3 box "
                                    "(collide + bounce-back/stream + moments, OpenMP streaming)"},
@@ -505,7 +542,7 @@ def main():
     world, rank, local, dist = dist_setup()
     import ctypes as C
 
-    from laboetie_gb300 import FP32_DEV, FP64, Box, library
+    from laboetie_gb300 import FP32_DEV, FP64, FP64_FUSED, Box, library
     from laboetie_gb300 import geometry as geo
 
     L = library()
@@ -552,10 +589,26 @@ def main():
     n0, rho0, j0 = box64.flow_get()
     box64.close()
 
+    # ---------------------------------------------------------- FP64 fused (FMA, pair form)
+    box64f = Box(nature, relaxation_time=TAU, f_ext=FEXT, precision=FP64_FUSED, device=local)
+    box64f.flow_init()
+    box64f.time_flow_steps(W, force_on=True)
+    box64f.sync()
+    barrier(dist)
+    ms64f = max_over_ranks(dist, box64f.time_flow_steps(K64, force_on=True))
+    barrier(dist)
+    box64f.mp_init(f_ext=FEXT, Db=0.01, ka=0.01 * math.exp(2.0), kd=0.01)
+    box64f.time_mp_steps(W)
+    ms_mp64f = max_over_ranks(dist, box64f.time_mp_steps(KMP64))
+    box64f.mp_release()
+
     # ---------------------------------------------------------- e2e through the C ABI
     rhos = np.zeros(nature.shape)
     js = [np.zeros(nature.shape) for _ in range(3)]
     host = [n0, rho0, *j0, rhos, *js]
+    # FP64 fused, with the same host buffers (registered below): upload of the FP64 populations
+    # and moments, K64 steps, download of density and flux
+    box64f.sync()
     for h in host:
         rc = L.lbgpu_host_register(h.ctypes.data, h.nbytes)
         if rc:
@@ -574,6 +627,21 @@ def main():
     if rc:
         raise RuntimeError("lbgpu_flow_get failed")
     box.close()
+    barrier(dist)
+    for h in host:
+        if L.lbgpu_host_register(h.ctypes.data, h.nbytes):
+            raise RuntimeError("cudaHostRegister failed")
+    t0 = time.perf_counter()
+    box64f.flow_set(n0, rho0, j0)
+    box64f.flow_steps(K64, force_on=True)
+    rc = L.lbgpu_flow_get(box64f.ctx, None, rhos.ctypes.data, *(x.ctypes.data for x in js))
+    box64f.sync()
+    t_e2e64 = max_over_ranks(dist, time.perf_counter() - t0)
+    for h in host:
+        L.lbgpu_host_unregister(h.ctypes.data)
+    if rc:
+        raise RuntimeError("lbgpu_flow_get failed")
+    box64f.close()
 
     # ---------------------------------------------------------- CPU baseline (rank 0, N=1)
     cpu = None
@@ -595,6 +663,8 @@ def main():
     ms_step64 = ms64 / K64
     value = world * nfluid * K / (ms32 * 1e-3) / 1e6
     mlups64 = world * nfluid * K64 / (ms64 * 1e-3) / 1e6
+    mlups64f = world * nfluid * K64 / (ms64f * 1e-3) / 1e6
+    dp = fp64_pipe("flow_step_f64_fused_porous128.md")
     achieved32 = BYTES_F32 * nfluid / (ms_step32 * 1e-3) / 1e9
     achieved64 = BYTES_F64 * nfluid / (ms_step64 * 1e-3) / 1e9
     tr = ncu_traffic("flow_aa_f32_porous192.md")
@@ -604,21 +674,30 @@ def main():
         "metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": round(ms_step32, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded porous medium)",
-        "config": {"workload": WORKLOAD, "boxes": world,
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "fluid_nodes": nfluid, "nodes": int(nature.size),
-                   "l2": f"inputs larger than L2: {round(BYTES_F32 / 2 * nfluid / 1e6)} MB of FP32 populations "
-                         "(fluid nodes only) against the 129 MB L2; no flush between steps"},
+        "config": config_of(world, nature),
+        "parallelism": "replicas" if world > 1 else "single",
+        "l2": f"inputs larger than L2: {round(BYTES_F32 / 2 * nfluid / 1e6)} MB of FP32 populations "
+              "(fluid nodes only) against the 129 MB L2; no flush between steps",
         "roofline": {"bound": "hbm", "achieved": round(achieved32, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved32 / hbm, 4), "peak_kind": peak_kind,
                      "traffic": (round(tr * nfluid) if tr else None),
                      "algorithmic_bytes_per_fluid_node": BYTES_F32},
-        "fp64": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
-                 "ms_per_step": round(ms_step64, 4),
-                 "roofline": {"bound": "hbm", "achieved": round(achieved64, 1), "peak": hbm,
-                              "unit": "GB/s", "frac": round(achieved64 / hbm, 4),
-                              "algorithmic_bytes_per_fluid_node": BYTES_F64},
-                 "speedup_fp32_over_fp64": round(value / mlups64, 2)},
+        "fp64": {
+            "what": "FP64 storage and arithmetic: 'strict' reproduces the reference operation for "
+                    "operation (bit-identical); 'fused' regroups the collision per velocity pair "
+                    "with fused multiply-adds (within 1e-12 of the oracle)",
+            "value": round(mlups64f, 2), "unit": "MLUPS", "steps": K64,
+            "ms_per_step": round(ms64f / K64, 4),
+            "roofline": fp64_roofline(dp, mlups64f * 1e6, clocks_out, nfluid, hbm, ms64f / K64),
+            "e2e": {"value": round(world * nfluid * K64 / t_e2e64 / 1e6, 2), "unit": "MLUPS",
+                    "h2d_bytes_per_step": int(h2d / K64), "d2h_bytes_per_step": int(d2h / K64),
+                    "what": "FP64 fused context: lbgpu_flow_set (n, density, j from pinned host) + "
+                            f"{K64} steps + lbgpu_flow_get (density, j to pinned host), wall clock"},
+            "strict": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
+                       "ms_per_step": round(ms_step64, 4),
+                       "hbm_frac": round(achieved64 / hbm, 4)},
+            "fused_over_strict": round(mlups64f / mlups64, 3),
+            "speedup_fp32_over_fp64_fused": round(value / mlups64f, 2)},
         "moment_propagation": {
             "fp32": {"value": round(world * nfluid * KMP / (ms_mp32 * 1e-3) / 1e6, 2),
                      "unit": "M fluid-node steps/s", "steps": KMP,
@@ -627,9 +706,10 @@ def main():
                                   "peak": hbm, "unit": "GB/s",
                                   "frac": round(40 * nfluid / (ms_mp32 / KMP * 1e-3) / 1e9 / hbm, 4),
                                   "algorithmic_bytes_per_fluid_node": 40}},
-            "fp64": {"value": round(world * nfluid * KMP64 / (ms_mp64 * 1e-3) / 1e6, 2),
-                     "unit": "M fluid-node steps/s", "steps": KMP64,
-                     "ms_per_step": round(ms_mp64 / KMP64, 4)},
+            "fp64": {"value": round(world * nfluid * KMP64 / (ms_mp64f * 1e-3) / 1e6, 2),
+                     "unit": "M fluid-node steps/s", "steps": KMP64, "kernel": "fused",
+                     "ms_per_step": round(ms_mp64f / KMP64, 4),
+                     "strict": round(world * nfluid * KMP64 / (ms_mp64 * 1e-3) / 1e6, 2)},
             "tracer": "Db 0.01, K = e^2 (kd 0.01), adsorption on interfacial fluid nodes"},
         "e2e": {"value": round(world * nfluid * K / t_e2e / 1e6, 2), "unit": "MLUPS",
                 "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),

@@ -58,7 +58,12 @@ enum lbgpu_status {
 /* Storage / arithmetic of the flow and tracer populations. */
 enum lbgpu_precision {
     LBGPU_FP64 = 0,      /* plain FP64, the reference's arithmetic operation by operation */
-    LBGPU_FP32_DEV = 1   /* FP32 deviations f - w*rho0 with FP32 collision; FP64 sums */
+    LBGPU_FP32_DEV = 1,  /* FP32 deviations f - w*rho0 with FP32 collision; FP64 sums */
+    LBGPU_FP64_FUSED = 2 /* FP64 storage and arithmetic, the collision regrouped per pair of
+                            opposite velocities and evaluated with fused multiply-adds, and the
+                            tracer gathers fused: within 1e-12 relative of LBGPU_FP64, not
+                            bit-identical (the operator calls lbgpu_collide, lbgpu_moments and
+                            lbgpu_bounce_back_stream stay operation for operation) */
 };
 
 typedef struct {

@@ -15,9 +15,11 @@ from .lbgpu import (  # noqa: F401
     PnpParams,
     FP64,
     FP32_DEV,
+    FP64_FUSED,
     library,
     library_path,
 )
 
-__all__ = ["LbgpuError", "Box", "Params", "Tracer", "PnpParams", "FP64", "FP32_DEV", "library",
+__all__ = ["LbgpuError", "Box", "Params", "Tracer", "PnpParams", "FP64", "FP32_DEV", "FP64_FUSED",
+           "library",
            "library_path"]

@@ -80,6 +80,13 @@ LbConst64 make_const64(double tau)
     K.c1 = 1.0 - 1.0 / t;
     K.c2 = 1.0 / t;
     K.c3 = 1.0 - 1.0 / (2.0 * t);
+    for (int w = 0; w < 3; ++w) {
+        K.c2a0[w] = K.c2 * K.a0[w];
+        K.c2a1[w] = K.c2 * K.a1[w];
+        K.c2a2[w] = K.c2 * K.a2[w];
+        K.c2a2cs2[w] = K.c2a2[w] * csq;
+        K.c3a1[w] = K.c3 * K.a1[w];
+    }
     return K;
 }
 
@@ -106,6 +113,13 @@ void fill_args64(lbgpu_ctx *ctx, FlowArgs64 &a)
         s = s + (double)c.y * a.F[1];
         s = s + (double)c.z * a.F[2];
         a.cf[l] = s;
+    }
+    // LBGPU_FP64_FUSED: per pair of opposite velocities, c3 a1 (c.F) and c3 2 a2 (c.F)
+    a.fused = ctx->p.precision == LBGPU_FP64_FUSED;
+    for (int p = 0; p < 9; ++p) {
+        const int l = pair_l(p), w = wclass(l);
+        a.kF[p] = ctx->K64.c3a1[w] * a.cf[l];
+        a.kT[p] = ctx->K64.c3 * ctx->K64.two_a2[w] * a.cf[l];
     }
     a.err_bits = &ctx->d_scratch->err_bits;
     a.status = &ctx->d_scratch->status;
@@ -183,7 +197,7 @@ int lbgpu_create(const lbgpu_params *p, const int8_t *nature, lbgpu_ctx **out)
         return fail_global(LBGPU_ERR_INVALID, "lbgpu_create: lx, ly, lz must be > 0");
     if (!(p->relaxation_time >= 0.5))
         return fail_global(LBGPU_ERR_INVALID, "relaxation_time must be > 0.5");
-    if (p->precision != LBGPU_FP64 && p->precision != LBGPU_FP32_DEV)
+    if (p->precision != LBGPU_FP64 && p->precision != LBGPU_FP32_DEV && p->precision != LBGPU_FP64_FUSED)
         return fail_global(LBGPU_ERR_INVALID, "lbgpu_create: unknown precision");
     const long long N = (long long)p->lx * p->ly * p->lz;
     if (N >= (1LL << 31)) return fail_global(LBGPU_ERR_INVALID, "lbgpu_create: more than 2^31 nodes");

@@ -81,6 +81,9 @@ struct LbConst64 {
     double a0[3], a1[3], a2[3], two_a2[3];  // per weight class
     double k1, k0;                          // (1 - cs^2) and (0 - cs^2)
     double c1, c2, c3;                      // 1-1/tau, 1/tau, 1-1/(2 tau)
+    // the pair-symmetric collision of LBGPU_FP64_FUSED, per weight class: c2 a0, c2 a1, c2 a2,
+    // c2 a2 cs^2, c3 a1
+    double c2a0[3], c2a1[3], c2a2[3], c2a2cs2[3], c3a1[3];
 };
 
 // Device-resident control block of the reference flow loop (equilibration.f90:143-491).

@@ -29,6 +29,8 @@ struct FlowArgs64 {
     LbConst64 K;
     double F[3];                 // uniform force f_ext (fluid nodes)
     double cf[Q];                // c_l . f_ext in the reference's evaluation order
+    int fused;                   // LBGPU_FP64_FUSED: the pair-symmetric collision with FMAs
+    double kF[9], kT[9];         // per pair: c3 a1 (c.F), c3 2 a2 (c.F) (fused, uniform force)
 };
 
 // FP32-deviation arguments: populations stored as d = f - w*rho0 (float).

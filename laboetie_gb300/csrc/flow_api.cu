@@ -98,7 +98,7 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     LBG_CK(ctx, cudaEventCreate(&ctx->ev1));
     // per lattice node: nature, flag word, rho and j (FP64), and for FP64 two population sets;
     // FP32 populations are checked once the layout (A/B or fluid nodes only) is known
-    const size_t pop = p.precision == LBGPU_FP64 ? 2 * Q * sizeof(double) : 0;
+    const size_t pop = p.precision != LBGPU_FP32_DEV ? 2 * Q * sizeof(double) : 0;
     if (int rc = check_room(ctx, (size_t)N * (1 + 4 + pop + 4 * sizeof(double)) + (1 << 20))) return rc;
     LBG_CK(ctx, dalloc(&ctx->d_nature, N));
     LBG_CK(ctx, dalloc(&ctx->d_mask, N));
@@ -112,7 +112,7 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
     LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->counts[0] == 0)  // supercell_definition.f90:189-191
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
-    if (p.precision == LBGPU_FP64) {
+    if (p.precision != LBGPU_FP32_DEV) {
         for (int b = 0; b < 2; ++b) LBG_CK(ctx, dalloc(&ctx->d_f[b], (size_t)Q * N));
     } else {
         const char *mode = std::getenv("LBGPU_FP32_STREAMING");
@@ -208,7 +208,7 @@ namespace {
 
 int need_fp64(lbgpu_ctx *ctx, const char *fn)
 {
-    if (ctx->p.precision != LBGPU_FP64)
+    if (ctx->p.precision == LBGPU_FP32_DEV)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, std::string(fn) + ": needs an FP64 context");
     return LBGPU_OK;
 }

@@ -1,4 +1,5 @@
-// flow_f64.cu -- FP64 strict D3Q19 kernels (compiled with -fmad=false).
+// flow_f64.cu -- FP64 D3Q19 kernels (compiled with -fmad=false): the strict form, and the fused
+// step of LBGPU_FP64_FUSED (explicit fused multiply-adds, collide_node_fused).
 //
 // Bit-exactness with the reference.  Every product and sum is evaluated in the operand order
 // of the Fortran source with separate roundings (no fused multiply-add in this translation
@@ -120,6 +121,61 @@ __device__ __forceinline__ void collide_node(double (&n)[Q], const double rho, c
             r = r + K.c3 * T;
         }
         n[l] = r;
+    });
+}
+
+// LBGPU_FP64_FUSED: the same BGK + Guo collision regrouped per pair of opposite velocities
+// (l, inv l), where c.j, c.u and c.F change sign and nothing else does:
+//   n_l   <- c1 n_l   + (E + O),   n_inv <- c1 n_inv + (E - O)
+//   E = c2 [a0 rho + a2 ((c.j)(c.u) - cs^2 j.u)] + c3 [2 a2 (c.u)(c.F) - a1 u.F]
+//   O = c2 a1 (c.j) + c3 a1 (c.F)
+// evaluated with fused multiply-adds and one reciprocal of rho: about half the FP64 operations
+// of the operation-for-operation form, which bounds this kernel on GB300's FP64 pipe.  UCF: the
+// uniform f_ext, with c3 a1 (c.F) and c3 2 a2 (c.F) taken per pair from a.kF / a.kT.
+template <int FMASK, bool UCF>
+__device__ __forceinline__ void collide_node_fused(double (&n)[Q], const double rho, const double jx,
+                                                   const double jy, const double jz, const double fx,
+                                                   const double fy, const double fz,
+                                                   const FlowArgs64 &a)
+{
+    const LbConst64 &K = a.K;
+    const double ir = 1.0 / rho;
+    const double ux = jx * ir, uy = jy * ir, uz = jz * ir;
+    const double ju = __fma_rn(jx, ux, __fma_rn(jy, uy, jz * uz));
+    double base[3];
+#pragma unroll
+    for (int w = 0; w < 3; ++w) base[w] = __fma_rn(K.c2a0[w], rho, -(K.c2a2cs2[w] * ju));
+    if constexpr (FMASK != 0) {
+        const double uF = __fma_rn(ux, fx, __fma_rn(uy, fy, uz * fz));
+#pragma unroll
+        for (int w = 0; w < 3; ++w) base[w] = __fma_rn(-K.c3a1[w], uF, base[w]);
+    }
+    n[0] = __fma_rn(K.c1, n[0], base[0]);
+    static_for<0, 9>([&](auto P) {
+        constexpr int p = decltype(P)::value;
+        constexpr int l = pair_l(p);
+        constexpr int li = inv(l);
+        constexpr Vel c = vel(l);
+        constexpr int w = wclass(l);
+        const double cj = dotc<c.x, c.y, c.z>(jx, jy, jz);
+        const double cu = dotc<c.x, c.y, c.z>(ux, uy, uz);
+        double A = __fma_rn(K.c2a2[w], cj * cu, base[w]);
+        double B = K.c2a1[w] * cj;
+        if constexpr (FMASK != 0) {
+            double kT, kF;
+            if constexpr (UCF) {
+                kT = a.kT[p];
+                kF = a.kF[p];
+            } else {
+                const double cF = dotc<c.x, c.y, c.z>(fx, fy, fz);
+                kT = (K.c3 * K.two_a2[w]) * cF;
+                kF = K.c3a1[w] * cF;
+            }
+            A = __fma_rn(kT, cu, A);
+            B = B + kF;
+        }
+        n[l] = __fma_rn(K.c1, n[l], A + B);
+        n[li] = __fma_rn(K.c1, n[li], A - B);
     });
 }
 
@@ -269,7 +325,7 @@ __device__ void control_step(FlowCtl *c, double *hist)
     if (finish) c->done = 1;
 }
 
-template <int FMASK, bool FIELD, bool CHECK, bool REF>
+template <int FMASK, bool FIELD, bool CHECK, bool REF, bool FUSED>
 __global__ void __launch_bounds__(BLOCK) k_flow_step(const FlowArgs64 a)
 {
     int parity = a.parity, fm = a.force_moment, fc = a.force_collide;
@@ -313,8 +369,13 @@ __global__ void __launch_bounds__(BLOCK) k_flow_step(const FlowArgs64 a)
                 a.jy[node] = jy;
                 a.jz[node] = jz;
             }
-            if (fc) collide_node<FMASK, !FIELD>(n, rho, jx, jy, jz, fx, fy, fz, a);
-            else collide_node<0, true>(n, rho, jx, jy, jz, 0.0, 0.0, 0.0, a);
+            if constexpr (FUSED) {
+                if (fc) collide_node_fused<FMASK, !FIELD>(n, rho, jx, jy, jz, fx, fy, fz, a);
+                else collide_node_fused<0, true>(n, rho, jx, jy, jz, 0.0, 0.0, 0.0, a);
+            } else {
+                if (fc) collide_node<FMASK, !FIELD>(n, rho, jx, jy, jz, fx, fy, fz, a);
+                else collide_node<0, true>(n, rho, jx, jy, jz, 0.0, 0.0, 0.0, a);
+            }
 #pragma unroll
             for (int l = 0; l < Q; ++l) dst[(long long)l * N + node] = n[l];
         }
@@ -458,17 +519,33 @@ __global__ void __launch_bounds__(BLOCK) k_init(const FlowArgs64 a, const double
 
 unsigned grid_of(long long N) { return (unsigned)((N + BLOCK - 1) / BLOCK); }
 
-template <bool FIELD, bool CHECK, bool REF>
+template <bool FIELD, bool CHECK, bool REF, bool FUSED>
 cudaError_t step_dispatch(const FlowArgs64 &a, int fmask, unsigned grid, cudaStream_t s)
 {
     switch (fmask) {
-    case 0: k_flow_step<0, FIELD, CHECK, REF><<<grid, BLOCK, 0, s>>>(a); break;
-    case 1: k_flow_step<1, FIELD, CHECK, REF><<<grid, BLOCK, 0, s>>>(a); break;
-    case 2: k_flow_step<2, FIELD, CHECK, REF><<<grid, BLOCK, 0, s>>>(a); break;
-    case 4: k_flow_step<4, FIELD, CHECK, REF><<<grid, BLOCK, 0, s>>>(a); break;
-    default: k_flow_step<7, FIELD, CHECK, REF><<<grid, BLOCK, 0, s>>>(a); break;
+    case 0: k_flow_step<0, FIELD, CHECK, REF, FUSED><<<grid, BLOCK, 0, s>>>(a); break;
+    case 1: k_flow_step<1, FIELD, CHECK, REF, FUSED><<<grid, BLOCK, 0, s>>>(a); break;
+    case 2: k_flow_step<2, FIELD, CHECK, REF, FUSED><<<grid, BLOCK, 0, s>>>(a); break;
+    case 4: k_flow_step<4, FIELD, CHECK, REF, FUSED><<<grid, BLOCK, 0, s>>>(a); break;
+    default: k_flow_step<7, FIELD, CHECK, REF, FUSED><<<grid, BLOCK, 0, s>>>(a); break;
     }
     return cudaGetLastError();
+}
+
+template <bool FUSED>
+cudaError_t launch_step(const FlowArgs64 &a, int fmask, bool field, bool check, bool ref,
+                        unsigned grid, cudaStream_t s)
+{
+    if (field) {
+        // a per-node force field: every component may be non-zero
+        if (ref) k_flow_step<7, true, true, true, FUSED><<<grid, BLOCK, 0, s>>>(a);
+        else if (check) k_flow_step<7, true, true, false, FUSED><<<grid, BLOCK, 0, s>>>(a);
+        else k_flow_step<7, true, false, false, FUSED><<<grid, BLOCK, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    if (ref) return step_dispatch<false, true, true, FUSED>(a, fmask, grid, s);
+    return check ? step_dispatch<false, true, false, FUSED>(a, fmask, grid, s)
+                 : step_dispatch<false, false, false, FUSED>(a, fmask, grid, s);
 }
 
 }  // namespace
@@ -477,16 +554,8 @@ cudaError_t launch_flow_step_f64(const FlowArgs64 &a, int fmask, bool field, boo
                                  bool ref, unsigned grid, cudaStream_t s)
 {
     if (!grid) grid = grid_of(a.N);
-    if (field) {
-        // a per-node force field: every component may be non-zero
-        if (ref) k_flow_step<7, true, true, true><<<grid, BLOCK, 0, s>>>(a);
-        else if (check) k_flow_step<7, true, true, false><<<grid, BLOCK, 0, s>>>(a);
-        else k_flow_step<7, true, false, false><<<grid, BLOCK, 0, s>>>(a);
-        return cudaGetLastError();
-    }
-    if (ref) return step_dispatch<false, true, true>(a, fmask, grid, s);
-    return check ? step_dispatch<false, true, false>(a, fmask, grid, s)
-                 : step_dispatch<false, false, false>(a, fmask, grid, s);
+    return a.fused ? launch_step<true>(a, fmask, field, check, ref, grid, s)
+                   : launch_step<false>(a, fmask, field, check, ref, grid, s);
 }
 
 cudaError_t launch_collide_f64(const FlowArgs64 &a, int fmask, bool field, cudaStream_t s)

@@ -124,7 +124,7 @@ int lbgpu_set_force_field(lbgpu_ctx *ctx, const double *fx, const double *fy, co
     if (!ctx) return LBGPU_ERR_INVALID;
     if ((fx == nullptr) != (fy == nullptr) || (fy == nullptr) != (fz == nullptr))
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_set_force_field: give all three components or none");
-    if (ctx->p.precision != LBGPU_FP64)
+    if (ctx->p.precision == LBGPU_FP32_DEV)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_set_force_field: needs an FP64 context");
     if (!fx) {
         for (int d = 0; d < 3; ++d) {

@@ -52,6 +52,7 @@ struct MpArgs64 {
     double lw[3];
     const double *phi;
     double z, pstat;
+    int fused;                         // LBGPU_FP64_FUSED: the step's gathers as fused multiply-adds
 };
 
 struct MpArgs32 {

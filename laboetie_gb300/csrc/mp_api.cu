@@ -141,7 +141,8 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
     mp_release(ctx);
     MpState *s = new MpState();
     ctx->mp = s;
-    s->prec = ctx->p.precision;
+    // the fused FP64 mode runs the FP64 tracer with fused gathers (a64.fused)
+    s->prec = ctx->p.precision == LBGPU_FP32_DEV ? LBGPU_FP32_DEV : LBGPU_FP64;
     s->tr = *tr;
     s->K = K;
     s->ads = std::fabs(s->K) > EPS;
@@ -199,6 +200,7 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
     a.phi = d_phi;      // charged: exp(-z phi)/Pstat per node, fermi factors per link
     a.z = tr->z;
     a.pstat = Pstat;
+    a.fused = ctx->p.precision == LBGPU_FP64_FUSED;
     s->nblocks = (unsigned)((N + MP_BLOCK - 1) / MP_BLOCK);
     int zc = 0;
     const unsigned resident = s->prec == LBGPU_FP64 ? 0u : mp32_slab_resident();

@@ -168,6 +168,9 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_init(const MpArgs64 a)
 // module_moment_propagation.f90:164-289, one step.  Grid-stride over the nodes.  The gathers
 // are branch-free: a link to a solid neighbour has coefficient 0 and the neighbour's P is 0, so
 // it adds an exact zero where the reference skips it (only the sign of an exact zero can differ).
+// FUSED (LBGPU_FP64_FUSED): each link's gather and the remaining-fraction terms as fused
+// multiply-adds, in the same order (within 1e-12 relative of the separately rounded form).
+template <bool FUSED>
 __global__ void __launch_bounds__(MP_BLOCK) k_mp_step(const MpArgs64 a)
 {
     const volatile MpCtl *vc = a.ctl;
@@ -190,16 +193,26 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_step(const MpArgs64 a)
             constexpr Vel c = vel(l);
             const long long rp = X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1];
             const double cf = a.coef[(long long)(l - 1) * N + r];
-            n0 = n0 + Px[rp] * cf;
-            n1 = n1 + Py[rp] * cf;
-            n2 = n2 + Pz[rp] * cf;
+            if constexpr (FUSED) {
+                n0 = __fma_rn(Px[rp], cf, n0);
+                n1 = __fma_rn(Py[rp], cf, n1);
+                n2 = __fma_rn(Pz[rp], cf, n2);
+            } else {
+                n0 = n0 + Px[rp] * cf;
+                n1 = n1 + Py[rp] * cf;
+                n2 = n2 + Pz[rp] * cf;
+            }
         });
         const double p0 = Px[r], p1 = Py[r], p2 = Pz[r];
         v[0] = v[0] + p0 * a.us[0][r];
         v[1] = v[1] + p1 * a.us[1][r];
         v[2] = v[2] + p2 * a.us[2][r];
         const double frac = a.frac[r];
-        if (!a.ads || !(m & INTERFACIAL_BIT)) {
+        if (FUSED && (!a.ads || !(m & INTERFACIAL_BIT))) {
+            n0 = __fma_rn(frac, p0, n0);
+            n1 = __fma_rn(frac, p1, n1);
+            n2 = __fma_rn(frac, p2, n2);
+        } else if (!a.ads || !(m & INTERFACIAL_BIT)) {
             n0 = n0 + frac * p0;
             n1 = n1 + frac * p1;
             n2 = n2 + frac * p2;
@@ -245,7 +258,8 @@ cudaError_t launch_mp_init_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
 
 cudaError_t launch_mp_step_f64(const MpArgs64 &a, unsigned grid, cudaStream_t s)
 {
-    k_mp_step<<<grid, MP_BLOCK, 0, s>>>(a);
+    if (a.fused) k_mp_step<true><<<grid, MP_BLOCK, 0, s>>>(a);
+    else k_mp_step<false><<<grid, MP_BLOCK, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@ _LIB_PATH = os.path.join(HERE, "_build", "liblbgpu.so")
 
 FP64 = 0
 FP32_DEV = 1
+FP64_FUSED = 2
 
 STATUS = {
     1 << 0: "invalid argument", 1 << 1: "CUDA error", 1 << 2: "negative population",
