@@ -70,7 +70,7 @@ def args_():
     ap.add_argument("--precision-mp-steps", type=int, default=20000)
     # charged solutes: Poisson-Nernst-Planck, then flow and tracer in the charged geometry
     ap.add_argument("--no-charged", action="store_true")
-    ap.add_argument("--pnp-max-outer", type=int, default=200)
+    ap.add_argument("--pnp-max-outer", type=int, default=40000)
     ap.add_argument("--charged-flow-steps", type=int, default=5000)
     ap.add_argument("--charged-mp-steps", type=int, default=5000)
     ap.add_argument("--poisson-size", type=int, default=192)
@@ -290,15 +290,22 @@ def bench_precision(a):
 
 def bench_charged(a):
     """Charged solutes (slit 1x1x64 and touching spheres 48^3, surface charge -0.01 e per
-    interfacial solid node, bjl 0.4, lambda_D 4, D+- 0.05): the Poisson-Nernst-Planck loop with
-    the reference's Jacobi solver (bit-identical to the oracle) and with the 4-colour SOR
-    (omega 1.8, tol 1e-10), the SOR error on potential and ion densities against the reference
-    solver, then FP32 vs FP64 flow (f_ext 1e-6) and tracer VACF in the charged geometry for a
-    neutral tracer and for a charged one (z = +1) in the potential, which the reference stops on
-    (module_moment_propagation.f90:71-79) and this library computes with its formulas."""
+    interfacial solid node, bjl 0.4, lambda_D 4, D+- 0.05).
+
+    * Time to residual of one Poisson solve from the initial charges (phi = 0): the reference's
+      Jacobi (omega 1.4) and the multicolour SOR (omega 1.8), each to the reference's tolerance
+      (sum|phi* - phi| <= 1e-5 anormf0) and to 1e-10, with the residual of the result measured
+      the same way for both (lbgpu_poisson_residual).
+    * The Poisson-Nernst-Planck loop run to the reference's own convergence test
+      (poisson_nernst_planck.f90:38-48) with the reference's solver (bit-identical to the oracle)
+      and with the SOR at the reference's tolerance; the SOR's error on potential and ion
+      densities against the reference solver.
+    * FP32 vs FP64 flow (f_ext 1e-6) and tracer VACF in the charged geometry for a neutral tracer
+      and for a charged one (z = +1) in the potential, which the reference stops on
+      (module_moment_propagation.f90:71-79) and this library computes with its formulas."""
     from laboetie_gb300 import FP32_DEV, FP64, Box
     from laboetie_gb300 import geometry as geo
-    from laboetie_gb300.lbgpu import POISSON_REFERENCE, POISSON_SOR4
+    from laboetie_gb300.lbgpu import POISSON_JACOBI, POISSON_REFERENCE, POISSON_SOR4
 
     cases = [("slit 1x1x64", geo.slit(1, 1, 64)), ("touching spheres 48^3", geo.cc(48, 48, 48))]
     out = []
@@ -307,24 +314,41 @@ def bench_charged(a):
         with Box(nat) as box:
             inter = box.interfacial()
         sigma = -0.01 * int(((nat == 1) & (inter == 1)).sum())
+        # one Poisson solve from the initial charges, each solver to each tolerance
+        ttr = {}
+        for tol_name, tol in (("reference_tol_1e-5", float(np.float32(1.0e-5))), ("tol_1e-10", 1e-10)):
+            for sname, solver, om in (("jacobi", POISSON_JACOBI, 1.4), ("sor", POISSON_SOR4, 1.8)):
+                with Box(nat) as box:
+                    box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
+                                 solver=solver, omega=om, tol=tol)
+                    cp0, cm0, phi0, an0 = box.pnp_get()
+                    box.sor()                      # warm-up solve: captures the sweep graphs
+                    box.pnp_set(cp0, cm0, phi0, an0)
+                    t = time.perf_counter()
+                    it = box.sor()
+                    dt = time.perf_counter() - t
+                    resid, _ = box.poisson_residual()
+                ttr.setdefault(tol_name, {})[sname] = {
+                    "omega": om, "sweeps": it, "ms": round(dt * 1e3, 3),
+                    "residual_over_anormf0": resid / an0}
+        res["poisson_time_to_residual"] = ttr
         sol = {}
-        for sname, solver in (("reference_jacobi", POISSON_REFERENCE), ("sor4", POISSON_SOR4)):
+        for sname, solver in (("reference_jacobi", POISSON_REFERENCE), ("sor", POISSON_SOR4)):
             with Box(nat) as box:
                 box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
-                             solver=solver, omega=1.8, tol=1e-10)
+                             solver=solver, omega=1.8, tol=float(np.float32(1.0e-5)))
                 t = time.perf_counter()
                 outer, sweeps, rc = box.poisson_nernst_planck(max_outer=a.pnp_max_outer, check=False)
                 dt = time.perf_counter() - t
                 cp, cm, phi, an = box.pnp_get()
             sol[sname] = (cp, cm, phi, an)
             res[sname] = {"outer": outer, "sweeps": sweeps, "seconds": round(dt, 4), "status": rc,
+                          "converged": rc == 0,
                           "sweeps_per_s": round(sweeps / dt, 1) if dt > 0 else None}
-            if solver == POISSON_SOR4 and any(d % 2 for d in nat.shape):
-                res[sname]["note"] = "odd box side: the 4-colour solver runs as Jacobi with omega 1.4 and tol 1e-10"
         rel = lambda x, y: float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
-        r, q = sol["reference_jacobi"], sol["sor4"]
-        res["sor4_vs_reference"] = {"phi": rel(q[2], r[2]), "c_plus": rel(q[0], r[0]),
-                                    "c_minus": rel(q[1], r[1])}
+        r, q = sol["reference_jacobi"], sol["sor"]
+        res["sor_vs_reference"] = {"phi": rel(q[2], r[2]), "c_plus": rel(q[0], r[0]),
+                                   "c_minus": rel(q[1], r[1])}
         # tracers in the flow (f_ext 1e-6) of the charged geometry: a neutral one, and a charged
         # one (z = +1) in the reference solver's potential (lbgpu_mp_init_charged; the reference
         # itself stops on a charged tracer, module_moment_propagation.f90:71-79)
@@ -353,18 +377,21 @@ def bench_charged(a):
                                   "tracer": "Db 0.01, K = e (kd 0.01), in the reference solver's potential"})
         out.append(res)
     # Poisson sweep roofline on a large charged box: 4 x 8 B per node and sweep (phi read and
-    # written, c+ and c- read).  Tolerance 0, so every solve runs exactly its sweep cap; an odd box
-    # side selects the Jacobi kernel, an even one the 4-colour kernel.
+    # written, c+ and c- read).  Tolerance 0, so every solve runs exactly its sweep cap: the
+    # Jacobi sweep, the 4-colour SOR (even sides) and the general multicolour SOR (odd sides, 9
+    # colours).
     hbm, _ = peaks()
     sweeps = {}
-    for sname, L in (("jacobi", a.poisson_size - 1), ("sor4", a.poisson_size)):
+    for sname, L, solver in (("jacobi", a.poisson_size, POISSON_JACOBI), ("sor4", a.poisson_size, POISSON_SOR4),
+                             ("sor9_odd_box", a.poisson_size - 1, POISSON_SOR4)):
         nat = geo.cc(L, L, L)
         with Box(nat) as box:
             inter = box.interfacial()
         sigma = -0.01 * int(((nat == 1) & (inter == 1)).sum())
         with Box(nat) as box:
             box.pnp_init(bjl=0.4, sigma=sigma, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
-                         solver=POISSON_SOR4, omega=1.8, tol=0.0, max_iter=a.poisson_sweeps)
+                         solver=solver, omega=1.8 if solver == POISSON_SOR4 else 1.4, tol=0.0,
+                         max_iter=a.poisson_sweeps)
             for k in range(2):            # warm-up solve (captures the sweep graphs), timed solve
                 t = time.perf_counter()
                 try:

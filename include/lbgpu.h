@@ -364,9 +364,14 @@ int lbgpu_serve(lbgpu_batch *b, const lbgpu_request *requests, int n, double du_
 enum lbgpu_poisson_solver {
     LBGPU_POISSON_REFERENCE = 0,  /* sor.f90: over-relaxed Jacobi, omega 1.4, stop when
                                      sum|phi* - phi| <= 1e-5 * anormf0 (bit-identical sweeps) */
-    LBGPU_POISSON_SOR4 = 1        /* 4-colour SOR of the same discrete equation with the given
-                                     omega and tol (stop when sum|dphi| <= tol * anormf0); needs
-                                     even lx, ly, lz, otherwise Jacobi with omega 1.4 and tol */
+    LBGPU_POISSON_SOR4 = 1,       /* multicolour successive over-relaxation of the same discrete
+                                     equation with the given omega and tol: 4 colours when lx, ly,
+                                     lz are even, up to 9 otherwise (2 for a 1 x 1 x even column),
+                                     so any box shape is coloured; stops on the reference's
+                                     measure, sum|phi* - phi| <= tol * anormf0, with phi* the
+                                     Jacobi target at each node as it is updated */
+    LBGPU_POISSON_JACOBI = 2      /* the reference's Jacobi sweep with the given omega and tol
+                                     (stop when sum|phi* - phi| <= tol * anormf0) */
 };
 
 /* The lb.in tags of the charged system (charges_init.f90:23-134, poisson_nernst_planck.f90). */
@@ -375,7 +380,7 @@ typedef struct {
     int charge_distrib;   /* 0 = 'int' (charge on interfacial solid nodes); 1 = 'sol' (refused,
                              as the reference stops on it) */
     int solver;           /* enum lbgpu_poisson_solver */
-    double omega, tol;    /* LBGPU_POISSON_SOR4 only */
+    double omega, tol;    /* LBGPU_POISSON_SOR4 and LBGPU_POISSON_JACOBI */
     int max_iter;         /* sweeps per solve; 0 = the reference's 500 000 */
     int np_loop_bug;      /* 1: Nernst-Planck links start only on the line (i, ly, lz), as the
                              loop bounds of just_eq_smolu.f90:68-70 do; 0: every site */
@@ -396,6 +401,12 @@ int lbgpu_just_eq_smolu(lbgpu_ctx *ctx, int *iters);
 /* poisson_nernst_planck.f90:38-48 (until the relative changes of phi, c+ and c- are all below
  * 1e-12, or max_outer iterations: LBGPU_ERR_STEP_CAP), then charge_test.f90. */
 int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *sor_iters_total);
+
+/* The residual of the discrete Poisson equation at the current phi, without changing it:
+ * *residual = sum over every node of |phi* - phi| (phi* the Jacobi target of sor.f90:54-62), the
+ * quantity the reference's stopping test compares with 1e-5 * anormf0; *anormf0 (optional) is
+ * the state's normalisation.  Solvers are compared on it at equal tolerance. */
+int lbgpu_poisson_residual(lbgpu_ctx *ctx, double *residual, double *anormf0);
 
 /* charge_test.f90:15-24: charges on solid and fluid nodes; LBGPU_ERR_CHARGE if they differ from
  * sigma and -sigma by more than 1e-10. */

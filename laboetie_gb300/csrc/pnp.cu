@@ -65,7 +65,10 @@ struct PnpArgs {
     double factor, omega, one_minus_omega;
     double eDp, eDm;
     double delta_axis, delta_diag;
-    int color;        // 4-colour SOR
+    int color;        // multicolour SOR: the colour of this launch
+    int ncolor;       // colours per sweep (the last colour's launch decides the stopping test)
+    int gen;          // general colouring (some side odd): colour from k_sor_color_gen's rule
+    int kx, ky, kz;   // colours per axis of the general colouring (1, 2 or 3)
     int loop_bug;     // just_eq_smolu.f90:68-70
 };
 
@@ -164,10 +167,57 @@ __global__ void __launch_bounds__(PB) k_sor_jacobi(const PnpArgs a, double *phi0
     });
 }
 
-// One colour of the 4-colour SOR: phi <- (1-omega) phi + omega * 1.5 (sum_{l>0} w_l phi(x-c_l) + b).
-// The sum of |change| over the four colours is the stopping measure; colour 3 decides.  The
-// threads walk only the colour's N/4 nodes (even lx and ly): in plane z the colour holds the rows
-// y = 2j + (c1 ^ z&1) and in them the nodes x = 2i + (c0 ^ z&1), c0 and c1 the colour's bits.
+// Colour of a coordinate along one axis for the multicolour SOR: a proper colouring of the
+// periodic ring of L nodes (adjacent nodes, the wrap included, get different colours): 0 for a
+// one-wide axis (a step along it returns to the node itself), x mod 2 for even L, and x mod 2
+// with the last node coloured 2 for odd L.
+__device__ __forceinline__ int ring_colour(int x, int L)
+{
+    if (L == 1) return 0;
+    if ((L & 1) == 0) return x & 1;
+    return x == L - 1 ? 2 : (x & 1);
+}
+
+// Update of one node of the multicolour SOR: phi <- (1-omega) phi + omega * 1.5 (sum_{l>0} w_l
+// phi(x-c_l) + b); returns the node's part of the stopping measure, |phi* - phi| with phi* the
+// reference's Jacobi target sum_{l>=0} w_l phi(x-c_l) + b at the current state (the quantity the
+// reference's test sums, sor.f90:67,78), so both solvers stop on the same residual.
+__device__ __forceinline__ double sor_node(const PnpArgs &a, double *phi, int x, int y, int z, long long r)
+{
+    // this solver is not the reference's, so it may fuse: explicit multiply-adds (the file is
+    // built without contraction for the reference sweeps) halve its FP64 instructions
+    double s = 0.0;
+    static_for<1, Q>([&](auto L) {
+        constexpr int l = decltype(L)::value;
+        constexpr Vel c = vel(l);
+        s = __fma_rn(a.a0[wclass(l)], phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)], s);
+    });
+    const double rhs = __fma_rn(a.factor, a.cp[r] - a.cm[r], s);
+    const double old = phi[r];
+    phi[r] = __fma_rn(a.one_minus_omega, old, a.omega * (1.5 * rhs));
+    return fabs(__fma_rn(-a.a0[0] * 2.0, old, rhs));   // |phi* - phi| = |rhs - (2/3) phi|
+}
+
+// The colour's last launch of a sweep decides the stopping test of the multicolour SOR.
+__device__ __forceinline__ void sor_colour_done(const PnpArgs &a, const double (&tot)[3])
+{
+    PnpCtl *c = a.ctl;
+    c->anorm += tot[0];
+    if (a.color == a.ncolor - 1) {
+        c->iter += 1;
+        if (c->anorm <= c->limit) {
+            c->converged = 1;
+            c->done = 1;
+        } else if (c->iter >= c->max_iter) {
+            c->done = 1;
+        }
+        if (!c->done) c->anorm = 0.0;
+    }
+}
+
+// One colour of the 4-colour SOR of boxes with even sides ((x+z)&1 | ((y+z)&1)<<1): the threads
+// walk only the colour's N/4 nodes: in plane z the colour holds the rows y = 2j + (c1 ^ z&1) and
+// in them the nodes x = 2i + (c0 ^ z&1), c0 and c1 the colour's bits.
 __global__ void __launch_bounds__(PB) k_sor_color(const PnpArgs a, double *phi)
 {
     const volatile PnpCtl *vc = a.ctl;
@@ -181,34 +231,54 @@ __global__ void __launch_bounds__(PB) k_sor_color(const PnpArgs a, double *phi)
         const int x = 2 * (int)(k - q * hx) + ((a.color & 1) ^ zp);
         const int y = 2 * (int)(q - (long long)z * hy) + (((a.color >> 1) & 1) ^ zp);
         const long long r = x + (long long)a.lx * (y + (long long)a.ly * z);
-        // this solver is not the reference's, so it may fuse: explicit multiply-adds (the file is
-        // built without contraction for the reference sweeps) halve its FP64 instructions
-        double s = 0.0;
-        static_for<1, Q>([&](auto L) {
+        t[0] = t[0] + sor_node(a, phi, x, y, z, r);
+    }
+    grid_sum3(t, a.partial, &a.ctl->blocks_done, [&](const double (&tot)[3]) { sor_colour_done(a, tot); });
+}
+
+// One colour of the multicolour SOR of any box (some side odd or one wide).  With gx, gy, gz the
+// ring colours of the node's coordinates (kx, ky, kz colours each), the node's colour is
+// A + ka B, A = (gx + gz) mod ka, B = (gy + gz) mod kb, ka = max(kx, kz), kb = max(ky, kz).  For
+// fixed gz, A is one-to-one in gx, and for fixed gx in gz (likewise B), so every D3Q19 link
+// changes A or B: a step along x or xy changes A (gz fixed), along y B, along z, xz or yz the
+// sum with the unchanged coordinate; nodes of one colour never neighbour each other, and a
+// colour's launch can update them in place.  Up to 9 colours (all sides odd); a 1 x 1 x N
+// column needs 2 (N even) or 3.  Grid-stride over every node, updating those of the colour.
+__global__ void __launch_bounds__(PB) k_sor_color_gen(const PnpArgs a, double *phi)
+{
+    const volatile PnpCtl *vc = a.ctl;
+    if (vc->done) return;
+    double t[3] = {0.0, 0.0, 0.0};
+    const int ka = max(a.kx, a.kz), kb = max(a.ky, a.kz);
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        int x, y, z;
+        coords(r, a.lx, a.ly, x, y, z);
+        const int gx = ring_colour(x, a.lx), gy = ring_colour(y, a.ly), gz = ring_colour(z, a.lz);
+        const int colour = (gx + gz) % ka + ka * ((gy + gz) % kb);
+        if (colour != a.color) continue;
+        t[0] = t[0] + sor_node(a, phi, x, y, z, r);
+    }
+    grid_sum3(t, a.partial, &a.ctl->blocks_done, [&](const double (&tot)[3]) { sor_colour_done(a, tot); });
+}
+
+// Sum of the reference's stopping measure |phi* - phi| over every node at the current phi (no
+// update): the residual both solvers are compared on.
+__global__ void __launch_bounds__(PB) k_residual(const PnpArgs a, const double *phi)
+{
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < a.N; r += (long long)gridDim.x * PB) {
+        int x, y, z;
+        coords(r, a.lx, a.ly, x, y, z);
+        double phistar = 0.0;
+        static_for<0, Q>([&](auto L) {
             constexpr int l = decltype(L)::value;
             constexpr Vel c = vel(l);
-            s = __fma_rn(a.a0[wclass(l)], phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)], s);
+            phistar = phistar + a.a0[wclass(l)] * phi[nb(x, y, z, -c.x, -c.y, -c.z, a.lx, a.ly, a.lz)];
         });
-        const double target = 1.5 * __fma_rn(a.factor, a.cp[r] - a.cm[r], s);
-        const double old = phi[r];
-        const double nw = __fma_rn(a.one_minus_omega, old, a.omega * target);
-        phi[r] = nw;
-        t[0] = t[0] + fabs(nw - old);
+        phistar = phistar + a.factor * (a.cp[r] - a.cm[r]);
+        t[0] = t[0] + fabs(phistar - phi[r]);
     }
-    grid_sum3(t, a.partial, &a.ctl->blocks_done, [&](const double (&tot)[3]) {
-        PnpCtl *c = a.ctl;
-        c->anorm += tot[0];
-        if (a.color == 3) {
-            c->iter += 1;
-            if (c->anorm <= c->limit) {
-                c->converged = 1;
-                c->done = 1;
-            } else if (c->iter >= c->max_iter) {
-                c->done = 1;
-            }
-            if (!c->done) c->anorm = 0.0;
-        }
-    });
+    block_partial4(t, a.partial);
 }
 
 // Link flux of just_eq_smolu.f90:86-99 from site a (origin) to site b along direction l.
@@ -397,7 +467,8 @@ int lbgpu_pnp_init(lbgpu_ctx *ctx, const lbgpu_pnp_params *p, double *anormf0)
     const double eps = 2.220446049250313e-16;
     if (p->D_plus < 0.0) return ctx_fail(ctx, LBGPU_ERR_INVALID, "D_plus <0. critical.");
     if (p->D_minus < 0.0) return ctx_fail(ctx, LBGPU_ERR_INVALID, "D_minus <0. critical.");
-    if (p->solver != LBGPU_POISSON_REFERENCE && p->solver != LBGPU_POISSON_SOR4)
+    if (p->solver != LBGPU_POISSON_REFERENCE && p->solver != LBGPU_POISSON_SOR4 &&
+        p->solver != LBGPU_POISSON_JACOBI)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_pnp_init: unknown solver");
     pnp_release(ctx);
     PnpState *s = new PnpState();
@@ -516,8 +587,14 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
     }
     PnpArgs a;
     fill_pnp_args(ctx, a);
-    const bool four = s->p.solver == LBGPU_POISSON_SOR4 && ctx->p.lx % 2 == 0 && ctx->p.ly % 2 == 0 &&
-                      ctx->p.lz % 2 == 0;
+    const bool multi = s->p.solver == LBGPU_POISSON_SOR4;
+    const bool four = multi && ctx->p.lx % 2 == 0 && ctx->p.ly % 2 == 0 && ctx->p.lz % 2 == 0;
+    auto ring = [](int L) { return L == 1 ? 1 : (L % 2 == 0 ? 2 : 3); };
+    a.kx = ring(ctx->p.lx);
+    a.ky = ring(ctx->p.ly);
+    a.kz = ring(ctx->p.lz);
+    a.gen = multi && !four;
+    a.ncolor = four ? 4 : std::max(a.kx, a.kz) * std::max(a.ky, a.kz);
     PnpCtl c;
     std::memset(&c, 0, sizeof(c));
     c.parity = s->par;
@@ -526,7 +603,7 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
         c.limit = (double)1.0e-5f * s->anormf0;         // sor.f90:18,78
         c.max_iter = s->p.max_iter > 0 ? s->p.max_iter : 500000;
     } else {
-        a.omega = four ? s->p.omega : 1.4;
+        a.omega = s->p.omega;
         c.limit = s->p.tol * s->anormf0;
         c.max_iter = s->p.max_iter > 0 ? s->p.max_iter : 500000;
     }
@@ -541,11 +618,12 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
         cudaGraph_t g;
         LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int q = 0; q < G; ++q) {
-            if (four) {
-                for (int col = 0; col < 4; ++col) {
+            if (multi) {
+                for (int col = 0; col < a.ncolor; ++col) {
                     PnpArgs b = a;
                     b.color = col;
-                    k_sor_color<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
+                    if (four) k_sor_color<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
+                    else k_sor_color_gen<<<grid, PB, 0, st>>>(b, s->phi[s->par]);
                 }
             } else {
                 k_sor_jacobi<<<grid, PB, 0, st>>>(a, s->phi[0], s->phi[1]);
@@ -569,7 +647,7 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
     }
     if (e != cudaSuccess) return ctx_cuda(ctx, e, "lbgpu_sor");
     if (!four) s->par = c.parity;
-    if (iters) *iters = s->p.solver == LBGPU_POISSON_REFERENCE ? c.iter - 1 : c.iter;  // sor.f90:87
+    if (iters) *iters = s->p.solver == LBGPU_POISSON_SOR4 ? c.iter : c.iter - 1;  // sor.f90:87
     if ((rc = sum_abs_phi(ctx, &s->anormf0))) return rc;          // sor.f90:90
     if (!c.converged)
         return ctx_fail(ctx, LBGPU_ERR_STEP_CAP, "maximum iterations 500 000 reached without convergence in sor");
@@ -610,6 +688,23 @@ int lbgpu_just_eq_smolu(lbgpu_ctx *ctx, int *iters)
     }
     if (iters) *iters = iter;
     return lbgpu_sync(ctx);
+}
+
+int lbgpu_poisson_residual(lbgpu_ctx *ctx, double *residual, double *anormf0)
+{
+    if (!ctx || !residual) return LBGPU_ERR_INVALID;
+    int rc = need_pnp(ctx, "lbgpu_poisson_residual");
+    if (rc) return rc;
+    PnpState *s = ctx->pnp;
+    PnpArgs a;
+    fill_pnp_args(ctx, a);
+    const unsigned grid = grid_for(ctx->N);
+    k_residual<<<grid, PB, 0, ctx->stream>>>(a, s->phi[s->par]);
+    double r4[4];
+    if ((rc = read4(ctx, grid, r4))) return rc;
+    *residual = r4[0];
+    if (anormf0) *anormf0 = s->anormf0;
+    return LBGPU_OK;
 }
 
 int lbgpu_charge_test(lbgpu_ctx *ctx, double *solid_charge, double *fluid_charge)

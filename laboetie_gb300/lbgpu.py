@@ -120,6 +120,7 @@ def library():
         ("lbgpu_just_eq_smolu", [vp, pi]),
         ("lbgpu_poisson_nernst_planck", [vp, i, pi, pi]),
         ("lbgpu_charge_test", [vp, C.POINTER(d), C.POINTER(d)]),
+        ("lbgpu_poisson_residual", [vp, C.POINTER(d), C.POINTER(d)]),
         ("lbgpu_electrostatic_pot", [vp, vp]),
         ("lbgpu_comp_j", [vp, vp, vp, vp, vp]),
         ("lbgpu_smolu", [vp, i, i, vp, vp, vp, vp]),
@@ -365,6 +366,7 @@ Box.mp_release = lambda self: self._chk(self.L.lbgpu_mp_release(self.ctx), "mp_r
 
 POISSON_REFERENCE = 0
 POISSON_SOR4 = 1
+POISSON_JACOBI = 2
 
 
 def _pnp_init(self, bjl=0.4, sigma=0.0, lambda_D=4.0, D_plus=0.05, D_minus=0.05,
@@ -411,6 +413,13 @@ def _pnp(self, max_outer=0, check=True):
         return o.value, t.value, rc
     self._chk(rc, "poisson_nernst_planck")
     return o.value, t.value
+
+
+def _poisson_residual(self):
+    """(sum |phi* - phi| at the current phi, anormf0)."""
+    r, an = C.c_double(0), C.c_double(0)
+    self._chk(self.L.lbgpu_poisson_residual(self.ctx, C.byref(r), C.byref(an)), "poisson_residual")
+    return r.value, an.value
 
 
 def _charge_test(self):
@@ -480,6 +489,7 @@ Box.sor = _sor
 Box.just_eq_smolu = _just_eq_smolu
 Box.poisson_nernst_planck = _pnp
 Box.charge_test = _charge_test
+Box.poisson_residual = _poisson_residual
 
 
 def _compensated_force_field(self, particle_diameter=1, particle_coords=(0, 0, 0), geometry_label=0):

@@ -11,7 +11,7 @@ import pytest
 
 from laboetie_gb300 import Box, LbgpuError
 from laboetie_gb300 import geometry as geo
-from laboetie_gb300.lbgpu import POISSON_SOR4
+from laboetie_gb300.lbgpu import POISSON_JACOBI, POISSON_SOR4
 
 pytestmark = pytest.mark.gpu
 
@@ -125,3 +125,47 @@ def test_pnp_refusals():
             box.pnp_init(sigma=-0.02, charge_distrib="sol")   # charges_init.f90:96-100
         with pytest.raises(LbgpuError):
             box.pnp_init(sigma=-0.02, D_plus=-1.0)            # charges_init.f90:132
+
+
+# --------------------------------------------------------------- multicolour SOR on any box
+
+@pytest.mark.parametrize("name,make", [("slit64", lambda: geo.slit(1, 1, 64)),
+                                       ("slit63", lambda: geo.slit(1, 1, 63)),
+                                       ("cc9", lambda: geo.cc(9, 9, 9)),
+                                       ("cyl", lambda: geo.cylinder(9, 9, 4))])
+def test_multicolour_sor_on_any_box_reaches_the_fixed_point(oracle_mod, name, make):
+    nat = make()
+    sigma, cp, cm, phi, an, rho_ch = charged(oracle_mod, nat)
+    phi_o, _, _ = oracle_mod.sor(nat, sigma, BJL, cp, cm, phi, an, omega=1.4, tol=1e-14)
+    with Box(nat) as box:
+        box.pnp_init(bjl=BJL, sigma=sigma, lambda_D=LAMBDA_D, D_plus=DPM, D_minus=DPM,
+                     solver=POISSON_SOR4, omega=1.8, tol=1e-13)
+        it = box.sor()
+        _, _, gphi, _ = box.pnp_get()
+    assert it > 0
+    assert close(gphi, phi_o, 1e-9)
+
+
+@pytest.mark.parametrize("name,make", [("slit64", lambda: geo.slit(1, 1, 64)),
+                                       ("cc8", lambda: geo.cc(8, 8, 8))])
+def test_jacobi_with_the_reference_tolerance_is_the_reference_solver(oracle_mod, name, make):
+    """LBGPU_POISSON_JACOBI with omega 1.4 and tol = the reference's 1.0e-5 (a default real)
+    sweeps exactly as the reference solver; the residual query returns the reference's stopping
+    measure at the final potential."""
+    from oracle import np_oracle as npo
+
+    nat = make()
+    sigma, cp, cm, phi, an, rho_ch = charged(oracle_mod, nat)
+    phi_o, an_o, it_o = oracle_mod.sor(nat, sigma, BJL, cp, cm, phi, an)
+    with Box(nat) as box:
+        box.pnp_init(bjl=BJL, sigma=sigma, lambda_D=LAMBDA_D, D_plus=DPM, D_minus=DPM,
+                     solver=POISSON_JACOBI, omega=1.4, tol=float(np.float32(1e-5)))
+        it = box.sor()
+        _, _, gphi, gan = box.pnp_get()
+        res, _ = box.poisson_residual()
+    assert it == it_o and np.array_equal(gphi, phi_o) and gan == an_o
+    # the measure restated on the host: sum |phi* - phi| with phi* = sum_l w_l phi(x - c_l) + b
+    factor = 4.0 * npo.PI * BJL * npo.KBT / 2.0
+    star = sum(npo.A0[l] * npo._shift(phi_o, npo.C[l]) for l in range(19)) + factor * (cp - cm)
+    want = np.abs(star - phi_o).sum()
+    assert abs(res - want) <= 1e-12 * want
