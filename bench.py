@@ -61,8 +61,8 @@ def args_():
     ap.add_argument("--batch-flow-steps", type=int, default=10000)
     ap.add_argument("--batch-mp-steps", type=int, default=10000)
     ap.add_argument("--batch-chunk", type=int, default=500, help="steps per call (one CUDA graph)")
-    ap.add_argument("--one-at-a-time-sample", type=int, default=6,
-                    help="cells (and a third as many tubes) timed one at a time")
+    ap.add_argument("--one-at-a-time-fraction", type=float, default=0.1,
+                    help="share of the cells and of the tubes timed one at a time (evenly spaced)")
     # FP32 error statement (permeability, D_eff, adsorbed fraction, retention time) vs FP64
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--precision-size", type=int, default=64)
@@ -416,7 +416,9 @@ def bench_charged(a):
 def bench_batched(a):
     """1024 chromatography cells + 64 tubes in one batch: flow steps, tracer start, tracer steps.
     Wall-clock solves/s through the public API, against the same solves one at a time through
-    the single-box API (a timed sample, extrapolated per family)."""
+    the single-box API (an evenly spaced sample of at least a tenth of each family, timed in
+    full and scaled to the family by fluid nodes).  Also the tuner's choices and the roofline of
+    the tiled in-place step (152 B per fluid node of the tiled boxes over the launch time)."""
     from laboetie_gb300 import FP32_DEV, Box
     from laboetie_gb300 import workloads as wl
     from laboetie_gb300.lbgpu import Batch
@@ -445,11 +447,15 @@ def bench_batched(a):
     dt = time.perf_counter() - t0
     v0, vs, _, st = b.mp_get(ids[0])
     deff_cell0 = (v0 / 2 + vs).tolist()
+    tuning = b.tuning()
     b.close()
-    # one at a time through the single-box API: a sample of each family, extrapolated
+    # one at a time through the single-box API: an evenly spaced sample of each family
     fam = {"cell": [], "tube": []}
-    ns = a.one_at_a_time_sample
-    sample = [c for c in cells if c[2] == "cell"][:ns] + [c for c in cells if c[2] == "tube"][:(max(1, ns // 3) if ns else 0)]
+    sample = []
+    for f in ("cell", "tube"):
+        members = [c for c in cells if c[2] == f]
+        k = max(1, math.ceil(a.one_at_a_time_fraction * len(members))) if members and a.one_at_a_time_fraction > 0 else 0
+        sample += [members[int(q * len(members) / k)] for q in range(k)]
     for n, fe, f in sample:
         nf = int((n == 0).sum())
         t = time.perf_counter()
@@ -470,10 +476,12 @@ def bench_batched(a):
     one = None
     if t_one > 0:
         one = {"value": round(n_solves / t_one, 3), "unit": "solves/s",
-               "sample": f"{len(fam['cell'])} cells + {len(fam['tube'])} tubes timed through "
-                         "lbgpu_flow_steps/lbgpu_mp_propagate one box at a time, "
-                         "extrapolated per family by fluid nodes",
-               "seconds_extrapolated": round(t_one, 2)}
+               "sample": f"{len(fam['cell'])} of {sum(1 for c in cells if c[2] == 'cell')} cells + "
+                         f"{len(fam['tube'])} of {sum(1 for c in cells if c[2] == 'tube')} tubes "
+                         "(evenly spaced), each solved in full through lbgpu_flow_steps/"
+                         "lbgpu_mp_propagate one box at a time; the family time scaled by fluid nodes",
+               "sample_seconds": round(sum(x[0] for f in fam for x in fam[f]), 2),
+               "seconds_scaled": round(t_one, 2)}
     return {
         "metric": "batched solves/s", "value": round(n_solves / dt, 3), "unit": "solves/s",
         "seconds": round(dt, 3), "solves": n_solves,
@@ -486,8 +494,25 @@ def bench_batched(a):
                    "smem_boxes": info["smem_boxes"], "bytes": info["bytes"]},
         "one_at_a_time": one,
         "speedup_vs_one_at_a_time": round(t_one / dt, 2) if one else None,
+        "tuning": tuning,
+        "roofline_tiled_flow": batch_roofline(tuning),
         "d_eff_cell0": deff_cell0,
     }
+
+
+def batch_roofline(t):
+    """HBM roofline of the tiled in-place flow step, from the tuner's timing of the chosen
+    variants: 152 algorithmic bytes per fluid node of the tiled boxes over the mean of the even and
+    the odd launch."""
+    if not t.get("tuned") or not t.get("tiled_fluid_nodes"):
+        return None
+    hbm, kind = peaks()
+    ms = 0.5 * (t["aa_ms"][0] + t["aa_ms"][1])
+    gbs = BYTES_F32 * t["tiled_fluid_nodes"] / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(gbs / hbm, 4), "peak_kind": kind, "ms_per_launch": round(ms, 5),
+            "algorithmic_bytes_per_fluid_node": BYTES_F32,
+            "note": "timed by the batch tuner on the tiled boxes alone (the 64 tubes)"}
 
 
 def bench_serving(a):

@@ -329,6 +329,25 @@ int lbgpu_batch_mp_fields(lbgpu_batch *b, int id, double *P, double *P_ads);
 int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *smem_boxes,
                      size_t *bytes_used);
 
+/* The batch tuner's choices.  The first call that holds at least 1024 flow-phase tiles times, on
+ * scratch copies of the tiled boxes (their state does not advance), every variant of the even
+ * and of the odd in-place step launch: one block per 256-node tile at 3..6 resident blocks per
+ * SM, or a persistent work list (4..6 blocks per SM claiming 1, 2 or 4 tiles at a time from an
+ * atomic ticket), and keeps the fastest; then the steps per CUDA graph (8, 32, 128 or 512: the
+ * smallest within 1 % of the fastest); the first call with at least 64 shared-memory boxes picks
+ * their block size. */
+typedef struct {
+    int tuned;                    /* 1 once the tiled launches were tuned */
+    int aa_work_list[2];          /* even, odd launch: 1 persistent work list, 0 block per tile */
+    int aa_min_blocks[2];         /* resident blocks per SM of the chosen variant */
+    int aa_tiles_per_claim[2];    /* tiles a work-list block claims at a time */
+    int smem_threads;             /* threads per shared-memory-resident box */
+    int steps_per_graph;          /* steps of one CUDA graph (0: one graph per call) */
+    float aa_ms[2];               /* time of one launch of the chosen variant when tuned */
+    long long tiled_fluid_nodes;  /* fluid nodes of the flow-phase tiled boxes it was timed on */
+} lbgpu_batch_tuning;
+int lbgpu_batch_get_tuning(lbgpu_batch *b, lbgpu_batch_tuning *out);
+
 typedef struct {
     lbgpu_cell cell;
     const int8_t *nature;   /* the caller keeps it alive until lbgpu_serve returns */

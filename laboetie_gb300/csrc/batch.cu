@@ -12,6 +12,7 @@
 // so a box gives the same result alone and in any mix, and in either path.  The tracer is the
 // single box's FP32 difference form (mp_f32.cu) with the same helpers and link order in every
 // path, so a batched box's P is bit-identical to a single box's on the same flow moments.
+#include <algorithm>
 #include <cfloat>
 
 #include "batch.h"
@@ -336,6 +337,54 @@ __global__ void __launch_bounds__(BATCH_BLOCK, MINB) k_batch_aa(const BatchInst 
     if (i < I.Nf) aa_node_compact<ODD>(I, i, soff);
 }
 
+// Persistent work-list forms of the tiled launches: a fixed grid of blocks (a few per SM) claims
+// `tpc` consecutive tiles at a time from an atomic ticket until the list is used up, so blocks
+// that draw cheap tiles (few fluid lanes) take more of them.  The last block to leave resets the
+// ticket for the next launch of the stream; no block ever waits on another.  Per tile the work
+// is the one-block-per-tile launch's, so the results are bit-identical to it.
+__device__ __forceinline__ bool claim_tiles(BatchTicket *tk, int ntiles, int tpc, unsigned &b0, unsigned &b1)
+{
+    __shared__ unsigned base;
+    __syncthreads();   // every thread has read the previous claim
+    if (threadIdx.x == 0) base = atomicAdd(&tk->next, (unsigned)tpc);
+    __syncthreads();
+    b0 = base;
+    if (b0 >= (unsigned)ntiles) return false;
+    b1 = min(b0 + (unsigned)tpc, (unsigned)ntiles);
+    return true;
+}
+
+__device__ __forceinline__ void release_ticket(BatchTicket *tk)
+{
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&tk->done, 1u) == gridDim.x - 1) {   // every block has made its last claim
+            tk->next = 0u;
+            tk->done = 0u;
+            __threadfence();
+        }
+    }
+}
+
+template <bool ODD, int MINB>
+__global__ void __launch_bounds__(BATCH_BLOCK, MINB) k_batch_aa_list(const BatchInst *__restrict__ insts,
+                                                                     const BatchTile *__restrict__ tiles,
+                                                                     int ntiles, int tpc, BatchTicket *tk)
+{
+    __shared__ unsigned soff[ODD ? Q : 1][BATCH_BLOCK];
+    unsigned b0, b1;
+    while (claim_tiles(tk, ntiles, tpc, b0, b1)) {
+        for (unsigned k = b0; k < b1; ++k) {
+            // odd launches walk the list from its end, as the one-block-per-tile form does
+            const BatchTile t = tiles[ODD ? (unsigned)ntiles - 1u - k : k];
+            const BatchInst &I = insts[t.inst];
+            const unsigned i = (unsigned)t.start + threadIdx.x;
+            if (i < I.Nf) aa_node_compact<ODD>(I, i, soff);
+        }
+    }
+    release_ticket(tk);
+}
+
 // One tracer step of every tiled box in the tracer phase; with INIT (one box, the tiles of
 // `inst` in order), the start of its tracer phase.  Each tile keeps its own running sums.
 template <bool INIT>
@@ -387,6 +436,49 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp(const BatchInst *__res
     if constexpr (INIT) {
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status_word(I), (unsigned)LBGPU_ERR_FRACTION);
     }
+}
+
+// The work-list form of the tiled tracer step (see k_batch_aa_list).
+__global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_list(const BatchInst *__restrict__ insts,
+                                                               const BatchTile *__restrict__ tiles,
+                                                               int ntiles, int tpc, int par, BatchTicket *tk)
+{
+    unsigned b0, b1;
+    while (claim_tiles(tk, ntiles, tpc, b0, b1)) {
+        for (unsigned kt = b0; kt < b1; ++kt) {
+            const BatchTile t = tiles[kt];
+            const BatchInst &I = insts[t.inst];
+            const unsigned k = (unsigned)t.start + threadIdx.x;
+            float vt32[3] = {0.0f, 0.0f, 0.0f};
+            unsigned bad = 0;
+            if (k < batch_units(I)) {
+                uint32_t m;
+                unsigned r;
+                int x, y, z;
+                if (I.compact) {
+                    m = __ldg(I.cmask + k);
+                    r = compact_xyz(I, __ldg(I.cpos + k), x, y, z);
+                } else {
+                    m = __ldg(I.mask + k);
+                    r = k;
+                    lattice_xyz(I, r, x, y, z);
+                }
+                if (m & FLUID_BIT)
+                    mp_node<false>(I.V, I.P[par], I.P[par ^ 1], I.A[par], I.A[par ^ 1], I.aux, r, x, y, z, m, I,
+                                   vt32, bad);
+            }
+            double vt[3] = {(double)vt32[0], (double)vt32[1], (double)vt32[2]};
+            block_sum3(vt);
+            if (threadIdx.x == 0) {
+                double *acc = I.tacc + (size_t)(t.start / BATCH_BLOCK) * BATCH_TACC;
+                for (int d = 0; d < 3; ++d) {
+                    acc[3 + d] += vt[d];
+                    acc[6 + d] = vt[d];
+                }
+            }
+        }
+    }
+    release_ticket(tk);
 }
 
 // One tracer step of the slab tiles of boxes in the tracer phase (mp_slab.cuh); each tile keeps
@@ -608,6 +700,35 @@ cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int 
 {
     if (ntiles <= 0) return cudaSuccess;
     k_batch_mp<false><<<ntiles, BATCH_BLOCK, 0, s>>>(insts, tiles, 0, par);
+    return cudaGetLastError();
+}
+
+template <int MINB>
+static void batch_aa_list(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int grid,
+                          int tpc, BatchTicket *tk, cudaStream_t s)
+{
+    if (odd) k_batch_aa_list<true, MINB><<<grid, BATCH_BLOCK, 0, s>>>(insts, tiles, ntiles, tpc, tk);
+    else k_batch_aa_list<false, MINB><<<grid, BATCH_BLOCK, 0, s>>>(insts, tiles, ntiles, tpc, tk);
+}
+
+cudaError_t launch_batch_aa_list(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int minb,
+                                 int grid, int tpc, BatchTicket *tk, cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    grid = std::max(1, std::min(grid, (ntiles + tpc - 1) / tpc));
+    if (minb <= 3) batch_aa_list<3>(insts, tiles, ntiles, odd, grid, tpc, tk, s);
+    else if (minb == 4) batch_aa_list<4>(insts, tiles, ntiles, odd, grid, tpc, tk, s);
+    else if (minb == 5) batch_aa_list<5>(insts, tiles, ntiles, odd, grid, tpc, tk, s);
+    else batch_aa_list<6>(insts, tiles, ntiles, odd, grid, tpc, tk, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_mp_list(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par, int grid,
+                                 int tpc, BatchTicket *tk, cudaStream_t s)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    grid = std::max(1, std::min(grid, (ntiles + tpc - 1) / tpc));
+    k_batch_mp_list<<<grid, BATCH_BLOCK, 0, s>>>(insts, tiles, ntiles, tpc, par, tk);
     return cudaGetLastError();
 }
 

@@ -65,12 +65,23 @@ struct BatchTile {
     int start;  // first node of the tile
 };
 
+// Work-list ticket of the persistent tiled launches: next tile to claim, blocks that left.
+struct BatchTicket {
+    unsigned next, done;
+};
+
 // one AA launch over the tiles of the tiled boxes (compact layout); minb: 3..6 resident blocks
 cudaError_t launch_batch_aa(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int minb,
                             cudaStream_t s);
+// the same as a persistent work list: `grid` blocks claim `tpc` tiles at a time from the ticket tk
+// (zero before the first launch; the last block of each launch zeroes it again)
+cudaError_t launch_batch_aa_list(const BatchInst *insts, const BatchTile *tiles, int ntiles, bool odd, int minb,
+                                 int grid, int tpc, BatchTicket *tk, cudaStream_t s);
 // one tracer step of the tiled boxes: P[par] -> P[par^1]
 cudaError_t launch_batch_mp(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
                             cudaStream_t s);
+cudaError_t launch_batch_mp_list(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par, int grid,
+                                 int tpc, BatchTicket *tk, cudaStream_t s);
 // the same for boxes with slab tiles (tile start = slab tile index within the box)
 cudaError_t launch_batch_mp_slab(const BatchInst *insts, const BatchTile *tiles, int ntiles, int par,
                                  cudaStream_t s);

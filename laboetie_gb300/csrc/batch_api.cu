@@ -130,6 +130,14 @@ struct lbgpu_batch {
     unsigned *d_du = nullptr;
     int cap_du = 0;
     int aa_minb[2] = {4, 5};      // resident blocks per SM of the even / odd AA launches
+    // work-list form of the even / odd AA launch (a persistent grid claiming tiles from a ticket)
+    // and the tiles a block claims at a time; 0: one block per tile
+    int aa_list[2] = {0, 0}, aa_tpc[2] = {1, 1};
+    float aa_ms[2] = {0.0f, 0.0f};    // measured time of one launch of the chosen variants
+    long long tuned_fluid = 0;        // fluid nodes of the flow-phase tiled boxes they were timed on
+    int steps_per_graph = 0;          // 0: one graph per call (before the tuner ran)
+    int sms = 0;
+    BatchTicket *d_ticket = nullptr;
     bool aa_tuned = false;
     bool smem_tuned = false;
     std::vector<int> desc_slot;   // descriptor index -> slot
@@ -261,6 +269,18 @@ int rebuild(lbgpu_batch *b)
     return LBGPU_OK;
 }
 
+// One AA launch of the flow-phase tiles in the variant the tuner chose (descriptors insts: the
+// batch's, or the tuner's scratch copies).
+int launch_aa(lbgpu_batch *b, const BatchInst *insts, int odd, cudaStream_t s)
+{
+    if (b->aa_list[odd])
+        LBB_CK(launch_batch_aa_list(insts, b->d_tiles, b->nflow, odd, b->aa_minb[odd], b->sms * b->aa_minb[odd],
+                                    b->aa_tpc[odd], b->d_ticket, s));
+    else
+        LBB_CK(launch_batch_aa(insts, b->d_tiles, b->nflow, odd, b->aa_minb[odd], s));
+    return LBGPU_OK;
+}
+
 // The launches of one call: the shared-memory boxes on the side stream, concurrently with the
 // per-step launches of the tiled boxes on the main stream.
 int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
@@ -275,7 +295,7 @@ int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
         LBB_CK(cudaEventRecord(b->join, b->side));
     }
     for (int t = 0; t < nsteps; ++t) {
-        LBB_CK(launch_batch_aa(b->d_insts, b->d_tiles, b->nflow, t & 1, b->aa_minb[t & 1], s));
+        if (int rc = launch_aa(b, b->d_insts, t & 1, s)) return rc;
         LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
         LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, s));
     }
@@ -316,14 +336,34 @@ int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
     return LBGPU_OK;
 }
 
-// Launch-bound tuner of the tiled AA launches: the first time a batch holds at least 1024 flow
-// tiles, every variant (3..6 resident blocks per SM) of the even and of the odd launch is timed
-// on scratch copies of the tiled boxes' populations (a second descriptor table points at them;
-// the boxes' state is not advanced) and the fastest is kept for the batch's lifetime.
-// LBGPU_BATCH_AA_MINB=<even>,<odd> fixes the variants instead.
+// Tuner of the tiled AA launches: the first time a batch holds at least 1024 flow tiles, every
+// variant of the even and of the odd launch is timed on scratch copies of the tiled boxes'
+// populations (a second descriptor table points at them; the boxes' state is not advanced) and
+// the fastest is kept for the batch's lifetime: one block per tile at 3..6 resident blocks per
+// SM, or the persistent work list (4..6 blocks per SM claiming 1, 2 or 4 tiles at a time from an
+// atomic ticket).  It then picks the steps per graph (see below).
+// LBGPU_BATCH_AA_MINB=<even>,<odd> fixes one-block-per-tile variants instead, and
+// LBGPU_BATCH_AA_LIST=<blocks per SM>,<tiles per claim>[,<steps per graph>] the work-list form
+// of both launches (for any number of tiles).
 int tune_aa(lbgpu_batch *b)
 {
-    if (b->aa_tuned || b->nflow < 1024) return LBGPU_OK;
+    if (b->aa_tuned) return LBGPU_OK;
+    if (const char *e = std::getenv("LBGPU_BATCH_AA_LIST")) {
+        int minb = 0, tpc = 0, spg = 0;
+        const int n = std::sscanf(e, "%d,%d,%d", &minb, &tpc, &spg);
+        if (n >= 2 && minb >= 3 && minb <= 6 && tpc >= 1) {
+            b->aa_tuned = true;
+            for (int k = 0; k < 2; ++k) {
+                b->aa_list[k] = 1;
+                b->aa_minb[k] = minb;
+                b->aa_tpc[k] = tpc;
+            }
+            if (n == 3 && spg > 0 && spg % 2 == 0) b->steps_per_graph = spg;
+            drop_graphs(b);
+            return LBGPU_OK;
+        }
+    }
+    if (b->nflow < 1024) return LBGPU_OK;
     b->aa_tuned = true;
     if (const char *e = std::getenv("LBGPU_BATCH_AA_MINB")) {
         int ev = 0, od = 0;
@@ -357,21 +397,81 @@ int tune_aa(lbgpu_batch *b)
         off += (size_t)Q * d.Nf;
     }
     LBB_CK(cudaMemcpyAsync(d_tmp, descs.data(), sizeof(BatchInst) * descs.size(), cudaMemcpyHostToDevice, s));
+    // candidates of each launch: one block per tile at 3..6 resident blocks per SM, and the
+    // persistent work list at 4..6 blocks per SM claiming 1, 2 or 4 tiles at a time
+    struct Cand {
+        int list, minb, tpc;
+    };
+    std::vector<Cand> cands;
+    for (int minb = 3; minb <= 6; ++minb) cands.push_back({0, minb, 1});
+    for (int minb = 4; minb <= 6; ++minb)
+        for (int tpc : {1, 2, 4}) cands.push_back({1, minb, tpc});
+    long long fluid = 0;
+    for (const auto &d : descs)
+        if (d.compact && d.phase == BATCH_FLOW) fluid += d.Nf;
     for (int odd = 0; odd < 2; ++odd) {
         float best = 1e30f;
-        for (int minb = 3; minb <= 6; ++minb) {
-            for (int k = 0; k < 2; ++k) LBB_CK(launch_batch_aa(d_tmp, b->d_tiles, b->nflow, odd, minb, s));
+        Cand keep = cands[0];
+        for (const Cand &c : cands) {
+            b->aa_list[odd] = c.list;
+            b->aa_minb[odd] = c.minb;
+            b->aa_tpc[odd] = c.tpc;
+            for (int k = 0; k < 2; ++k)
+                if (int rc = launch_aa(b, d_tmp, odd, s)) return rc;
             LBB_CK(cudaEventRecord(b->ev0, s));
-            for (int k = 0; k < 6; ++k) LBB_CK(launch_batch_aa(d_tmp, b->d_tiles, b->nflow, odd, minb, s));
+            for (int k = 0; k < 6; ++k)
+                if (int rc = launch_aa(b, d_tmp, odd, s)) return rc;
             LBB_CK(cudaEventRecord(b->ev1, s));
             LBB_CK(cudaEventSynchronize(b->ev1));
             float ms = 0.0f;
             LBB_CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
             if (ms < best) {
                 best = ms;
-                b->aa_minb[odd] = minb;
+                keep = c;
             }
         }
+        b->aa_list[odd] = keep.list;
+        b->aa_minb[odd] = keep.minb;
+        b->aa_tpc[odd] = keep.tpc;
+        b->aa_ms[odd] = best / 6.0f;
+    }
+    b->tuned_fluid = fluid;
+    // steps per graph: a call's steps run as graphs of S steps (the last one holds the rest); S
+    // is the smallest of 8, 32, 128, 512 whose 512 steps (AA launches on the scratch copies) take
+    // no more than 1 % longer than the fastest S (graph launches cost a few microseconds, while
+    // a smaller S lets the host act sooner on a long call)
+    {
+        float tS[4];
+        const int Ss[4] = {8, 32, 128, 512};
+        for (int q = 0; q < 4; ++q) {
+            cudaGraph_t g;
+            cudaGraphExec_t ex;
+            LBB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int rc = LBGPU_OK;
+            for (int t = 0; t < Ss[q] && !rc; ++t) rc = launch_aa(b, d_tmp, t & 1, s);
+            const cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (rc) {
+                if (ce == cudaSuccess) cudaGraphDestroy(g);
+                return rc;
+            }
+            LBB_CK(ce);
+            const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            LBB_CK(ie);
+            LBB_CK(cudaGraphLaunch(ex, s));   // warm-up
+            LBB_CK(cudaEventRecord(b->ev0, s));
+            for (int k = 0; k < 512 / Ss[q]; ++k) LBB_CK(cudaGraphLaunch(ex, s));
+            LBB_CK(cudaEventRecord(b->ev1, s));
+            LBB_CK(cudaEventSynchronize(b->ev1));
+            LBB_CK(cudaEventElapsedTime(&tS[q], b->ev0, b->ev1));
+            cudaGraphExecDestroy(ex);
+        }
+        const float fastest = *std::min_element(tS, tS + 4);
+        for (int q = 0; q < 4; ++q)
+            if (tS[q] <= 1.01f * fastest) {
+                b->steps_per_graph = Ss[q];
+                break;
+            }
     }
     LBB_CK(cudaFreeAsync(scratch, s));
     LBB_CK(cudaFreeAsync(d_tmp, s));
@@ -445,14 +545,27 @@ int tune_smem(lbgpu_batch *b)
     return LBGPU_OK;
 }
 
+// A call's steps run as graphs of steps_per_graph steps (the tuner's choice), the last one with
+// the rest and the convergence check.  launch = false only captures the graphs.
+int call_graphs(lbgpu_batch *b, int nsteps, bool check, bool launch)
+{
+    const int S = b->steps_per_graph > 0 ? b->steps_per_graph : nsteps;
+    int left = nsteps;
+    while (left > 0) {
+        const int n = left > S ? S : left;
+        left -= n;
+        cudaGraphExec_t exec = nullptr;
+        if (int rc = graph_of(b, n, check && left == 0, &exec)) return rc;
+        if (launch) LBB_CK(cudaGraphLaunch(exec, b->stream));
+    }
+    return LBGPU_OK;
+}
+
 int run_steps(lbgpu_batch *b, int nsteps, bool check)
 {
     if (int rc = tune_aa(b)) return rc;
     if (int rc = tune_smem(b)) return rc;
-    cudaGraphExec_t exec = nullptr;
-    int rc = graph_of(b, nsteps, check, &exec);
-    if (rc) return rc;
-    LBB_CK(cudaGraphLaunch(exec, b->stream));
+    if (int rc = call_graphs(b, nsteps, check, true)) return rc;
     for (auto &sl : b->slots)
         if (sl.active && sl.d.phase == BATCH_MP) sl.mp_steps += nsteps;
     return LBGPU_OK;
@@ -508,6 +621,9 @@ int lbgpu_batch_create(int device, size_t memory_budget, lbgpu_batch **out)
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_counts, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_ticket, sizeof(BatchTicket));
+    if (e == cudaSuccess) e = cudaMemset(b->d_ticket, 0, sizeof(BatchTicket));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
     int optin = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     if (e == cudaSuccess) {
@@ -540,6 +656,7 @@ void lbgpu_batch_destroy(lbgpu_batch *b)
     cudaFree(b->d_smem);
     cudaFree(b->d_du);
     cudaFree(b->d_counts);
+    cudaFree(b->d_ticket);
     for (cudaEvent_t ev : {b->ev0, b->ev1, b->fork, b->join})
         if (ev) cudaEventDestroy(ev);
     if (b->side) cudaStreamDestroy(b->side);
@@ -722,14 +839,30 @@ int lbgpu_batch_time_steps(lbgpu_batch *b, int nsteps, float *ms)
     int rc = rebuild(b);
     if (rc) return rc;
     const bool work = !b->desc_slot.empty() && nsteps > 0;
-    cudaGraphExec_t exec = nullptr;
     if ((rc = tune_aa(b)) || (rc = tune_smem(b))) return rc;             // outside the timed region
-    if (work && (rc = graph_of(b, nsteps, false, &exec))) return rc;
+    if (work && (rc = call_graphs(b, nsteps, false, false))) return rc;
     LBB_CK(cudaEventRecord(b->ev0, b->stream));
     if (work && (rc = run_steps(b, nsteps, false))) return rc;
     LBB_CK(cudaEventRecord(b->ev1, b->stream));
     LBB_CK(cudaEventSynchronize(b->ev1));
     LBB_CK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return LBGPU_OK;
+}
+
+int lbgpu_batch_get_tuning(lbgpu_batch *b, lbgpu_batch_tuning *out)
+{
+    if (!b || !out) return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_get_tuning: null argument");
+    std::memset(out, 0, sizeof(*out));
+    out->tuned = b->aa_tuned ? 1 : 0;
+    for (int k = 0; k < 2; ++k) {
+        out->aa_work_list[k] = b->aa_list[k];
+        out->aa_min_blocks[k] = b->aa_minb[k];
+        out->aa_tiles_per_claim[k] = b->aa_tpc[k];
+        out->aa_ms[k] = b->aa_ms[k];
+    }
+    out->smem_threads = b->smem_threads;
+    out->steps_per_graph = b->steps_per_graph;
+    out->tiled_fluid_nodes = b->tuned_fluid;
     return LBGPU_OK;
 }
 

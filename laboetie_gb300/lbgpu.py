@@ -554,6 +554,15 @@ class RequestResult(C.Structure):
     ]
 
 
+class BatchTuning(C.Structure):
+    """lbgpu_batch_tuning (include/lbgpu.h)."""
+    _fields_ = [
+        ("tuned", C.c_int), ("aa_work_list", C.c_int * 2), ("aa_min_blocks", C.c_int * 2),
+        ("aa_tiles_per_claim", C.c_int * 2), ("smem_threads", C.c_int), ("steps_per_graph", C.c_int),
+        ("aa_ms", C.c_float * 2), ("tiled_fluid_nodes", C.c_longlong),
+    ]
+
+
 def make_cell(shape, relaxation_time=1.0, f_ext=(0.0, 0.0, 0.0), rho0=1.0, tracer=None) -> Cell:
     """shape = (lx, ly, lz); tracer = dict of lbgpu_tracer fields (Db, ka, kd, f_ext) or None."""
     c = Cell()
@@ -584,6 +593,7 @@ def _batch_lib():
         ("lbgpu_batch_mp_get", [vp, i, vp, vp, vp, pi], C.c_int),
         ("lbgpu_batch_mp_fields", [vp, i, vp, vp], C.c_int),
         ("lbgpu_batch_info", [vp, pi, C.POINTER(C.c_longlong), pi, C.POINTER(C.c_size_t)], C.c_int),
+        ("lbgpu_batch_get_tuning", [vp, C.POINTER(BatchTuning)], C.c_int),
         ("lbgpu_serve", [vp, vp, i, d, i, vp], C.c_int),
     ):
         f = getattr(L, name)
@@ -713,6 +723,15 @@ class Batch:
         self._chk(self.L.lbgpu_batch_info(self.b, C.byref(a), C.byref(f), C.byref(sm), C.byref(by)),
                   "batch_info")
         return dict(active=a.value, fluid_nodes=f.value, smem_boxes=sm.value, bytes=by.value)
+
+    def tuning(self):
+        """The tuner's choices (lbgpu_batch_get_tuning) as a dict."""
+        t = BatchTuning()
+        self._chk(self.L.lbgpu_batch_get_tuning(self.b, C.byref(t)), "batch_get_tuning")
+        return {"tuned": bool(t.tuned), "aa_work_list": list(t.aa_work_list),
+                "aa_min_blocks": list(t.aa_min_blocks), "aa_tiles_per_claim": list(t.aa_tiles_per_claim),
+                "smem_threads": t.smem_threads, "steps_per_graph": t.steps_per_graph,
+                "aa_ms": [float(x) for x in t.aa_ms], "tiled_fluid_nodes": t.tiled_fluid_nodes}
 
     def serve(self, requests, du_tol=1e-8, check_every=100):
         """requests: list of dicts {nature, arrival, max_steps, mp_steps, relaxation_time, f_ext,

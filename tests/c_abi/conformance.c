@@ -49,6 +49,12 @@ static int layout(void)
     F(lbgpu_request_result, status); F(lbgpu_request_result, mp_steps);
     F(lbgpu_request_result, fluid_nodes); F(lbgpu_request_result, vacf0);
     F(lbgpu_request_result, vacf_sum); Z(lbgpu_request_result);
+
+    F(lbgpu_batch_tuning, tuned); F(lbgpu_batch_tuning, aa_work_list);
+    F(lbgpu_batch_tuning, aa_min_blocks); F(lbgpu_batch_tuning, aa_tiles_per_claim);
+    F(lbgpu_batch_tuning, smem_threads); F(lbgpu_batch_tuning, steps_per_graph);
+    F(lbgpu_batch_tuning, aa_ms); F(lbgpu_batch_tuning, tiled_fluid_nodes);
+    Z(lbgpu_batch_tuning);
     return 0;
 }
 

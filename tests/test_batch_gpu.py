@@ -89,6 +89,27 @@ def test_batch_shared_memory_and_tiled_paths_agree(monkeypatch):
             assert np.allclose(x, y, rtol=1e-6, atol=1e-9 * np.abs(ma[0]).max())
 
 
+@pytest.mark.parametrize("variant", ["4,1,8", "5,2,32", "6,4,16"])
+def test_batch_work_list_launch_equals_one_block_per_tile(monkeypatch, variant):
+    """The persistent work-list form of the tiled in-place step (blocks per SM, tiles claimed at a
+    time, steps per graph forced through LBGPU_BATCH_AA_LIST) gives every box the same bits as one
+    block per tile: the tiles are claimed in another order and by other blocks, but each node's
+    arithmetic is the same; the call's steps also run as several graphs."""
+    cells = _cells()
+    base = _run(cells, range(len(cells)), 300, 200)
+    monkeypatch.setenv("LBGPU_BATCH_AA_LIST", variant)
+    with Batch() as b:
+        b.add(cells[3][0], f_ext=cells[3][1])
+        b.steps(2)
+        t = b.tuning()
+    minb, tpc, spg = (int(v) for v in variant.split(","))
+    assert t["aa_work_list"] == [1, 1] and t["aa_min_blocks"] == [minb, minb]
+    assert t["aa_tiles_per_claim"] == [tpc, tpc] and t["steps_per_graph"] == spg
+    listed = _run(cells, range(len(cells)), 300, 200)
+    for i in range(len(cells)):
+        _same(listed[i], base[i])
+
+
 def test_batch_flow_reaches_the_fp64_steady_state(oracle_mod):
     """Poiseuille slit 4x4x34, tau 1, f_ext 1e-5: the batch's converged velocity profile
     agrees with the FP64 oracle's converged profile to 1e-4 of its maximum."""

@@ -21,9 +21,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "c_abi", "conformance.c")
 STRUCTS = ["lbgpu_params", "lbgpu_tracer", "lbgpu_pnp_params", "lbgpu_cell", "lbgpu_request",
-           "lbgpu_request_result"]
+           "lbgpu_request_result", "lbgpu_batch_tuning"]
 KIND = {"c_int": (4, 4), "c_long_long": (8, 8), "c_double": (8, 8), "c_ptr": (8, 8),
-        "c_int8_t": (1, 1), "c_size_t": (8, 8)}
+        "c_int8_t": (1, 1), "c_size_t": (8, 8), "c_float": (4, 4)}
 
 
 def fortran_types():
@@ -110,7 +110,8 @@ def test_header_layout_equals_the_fortran_bind_c_type(conformance_exe, name):
 
 @pytest.mark.parametrize("name,cls", [
     ("lbgpu_params", "Params"), ("lbgpu_tracer", "Tracer"), ("lbgpu_pnp_params", "PnpParams"),
-    ("lbgpu_cell", "Cell"), ("lbgpu_request", "Request"), ("lbgpu_request_result", "RequestResult")])
+    ("lbgpu_cell", "Cell"), ("lbgpu_request", "Request"), ("lbgpu_request_result", "RequestResult"),
+    ("lbgpu_batch_tuning", "BatchTuning")])
 def test_python_mirrors_equal_the_header(conformance_exe, name, cls):
     import ctypes
 
