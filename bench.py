@@ -80,7 +80,7 @@ def args_():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-n", type=int, default=48)
     ap.add_argument("--serve-rates", default="2,8,32")
-    ap.add_argument("--serve-max-steps", type=int, default=20000)
+    ap.add_argument("--serve-max-steps", type=int, default=100000)
     ap.add_argument("--serve-mp-steps", type=int, default=10000)
     return ap.parse_args()
 
@@ -517,8 +517,11 @@ def batch_roofline(t):
 
 def bench_serving(a):
     """Poisson request streams at several rates through lbgpu_serve (continuous batching):
-    p50/p99 latency (arrival to finish) and solves/s; the same stream served one request at a
-    time (each alone, back to back) as the no-batching baseline of the highest rate."""
+    p50/p99 latency (arrival to finish) and solves/s, over all requests, over those whose flow
+    converged and over those that reached the step cap, and per family; the same stream served
+    one request at a time (each alone, back to back) as the no-batching baseline of the highest
+    rate, with each family's share of that time (the large cavities and touching-sphere cells are
+    HBM-bound alone and in the mix, so they bound the gain of batching: the Amdahl bound below)."""
     from laboetie_gb300 import workloads as wl
     from laboetie_gb300.lbgpu import Batch
 
@@ -535,20 +538,46 @@ def bench_serving(a):
             wall = time.perf_counter() - t
         lat = np.array([r["finished"] - q["arrival"] for r, q in zip(res, reqs)])
         ok = [r for r in res if r["status"] in (0, 1 << 5)]   # served; 1 << 5: flow capped
+
+        def pct(sel):
+            v = lat[sel]
+            if not len(v):
+                return None
+            return {"n": int(len(v)), "p50_s": round(float(np.percentile(v, 50)), 4),
+                    "p99_s": round(float(np.percentile(v, 99)), 4)}
+        conv = np.array([bool(r["converged"]) for r in res])
+        capped = np.array([r["status"] == 1 << 5 for r in res])
+        fam_arr = np.array(fams)
+        per_family = {}
+        for f in sorted(set(fams)):
+            sel = fam_arr == f
+            per_family[f] = dict(pct(sel), capped=int((capped & sel).sum()),
+                                 mean_flow_steps=round(float(np.mean([r["steps"] for r, s in zip(res, sel) if s])), 1),
+                                 mean_fluid_nodes=round(float(np.mean([r["fluid_nodes"] for r, s in zip(res, sel) if s])), 1))
         out.append({"rate_per_s": rate, "n": len(reqs), "ok": len(ok),
-                    "converged": sum(1 for r in ok if r["converged"]),
+                    "converged": int(conv.sum()), "capped": int(capped.sum()),
                     "solves_per_s": round(len(ok) / wall, 3), "seconds": round(wall, 2),
                     "p50_s": round(float(np.percentile(lat, 50)), 4),
                     "p99_s": round(float(np.percentile(lat, 99)), 4),
+                    "converged_latency": pct(conv), "capped_latency": pct(capped),
                     "mean_flow_steps": round(float(np.mean([r["steps"] for r in ok])), 1),
-                    "families": {f: fams.count(f) for f in sorted(set(fams))}})
+                    "families": per_family})
         if k == len(rates) - 1:
             t = time.perf_counter()
-            for q in reqs:
+            fam_time = {}
+            for q, f in zip(reqs, fams):
+                t1 = time.perf_counter()
                 with Batch() as b:
                     b.serve([dict(q, arrival=0.0)], du_tol=1e-8, check_every=100)
+                fam_time[f] = fam_time.get(f, 0.0) + time.perf_counter() - t1
             t_fifo = time.perf_counter() - t
+            # Amdahl bound of batching: the time the families that batching cannot speed up
+            # (their boxes keep the device busy alone) take one at a time, against the whole
+            big = sum(v for f, v in fam_time.items() if f in ("cc", "cavity"))
             fifo = {"solves_per_s": round(len(reqs) / t_fifo, 3), "seconds": round(t_fifo, 2),
+                    "family_seconds": {f: round(v, 2) for f, v in sorted(fam_time.items())},
+                    "share_of_large_families": round(big / t_fifo, 3),
+                    "speedup_bound_if_large_families_gain_nothing": round(t_fifo / big, 2) if big > 0 else None,
                     "what": "the highest-rate stream, each request served alone, back to back"}
     return {"metric": "served solves/s, p50/p99 latency", "rates": out, "one_at_a_time": fifo,
             "config": {"workload": "Poisson arrivals; slit 4x4x(16..128), cylinder z (16..96)^2 x 32 "

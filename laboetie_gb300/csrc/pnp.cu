@@ -281,6 +281,24 @@ __global__ void __launch_bounds__(PB) k_residual(const PnpArgs a, const double *
     block_partial4(t, a.partial);
 }
 
+// Sum of phi over every node (block partials), and phi -= shift: the multicolour SOR's solution is
+// pinned to the sum of phi it started from, which the reference's Jacobi sweep keeps (its weights
+// sum to 1 and a neutral system's charge terms sum to 0), so that both solvers return the same
+// member of the family of solutions of the periodic problem (they differ by a constant).
+__global__ void __launch_bounds__(PB) k_sum_phi(const double *phi, long long N, double *partial)
+{
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < N; r += (long long)gridDim.x * PB)
+        t[0] = t[0] + phi[r];
+    block_partial4(t, partial);
+}
+
+__global__ void __launch_bounds__(PB) k_shift_phi(double *phi, long long N, double shift)
+{
+    for (long long r = (long long)blockIdx.x * PB + threadIdx.x; r < N; r += (long long)gridDim.x * PB)
+        phi[r] = phi[r] - shift;
+}
+
 // Link flux of just_eq_smolu.f90:86-99 from site a (origin) to site b along direction l.
 __device__ __forceinline__ void link_flux(const PnpArgs &k, long long ra, long long rb, double delta,
                                           double &Jp, double &Jm)
@@ -638,6 +656,13 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
             return ctx_cuda(ctx, ce, "instantiate sor");
         }
     }
+    double sum0 = 0.0;
+    if (multi) {
+        double r4[4];
+        k_sum_phi<<<grid, PB, 0, st>>>(s->phi[s->par], ctx->N, s->partial);
+        if ((rc = read4(ctx, grid, r4))) return rc;
+        sum0 = r4[0];
+    }
     cudaError_t e = cudaSuccess;
     for (int round = 0;; ++round) {
         e = cudaGraphLaunch(s->sor_exec[round == 0 ? 0 : 1], st);
@@ -646,7 +671,14 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
         if (e != cudaSuccess || c.done) break;
     }
     if (e != cudaSuccess) return ctx_cuda(ctx, e, "lbgpu_sor");
-    if (!four) s->par = c.parity;
+    if (multi) {
+        double r4[4];
+        k_sum_phi<<<grid, PB, 0, st>>>(s->phi[s->par], ctx->N, s->partial);
+        if ((rc = read4(ctx, grid, r4))) return rc;
+        k_shift_phi<<<grid, PB, 0, st>>>(s->phi[s->par], ctx->N, (r4[0] - sum0) / (double)ctx->N);
+        LBG_CK(ctx, cudaGetLastError());
+    }
+    if (!multi) s->par = c.parity;
     if (iters) *iters = s->p.solver == LBGPU_POISSON_SOR4 ? c.iter : c.iter - 1;  // sor.f90:87
     if ((rc = sum_abs_phi(ctx, &s->anormf0))) return rc;          // sor.f90:90
     if (!c.converged)
