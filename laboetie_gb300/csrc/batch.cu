@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(BATCH_BLOCK) k_batch_mp_v(const BatchInst *__r
     node_moments64(I, k, rho, J[0], J[1], J[2]);
     float o[3];
     for (int d = 0; d < 3; ++d) o[d] = (float)((J[d] + I.tfext[d]) / rho);
-    I.V[r] = make_float4(o[0], o[1], o[2], 0.0f);
+    I.V[r] = make_float4(o[0], o[1], o[2], 1.0f);   // w: fluid flag (the slab step's link mask)
 }
 
 // One block per small box in the flow phase, for all the steps of a call: load, nsteps steps in

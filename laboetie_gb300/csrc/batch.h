@@ -54,6 +54,9 @@ struct BatchInst {
     // 32 x 8 columns and zc planes (mp_slab.cuh); 0 otherwise
     int zc;
     int ntacc;              // tiles with VACF accumulators in tacc (the status word follows)
+    // the slab step's bounded waits (batch tiles stage with per-thread copies: unused, zero)
+    unsigned long long wait_ns;
+    int skip_copies;
 };
 
 // Nodes a box's kernels iterate (compact fluid nodes or lattice nodes) and its 256-node tiles.

@@ -78,6 +78,11 @@ struct MpArgs32 {
     // and elec_slope for the per-link fermi factors (the grid-stride step is used)
     int charged;
     float lw[3], z, inv_pstat, E[3];
+    // bounded waits of the slab step's bulk copies: the limit (ns); skip_copies (set only by a
+    // test, LBGPU_MP_TEST_SKIP_COPIES=1) arms each plane's barrier without issuing its copies, so
+    // the wait runs out and the step reports LBGPU_ERR_TIMEOUT without any fault
+    unsigned long long wait_ns;
+    int skip_copies;
 };
 
 // Shared-memory slab variant of the FP32 step (mp_f32.cu): 32 x 8 column tiles sweeping a chunk

@@ -238,6 +238,11 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
         b.ly = a.ly;
         b.lz = a.lz;
         b.ads = s->ads;
+        // LBGPU_MP_TEST_SKIP_COPIES=1 (tests only): the slab step arms its barriers without
+        // issuing the bulk copies, and its bounded waits (50 ms then) run out
+        const char *skip_env = std::getenv("LBGPU_MP_TEST_SKIP_COPIES");
+        b.skip_copies = skip_env && std::string(skip_env) == "1";
+        b.wait_ns = b.skip_copies ? 50000000ull : 2000000000ull;
         // LBGPU_MP_SLAB=0: the grid-stride step everywhere (same per-node arithmetic)
         const char *slab_env = std::getenv("LBGPU_MP_SLAB");
         b.slab = !(slab_env && std::string(slab_env) == "0");

@@ -176,21 +176,25 @@ __global__ void __launch_bounds__(MP_BLOCK, 4)
               [&](const double (&tot)[3]) { mp_control(a.ctl, a.hist, tot); });
 }
 
-// V = (j + f_ext - rho q D E)/rho on fluid nodes (FP64, rounded once to FP32); 0 on solid.
+// V = (j + f_ext - rho q D E)/rho on fluid nodes (FP64, rounded once to FP32); 0 on solid.  The
+// fourth component holds the potential for a charged tracer, else the node's fluid flag (1 or 0),
+// which the slab step multiplies into a link's lambda w / 2 instead of testing the link's
+// bounce-back bit.
 __global__ void __launch_bounds__(MP_BLOCK) k_mp_v(const MpArgs64 a, float4 *V)
 {
     const long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x;
     if (r >= a.N) return;
-    const float phi = a.phi ? (float)a.phi[r] : 0.0f;   // charged tracer: the potential
-    if (!(a.mask[r] & FLUID_BIT)) {
-        V[r] = make_float4(0.f, 0.f, 0.f, phi);
+    const bool fluid = a.mask[r] & FLUID_BIT;
+    const float w = a.phi ? (float)a.phi[r] : (fluid ? 1.0f : 0.0f);
+    if (!fluid) {
+        V[r] = make_float4(0.f, 0.f, 0.f, w);
         return;
     }
     const double rho = a.rho[r];
     const double J[3] = {a.jx[r], a.jy[r], a.jz[r]};
     float o[3];
     for (int d = 0; d < 3; ++d) o[d] = (float)((J[d] + a.fext[d] - rho * a.q * a.D * a.E[d]) / rho);
-    V[r] = make_float4(o[0], o[1], o[2], phi);
+    V[r] = make_float4(o[0], o[1], o[2], w);
 }
 
 }  // namespace

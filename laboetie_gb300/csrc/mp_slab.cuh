@@ -7,8 +7,8 @@
 // (and the node's fixed (u*, D)) are loaded into registers ahead of use.  One block barrier per
 // plane.  mp_slab_planes is the difference form of mp_f32.cu:k_mp32 (same operations in the same
 // order, so P is bit-identical) visiting each plane once, for single boxes and batched ones alike.
-// The argument struct provides V, P[2], A[2], aux, mask, lx, ly, lz, ads, ka, kd, one_minus_kd,
-// a1[3], lwh[3].
+// The argument struct provides V (its w component: the node's fluid flag, 1 or 0), P[2], A[2],
+// aux, mask, lx, ly, lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3], wait_ns, skip_copies.
 #pragma once
 
 #include <type_traits>
@@ -35,6 +35,14 @@ constexpr size_t MPS_SMEM = 128 + sizeof(float4) * 8 * SPLP + 4 * sizeof(uint64_
 __device__ __forceinline__ float mp32_scatter(bool blocked, float a1, float cv, float lwh)
 {
     return blocked ? 0.0f : __fmaf_rn(a1, cv, lwh);
+}
+
+// The same from the neighbour's staged record: lwhf = (lambda w / 2) * (its fluid flag, 1 or 0)
+// and V = 0 on a solid neighbour, so a blocked link gives fma(a1, 0, 0) = 0 and an open one
+// fma(a1, c.V, lambda w / 2): the bits of mp32_scatter with no test of the link's bit.
+__device__ __forceinline__ float mp32_scatter_flag(float a1, float cv, float lwhf)
+{
+    return __fmaf_rn(a1, cv, lwhf);
 }
 
 // One incoming link of an FP32 step: n += sp_in (P(r + c_l) - P(r)).
@@ -162,6 +170,9 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
         __syncthreads();
     }
     auto slot = [&](int zz) { return (zz - z0 + 1) & 3; };
+    const unsigned long long wait_ns = a.wait_ns ? a.wait_ns : 2000000000ull;
+    const bool skip_copies = a.skip_copies != 0;
+    int last_issued = z0 - 2, last_waited = z0 - 2;   // bulk-copied planes issued / arrived
     // plane zz (<= z1) into its slot; per-thread copies commit one group per call (an empty one
     // past z1), so that "plane zz+1 arrived" is always "all but the latest group complete"
     auto load_plane = [&](int zz) {
@@ -171,9 +182,12 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
             if (tma) {
                 if (threadIdx.x == 0) {
                     mbar_arrive_expect_tx(&bars[slot(zz)], 2 * MPS_TMA_BYTES);
-                    tma_load_4d(dv, tmV, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
-                    tma_load_4d(dp, tmP, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
+                    if (!skip_copies) {
+                        tma_load_4d(dv, tmV, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
+                        tma_load_4d(dp, tmP, 0, x0 - 1, y0 - 1, gz, &bars[slot(zz)]);
+                    }
                 }
+                last_issued = zz;
             } else {
                 for (int k = threadIdx.x; k < SPL; k += MP_BLOCK) {
                     const int hx = k % SHX, hy = k / SHX;
@@ -195,7 +209,9 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
             cp_async_wait1();
             return true;
         }
-        return mbar_wait(&bars[slot(zz)], (unsigned)(((zz - z0 + 1) >> 2) & 1));
+        const bool done = mbar_wait(&bars[slot(zz)], (unsigned)(((zz - z0 + 1) >> 2) & 1), wait_ns);
+        if (done) last_waited = zz;
+        return done;
     };
     const int tx = threadIdx.x % MPS_TX, ty = threadIdx.x / MPS_TX;
     const int x = x0 + tx, y = y0 + ty;
@@ -224,8 +240,10 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
     auto step = [&](auto DA, auto DB, auto DC, Node &A, Node &B, Node &C, int zz) {
         constexpr bool da = decltype(DA)::value, db = decltype(DB)::value, dc = decltype(DC)::value;
         if (dc && ok) ok = wait_plane(zz + 1);
-        __syncthreads();
-        load_plane(zz + 3);
+        // one verdict for the block: once a wait has run out, no thread uses the ring and no new
+        // copy is issued (the per-thread path never fails)
+        ok = __syncthreads_and(ok);
+        if (ok) load_plane(zz + 3);
         if constexpr (dc) {   // node zz+1 enters; its centre P is the next step's centre point
             C.m = m_next;
             m_next = mask_at(zz + 2);
@@ -234,8 +252,9 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
         }
         if constexpr (db)
             if (B.m & FLUID_BIT) B.ax = __ldg(a.aux + col0 + plane * zz);   // used at step zz+1
-        const uint32_t any = (da ? A.m : 0u) | (db ? B.m : 0u) | (dc ? C.m : 0u);
-        if (ok && (any & FLUID_BIT)) {
+        // every lane runs the links (no branch: a warp runs them whenever one of its lanes has a
+        // fluid node in flight); a lane without one adds onto a running sum it never stores
+        if (ok) {
             const int s0 = slot(zz) * SPLP + c0;
             static_for<0, 9>([&](auto K) {
                 constexpr int k = decltype(K)::value;
@@ -246,22 +265,29 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
                     float4 pn;
                     if constexpr (dx == 0 && dy == 0) pn = B.p;
                     else pn = sP[s0 + dy * SHX + dx];
+                    // lambda w / 2 of the point's two weight classes times its fluid flag: axis
+                    // links (dx, dy) = (0, 0) in z and the in-plane axis links, diagonal the rest
+                    constexpr bool need_ax = (dx == 0 && dy == 0) || (db && dx * dx + dy * dy == 1);
+                    constexpr bool need_dg = (dx * dx + dy * dy == 2 && db) || (dx * dx + dy * dy == 1 && (dc || da));
+                    float lw_ax = 0.0f, lw_dg = 0.0f;
+                    if constexpr (need_ax) lw_ax = __fmul_rn(a.lwh[1], vn.w);
+                    if constexpr (need_dg) lw_dg = __fmul_rn(a.lwh[2], vn.w);
                     if constexpr (dc && axis) {   // link (dx, dy, -1) of node zz+1
                         constexpr int l = link_of(dx, dy, -1);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((C.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, 1>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, 1>(vn), w == 1 ? lw_ax : lw_dg),
                                   pn, C.p, C.n.x, C.n.y, C.n.z);
                     }
                     if constexpr (db && (dx != 0 || dy != 0)) {   // link (dx, dy, 0) of node zz
                         constexpr int l = link_of(dx, dy, 0);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((B.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, 0>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, 0>(vn), w == 1 ? lw_ax : lw_dg),
                                   pn, B.p, B.n.x, B.n.y, B.n.z);
                     }
                     if constexpr (da && axis) {   // link (dx, dy, +1) of node zz-1
                         constexpr int l = link_of(dx, dy, 1);
                         constexpr int w = wclass(l);
-                        mp32_link(mp32_scatter((A.m >> inv(l)) & 1u, a.a1[w], mp32_cdot<-dx, -dy, -1>(vn), a.lwh[w]),
+                        mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, -1>(vn), w == 1 ? lw_ax : lw_dg),
                                   pn, A.p, A.n.x, A.n.y, A.n.z);
                     }
                 }
@@ -287,7 +313,8 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
     load_plane(z0 - 1);
     load_plane(z0);
     ok = wait_plane(z0 - 1);
-    load_plane(z0 + 1);
+    ok = __syncthreads_and(ok);
+    if (ok) load_plane(z0 + 1);
     __syncthreads();
     S0.p = (ok && col) ? sP[slot(z0 - 1) * SPLP + c0] : zero;   // centre P of plane z0-1
     // S0, S1, S2 = nodes zz-1, zz, zz+1 at step zz (a loop unrolled by three to rotate the slots
@@ -299,7 +326,14 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
         S1 = S2;
     }
     step(T{}, F{}, F{}, S0, S1, S2, z1);   // the last node's links from plane z1
-    if (!ok && status) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
+    if (!ok) {
+        // a wait ran out: let the copies already issued into this block's shared memory land
+        // (each wait bounded again) before the block leaves, then report
+        if (tma)
+            for (int zz = last_waited + 1; zz <= last_issued; ++zz)
+                if (zz >= z0 - 1) mbar_wait(&bars[slot(zz)], (unsigned)(((zz - z0 + 1) >> 2) & 1), wait_ns);
+        if (status && threadIdx.x == 0) atomicOr(status, (unsigned)LBGPU_ERR_TIMEOUT);
+    }
 }
 
 }  // namespace lbg

@@ -43,9 +43,10 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Waits for the phase of the given parity to complete: at most about 2 s of global time (and
-// 2^28 polls should the timer not advance); false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+// Waits for the phase of the given parity to complete: at most about limit_ns of global time
+// (2 s by default, and 2^28 polls should the timer not advance); false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity,
+                                          unsigned long long limit_ns = 2000000000ull)
 {
     const unsigned s = smem_addr(bar);
     unsigned long long t0 = 0;
@@ -60,7 +61,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
         if ((it & 63u) == 0u) {
             const unsigned long long t = global_ns();
             if (it == 0u) t0 = t;
-            else if (t - t0 > 2000000000ull) return false;
+            else if (t - t0 > limit_ns) return false;
         }
     }
     return false;

@@ -72,3 +72,31 @@ def test_repeated_runs_are_bit_identical():
             assert all(np.array_equal(p, q) for p, q in zip(x, y))
         else:
             assert np.array_equal(x, y)
+
+
+def test_tracer_copy_wait_that_runs_out_reports_timeout_promptly(monkeypatch):
+    """The FP32 tracer's slab step waits, bounded, for the bulk copies that stage its planes.
+    LBGPU_MP_TEST_SKIP_COPIES=1 arms each plane's barrier without issuing its copies (a flag that
+    nothing sets: no fault, no hang): every interior tile's wait runs out after 50 ms, the block
+    lets nothing else land, leaves its nodes alone and reports LBGPU_ERR_TIMEOUT.  The call returns
+    that status after its first step's graph, not after the 5000 steps asked for, and the context
+    stays usable."""
+    monkeypatch.setenv("LBGPU_MP_TEST_SKIP_COPIES", "1")
+    nat = geo.porous_spheres(96, 6.0, 0.7, 11)   # interior 32 x 8 tiles: bulk-copied planes
+    fluid = nat == 0
+    rho = np.where(fluid, 1.0, 0.0)
+    j = [np.where(fluid, 1e-4, 0.0), np.zeros(nat.shape), np.zeros(nat.shape)]
+    import time
+
+    with Box(nat, precision=FP32_DEV) as box:
+        box.mp_init(moments=(rho, j), Db=0.01)
+        t = time.perf_counter()
+        with pytest.raises(LbgpuError) as e:
+            box.mp_propagate(5000)
+        dt = time.perf_counter() - t
+        assert e.value.status & (1 << 10)
+        assert dt < 30.0
+        box.flow_init()                           # the context still runs work
+        box.flow_steps(4, force_on=True)
+        _, r2, _ = box.flow_get(populations=False)
+    assert np.isfinite(r2).all()
