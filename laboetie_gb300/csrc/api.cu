@@ -101,6 +101,8 @@ void fill_args64(lbgpu_ctx *ctx, FlowArgs64 &a)
     a.jz = ctx->d_j[2];
     a.rho = ctx->d_rho;
     a.N = ctx->N;
+    a.fidx = ctx->d_fidx;
+    a.Nf = ctx->d_fidx ? (long long)ctx->counts[0] : 0;
     a.lx = ctx->p.lx;
     a.ly = ctx->p.ly;
     a.lz = ctx->p.lz;

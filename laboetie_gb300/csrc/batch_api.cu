@@ -49,6 +49,7 @@ struct Slot {
 struct GraphEntry {
     int nsteps = 0;
     bool check = false;
+    bool smem = false;   // holds the shared-memory boxes' launch
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -281,35 +282,50 @@ int launch_aa(lbgpu_batch *b, const BatchInst *insts, int odd, cudaStream_t s)
     return LBGPU_OK;
 }
 
-// The launches of one call: the shared-memory boxes on the side stream, concurrently with the
+// The shared-memory boxes' launch for nsteps steps on the side stream, forked from the main one
+// (the main stream waits on b->join for it).
+int enqueue_smem(lbgpu_batch *b, int nsteps, bool check)
+{
+    LBB_CK(cudaEventRecord(b->fork, b->stream));
+    LBB_CK(cudaStreamWaitEvent(b->side, b->fork, 0));
+    LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem_flow, b->nsmem - b->nsmem_flow, nsteps, check,
+                             b->d_du, b->smem_bytes_flow, b->smem_bytes_mp, b->smem_threads, b->side));
+    LBB_CK(cudaEventRecord(b->join, b->side));
+    return LBGPU_OK;
+}
+
+int clear_du(lbgpu_batch *b)
+{
+    LBB_CK(cudaMemsetAsync(b->d_du, 0, sizeof(unsigned) * std::max<size_t>(b->desc_slot.size(), 1), b->stream));
+    return LBGPU_OK;
+}
+
+// The launches of one call (or, with smem = false, of a part of a call whose shared-memory boxes
+// run in a launch of their own): the shared-memory boxes on the side stream, concurrently with the
 // per-step launches of the tiled boxes on the main stream.
-int enqueue_steps(lbgpu_batch *b, int nsteps, bool check)
+int enqueue_steps(lbgpu_batch *b, int nsteps, bool check, bool smem)
 {
     cudaStream_t s = b->stream;
-    if (check) LBB_CK(cudaMemsetAsync(b->d_du, 0, sizeof(unsigned) * std::max<size_t>(b->desc_slot.size(), 1), s));
-    if (b->nsmem) {
-        LBB_CK(cudaEventRecord(b->fork, s));
-        LBB_CK(cudaStreamWaitEvent(b->side, b->fork, 0));
-        LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem_flow, b->nsmem - b->nsmem_flow, nsteps, check,
-                                 b->d_du, b->smem_bytes_flow, b->smem_bytes_mp, b->smem_threads, b->side));
-        LBB_CK(cudaEventRecord(b->join, b->side));
-    }
+    if (check && smem)
+        if (int rc = clear_du(b)) return rc;
+    if (b->nsmem && smem)
+        if (int rc = enqueue_smem(b, nsteps, check)) return rc;
     for (int t = 0; t < nsteps; ++t) {
         if (int rc = launch_aa(b, b->d_insts, t & 1, s)) return rc;
         LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
         LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, s));
     }
     if (check) LBB_CK(launch_batch_check(b->d_insts, b->d_tiles, b->nflow, b->d_du, s));
-    if (b->nsmem) LBB_CK(cudaStreamWaitEvent(s, b->join, 0));
+    if (b->nsmem && smem) LBB_CK(cudaStreamWaitEvent(s, b->join, 0));
     return LBGPU_OK;
 }
 
 // The graph of one call (nsteps, check), captured on first use and kept until the batch's
 // tables change.
-int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
+int graph_of(lbgpu_batch *b, int nsteps, bool check, bool smem, cudaGraphExec_t *out)
 {
     for (auto &g : b->graphs)
-        if (g.nsteps == nsteps && g.check == check) {
+        if (g.nsteps == nsteps && g.check == check && g.smem == smem) {
             *out = g.exec;
             return LBGPU_OK;
         }
@@ -317,7 +333,7 @@ int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
     cudaGraph_t graph;
     cudaGraphExec_t exec;
     LBB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int rc = enqueue_steps(b, nsteps, check);
+    const int rc = enqueue_steps(b, nsteps, check, smem);
     const cudaError_t e = cudaStreamEndCapture(s, &graph);
     if (rc) {
         if (e == cudaSuccess) cudaGraphDestroy(graph);
@@ -331,7 +347,7 @@ int graph_of(lbgpu_batch *b, int nsteps, bool check, cudaGraphExec_t *out)
         cudaGraphExecDestroy(b->graphs.front().exec);
         b->graphs.erase(b->graphs.begin());
     }
-    b->graphs.push_back({nsteps, check, exec});
+    b->graphs.push_back({nsteps, check, smem, exec});
     *out = exec;
     return LBGPU_OK;
 }
@@ -546,18 +562,28 @@ int tune_smem(lbgpu_batch *b)
 }
 
 // A call's steps run as graphs of steps_per_graph steps (the tuner's choice), the last one with
-// the rest and the convergence check.  launch = false only captures the graphs.
+// the rest and the convergence check.  The shared-memory boxes step the whole call in one launch
+// whatever the split (each of their launches loads and stores the boxes once): inside the graph
+// when the call is one graph, else launched on its own before the graphs, which then hold only
+// the tiled boxes' launches.  launch = false only captures the graphs.
 int call_graphs(lbgpu_batch *b, int nsteps, bool check, bool launch)
 {
     const int S = b->steps_per_graph > 0 ? b->steps_per_graph : nsteps;
+    const bool split = S < nsteps && b->nsmem > 0;
+    if (split && launch) {
+        if (check)
+            if (int rc = clear_du(b)) return rc;
+        if (int rc = enqueue_smem(b, nsteps, check)) return rc;
+    }
     int left = nsteps;
     while (left > 0) {
         const int n = left > S ? S : left;
         left -= n;
         cudaGraphExec_t exec = nullptr;
-        if (int rc = graph_of(b, n, check && left == 0, &exec)) return rc;
+        if (int rc = graph_of(b, n, check && left == 0, !split, &exec)) return rc;
         if (launch) LBB_CK(cudaGraphLaunch(exec, b->stream));
     }
+    if (split && launch) LBB_CK(cudaStreamWaitEvent(b->stream, b->join, 0));
     return LBGPU_OK;
 }
 

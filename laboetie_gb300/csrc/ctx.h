@@ -46,6 +46,10 @@ struct lbgpu_ctx {
     int8_t *d_nature = nullptr;
     uint32_t *d_mask = nullptr;
 
+    // FP64 contexts: the lattice indices of the fluid nodes in lattice order (counts[0] of them);
+    // the FP64 step kernels run one thread per entry, so no lane of a warp idles on a solid node
+    uint32_t *d_fidx = nullptr;
+
     // flow state.  FP64: d_f[2] doubles; FP32 deviation: d_g[2] floats.
     double *d_f[2] = {nullptr, nullptr};
     float *d_g[2] = {nullptr, nullptr};

@@ -22,6 +22,8 @@ struct FlowArgs64 {
     unsigned long long *err_bits;// operator-mode max reduction target
     unsigned *status;            // operator-mode status bits
     long long N;
+    const uint32_t *fidx;        // lattice indices of the Nf fluid nodes (step kernel), or null
+    long long Nf;
     int lx, ly, lz;
     int parity;                  // fixed mode: buffer read this step
     int force_moment;            // fixed mode: f_ext in the moments of this step

@@ -114,6 +114,16 @@ int ctx_init_device(lbgpu_ctx *ctx, const int8_t *nature)
         return ctx_fail(ctx, LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
     if (p.precision != LBGPU_FP32_DEV) {
         for (int b = 0; b < 2; ++b) LBG_CK(ctx, dalloc(&ctx->d_f[b], (size_t)Q * N));
+        std::vector<uint32_t> fidx;
+        fidx.reserve(ctx->counts[0]);
+        for (long long i = 0; i < N; ++i)
+            if (nature[i] == 0) fidx.push_back((uint32_t)i);
+        if (fidx.size() != ctx->counts[0])
+            return ctx_fail(ctx, LBGPU_ERR_CUDA, "fluid node count differs between host and device");
+        LBG_CK(ctx, dalloc(&ctx->d_fidx, fidx.size()));
+        LBG_CK(ctx, cudaMemcpyAsync(ctx->d_fidx, fidx.data(), sizeof(uint32_t) * fidx.size(),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+        LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));   // the host list goes out of scope
     } else {
         const char *mode = std::getenv("LBGPU_FP32_STREAMING");
         ctx->aa = !(mode && std::string(mode) == "ab");
@@ -160,6 +170,7 @@ void ctx_release_device(lbgpu_ctx *ctx)
         if (ctx->graph_fixed[f]) cudaGraphExecDestroy(ctx->graph_fixed[f]);
     cudaFree(ctx->d_nature);
     cudaFree(ctx->d_mask);
+    cudaFree(ctx->d_fidx);
     cudaFree(ctx->d_cpos);
     cudaFree(ctx->d_cmask);
     cudaFree(ctx->d_rowtab);

@@ -361,7 +361,10 @@ __global__ void __launch_bounds__(BLOCK) k_flow_step(const FlowArgs64 a)
     const double *__restrict__ src = parity ? a.f1 : a.f0;
     double *__restrict__ dst = parity ? a.f0 : a.f1;
     const long long N = a.N;
-    const long long node = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    // one thread per fluid node through the list (every lane of a warp does work), else one per
+    // lattice node
+    const long long i = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long node = a.fidx ? (i < a.Nf ? (long long)a.fidx[i] : N) : i;
     double err = 0.0;
     unsigned bad = 0;
     if (node < N) {
@@ -580,7 +583,7 @@ cudaError_t launch_step(const FlowArgs64 &a, int fmask, bool field, bool check, 
 cudaError_t launch_flow_step_f64(const FlowArgs64 &a, int fmask, bool field, bool check,
                                  bool ref, unsigned grid, cudaStream_t s)
 {
-    if (!grid) grid = grid_of(a.N);
+    if (!grid) grid = grid_of(a.fidx ? a.Nf : a.N);
     return a.fused ? launch_step<true>(a, fmask, field, check, ref, grid, s)
                    : launch_step<false>(a, fmask, field, check, ref, grid, s);
 }

@@ -42,6 +42,8 @@ struct MpArgs64 {
     MpCtl *ctl;
     double *hist;                      // 3 per step
     long long N;
+    const uint32_t *fidx;              // lattice indices of the Nf fluid nodes (step kernel), or null
+    long long Nf;
     int lx, ly, lz;
     int ads;
     double lambda, ka, kd, one_minus_kd, bw;

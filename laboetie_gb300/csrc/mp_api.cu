@@ -201,6 +201,8 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
     a.z = tr->z;
     a.pstat = Pstat;
     a.fused = ctx->p.precision == LBGPU_FP64_FUSED;
+    a.fidx = ctx->d_fidx;
+    a.Nf = ctx->d_fidx ? (long long)ctx->counts[0] : 0;
     s->nblocks = (unsigned)((N + MP_BLOCK - 1) / MP_BLOCK);
     int zc = 0;
     const unsigned resident = s->prec == LBGPU_FP64 ? 0u : mp32_slab_resident();
@@ -325,7 +327,11 @@ static int mp_run(lbgpu_ctx *ctx, int nsteps, double *vacf_out, int *steps_done,
     cudaGraphExec_t exec;
     LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < G; ++k) {
-        const unsigned grid = std::min(s->nblocks, MP_MAX_BLOCKS);
+        // the FP64 step walks the fluid-node list: one thread per fluid node
+        const unsigned grid = std::min(s->prec == LBGPU_FP64 && s->a64.fidx
+                                           ? (unsigned)((s->a64.Nf + MP_BLOCK - 1) / MP_BLOCK)
+                                           : s->nblocks,
+                                       MP_MAX_BLOCKS);
         cudaError_t e = s->prec == LBGPU_FP64 ? launch_mp_step_f64(s->a64, grid, st)
                                               : launch_mp_step_f32(s->a32, grid, s->tma_ok ? s->tm : nullptr, st);
         if (e != cudaSuccess) {

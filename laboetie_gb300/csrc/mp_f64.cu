@@ -181,8 +181,11 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp_step(const MpArgs64 a)
     const double *__restrict__ Py = a.P[par][1];
     const double *__restrict__ Pz = a.P[par][2];
     double v[3] = {0.0, 0.0, 0.0};
-    for (long long r = (long long)blockIdx.x * MP_BLOCK + threadIdx.x; r < N;
-         r += (long long)gridDim.x * MP_BLOCK) {
+    // the fluid nodes through their list (every lane of a warp does work), else every lattice node
+    const long long n_it = a.fidx ? a.Nf : N;
+    for (long long i = (long long)blockIdx.x * MP_BLOCK + threadIdx.x; i < n_it;
+         i += (long long)gridDim.x * MP_BLOCK) {
+        const long long r = a.fidx ? (long long)a.fidx[i] : i;
         const uint32_t m = a.mask[r];
         if (!(m & FLUID_BIT)) continue;
         long long X[3], Y[3], Z[3];

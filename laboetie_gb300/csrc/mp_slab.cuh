@@ -54,6 +54,16 @@ __device__ __forceinline__ void mp32_link(float spp, const float4 &pn, const flo
     n2 = __fmaf_rn(spp, __fsub_rn(pn.z, p.z), n2);
 }
 
+// The same with the x and y sums as one pair: packed FP32 operations (add.rn.f32x2 and
+// fma.rn.f32x2 round each element as the scalar operation does, and pn - p = pn + (-p) exactly),
+// so the bits are those of mp32_link with two instructions fewer per link.
+__device__ __forceinline__ void mp32_link2(float spp, const float4 &pn, const float4 &p, float2 &nxy, float &nz)
+{
+    const float2 d = __fadd2_rn(make_float2(pn.x, pn.y), make_float2(-p.x, -p.y));
+    nxy = __ffma2_rn(make_float2(spp, spp), d, nxy);
+    nz = __fmaf_rn(spp, __fsub_rn(pn.z, p.z), nz);
+}
+
 // End of an FP32 step: n = P(r) + (n + D P(r)), D = sum sp_in - sum sp_out of the node.
 __device__ __forceinline__ void mp32_finish(const float4 &p, float D, float &n0, float &n1, float &n2)
 {
@@ -77,17 +87,20 @@ __device__ __forceinline__ float4 mp32_adsorb(const float4 &p, const float4 &qa,
 }
 
 // c.V of a link (x, y, z summed in that order, signs folded): the one definition every FP32 tracer
-// kernel uses, so that their scattering probabilities round alike.
+// kernel uses, so that their scattering probabilities round alike.  The first term is taken as it
+// is (not added to 0), which differs from 0 + term only in the sign of a zero; c.V enters only
+// fma(a1, c.V, lwh) with lwh >= +0, where a zero of either sign gives the same result, so the
+// scattering probabilities keep their bits and an axis link costs no addition.
 template <int CX, int CY, int CZ>
 __device__ __forceinline__ float mp32_cdot(const float4 &v)
 {
-    float s = 0.0f;
-    if constexpr (CX > 0) s += v.x;
-    if constexpr (CX < 0) s -= v.x;
-    if constexpr (CY > 0) s += v.y;
-    if constexpr (CY < 0) s -= v.y;
-    if constexpr (CZ > 0) s += v.z;
-    if constexpr (CZ < 0) s -= v.z;
+    static_assert(CX != 0 || CY != 0 || CZ != 0, "rest link");
+    constexpr int first = CX != 0 ? 0 : (CY != 0 ? 1 : 2);
+    float s = first == 0 ? (CX > 0 ? v.x : -v.x) : (first == 1 ? (CY > 0 ? v.y : -v.y) : (CZ > 0 ? v.z : -v.z));
+    if constexpr (first < 1 && CY > 0) s += v.y;
+    if constexpr (first < 1 && CY < 0) s -= v.y;
+    if constexpr (first < 2 && CZ > 0) s += v.z;
+    if constexpr (first < 2 && CZ < 0) s -= v.z;
     return s;
 }
 
@@ -217,28 +230,44 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
     const int x = x0 + tx, y = y0 + ty;
     const bool col = x < lx && y < ly;
     const int c0 = (ty + 1) * SHX + (tx + 1);
-    const size_t col0 = (size_t)x + (size_t)lx * (size_t)y, plane = (size_t)lx * (size_t)ly;
+    // node offsets in 32 bits (a box holds fewer than 2^31 nodes); the column's arrays are
+    // addressed from its first node
+    const unsigned col0 = (unsigned)x + (unsigned)lx * (unsigned)y, plane = (unsigned)lx * (unsigned)ly;
+    const uint32_t *__restrict__ mcol = a.mask + col0;
+    const float4 *__restrict__ auxcol = a.aux + col0;
+    float4 *__restrict__ Pout = a.P[par ^ 1] + col0;
     // flag word of the column's node z; 0 (no fluid bit, no work) outside the tile's nodes
-    auto mask_at = [&](int z) { return (col && z >= z0 && z < z1) ? __ldg(a.mask + col0 + plane * z) : 0u; };
+    auto mask_at = [&](int z) { return (col && z < z1) ? __ldg(mcol + plane * (unsigned)z) : 0u; };
     const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     bool ok = true;   // false once a wait for a bulk copy ran out
     // a node of the column in flight: P (also the centre point of its plane for the links of
-    // the nodes above and below), running sum, flag word, fixed (u*, D)
+    // the nodes above and below), running sums (x and y as one packed pair), flag word
     struct Node {
-        float4 p, n, ax;
+        float4 p;
+        float2 nxy;
+        float nz;
         uint32_t m;
     };
     Node S0, S1, S2;
     S0.m = S1.m = S2.m = 0u;
     S0.p = S1.p = S2.p = zero;
-    S0.n = S1.n = S2.n = zero;
-    S0.ax = S1.ax = S2.ax = zero;
+    S0.nxy = S1.nxy = S2.nxy = make_float2(0.0f, 0.0f);
+    S0.nz = S1.nz = S2.nz = 0.0f;
     uint32_t m_next = mask_at(z0);   // flag word of node zz+1 at the start of step zz
     // Step zz with A = node zz-1, B = node zz, C = node zz+1 (DA, DB, DC: which of them can be
     // nodes of the tile: the first step zz = z0-1 has only C, the last zz = z1 only A, and each
     // computes only their links).
     auto step = [&](auto DA, auto DB, auto DC, Node &A, Node &B, Node &C, int zz) {
         constexpr bool da = decltype(DA)::value, db = decltype(DB)::value, dc = decltype(DC)::value;
+        // node zz-1's fixed (u*, D), needed at the end of this step: loaded before the links, so
+        // that they hide its latency
+        float4 axA = zero;
+        if constexpr (da)
+            if (A.m & FLUID_BIT) axA = __ldg(auxcol + plane * (unsigned)(zz - 1));
+        // the adsorbed part of node zz, read when it finishes at the end of the next step: asked
+        // into L1 now (no register held), so that read does not wait on L2/HBM
+        if constexpr (db)
+            if (a.ads && (B.m & INTERFACIAL_BIT)) prefetch_l1(a.A[par] + col0 + plane * (unsigned)zz);
         if (dc && ok) ok = wait_plane(zz + 1);
         // one verdict for the block: once a wait has run out, no thread uses the ring and no new
         // copy is issued (the per-thread path never fails)
@@ -248,10 +277,9 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
             C.m = m_next;
             m_next = mask_at(zz + 2);
             C.p = (ok && col) ? sP[slot(zz + 1) * SPLP + c0] : zero;
-            C.n = zero;
+            C.nxy = make_float2(0.0f, 0.0f);
+            C.nz = 0.0f;
         }
-        if constexpr (db)
-            if (B.m & FLUID_BIT) B.ax = __ldg(a.aux + col0 + plane * zz);   // used at step zz+1
         // every lane runs the links (no branch: a warp runs them whenever one of its lanes has a
         // fluid node in flight); a lane without one adds onto a running sum it never stores
         if (ok) {
@@ -276,35 +304,35 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
                         constexpr int l = link_of(dx, dy, -1);
                         constexpr int w = wclass(l);
                         mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, 1>(vn), w == 1 ? lw_ax : lw_dg),
-                                  pn, C.p, C.n.x, C.n.y, C.n.z);
+                                   pn, C.p, C.nxy.x, C.nxy.y, C.nz);
                     }
                     if constexpr (db && (dx != 0 || dy != 0)) {   // link (dx, dy, 0) of node zz
                         constexpr int l = link_of(dx, dy, 0);
                         constexpr int w = wclass(l);
                         mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, 0>(vn), w == 1 ? lw_ax : lw_dg),
-                                  pn, B.p, B.n.x, B.n.y, B.n.z);
+                                   pn, B.p, B.nxy.x, B.nxy.y, B.nz);
                     }
                     if constexpr (da && axis) {   // link (dx, dy, +1) of node zz-1
                         constexpr int l = link_of(dx, dy, 1);
                         constexpr int w = wclass(l);
                         mp32_link(mp32_scatter_flag(a.a1[w], mp32_cdot<-dx, -dy, -1>(vn), w == 1 ? lw_ax : lw_dg),
-                                  pn, A.p, A.n.x, A.n.y, A.n.z);
+                                   pn, A.p, A.nxy.x, A.nxy.y, A.nz);
                     }
                 }
             });
         }
         if constexpr (da) {
             if (ok && (A.m & FLUID_BIT)) {   // node zz-1 has all its links
-                const size_t r = col0 + plane * (zz - 1);
-                float4 n = A.n;
-                const float4 p = A.p, ax = A.ax;
-                vt[0] += p.x * ax.x;
-                vt[1] += p.y * ax.y;
-                vt[2] += p.z * ax.z;
-                mp32_finish(p, ax.w, n.x, n.y, n.z);
+                const unsigned r = plane * (unsigned)(zz - 1);
+                float n0 = A.nxy.x, n1 = A.nxy.y, n2 = A.nz;
+                const float4 p = A.p;
+                vt[0] += p.x * axA.x;
+                vt[1] += p.y * axA.y;
+                vt[2] += p.z * axA.z;
+                mp32_finish(p, axA.w, n0, n1, n2);
                 if (a.ads && (A.m & INTERFACIAL_BIT))
-                    a.A[par ^ 1][r] = mp32_adsorb(p, a.A[par][r], a.ka, a.kd, a.one_minus_kd, n.x, n.y, n.z);
-                __stcs(a.P[par ^ 1] + r, make_float4(n.x, n.y, n.z, 0.0f));
+                    a.A[par ^ 1][col0 + r] = mp32_adsorb(p, a.A[par][col0 + r], a.ka, a.kd, a.one_minus_kd, n0, n1, n2);
+                __stcs(Pout + r, make_float4(n0, n1, n2, 0.0f));
             }
         }
     };
