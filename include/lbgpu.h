@@ -333,9 +333,9 @@ int lbgpu_batch_info(lbgpu_batch *b, int *active, long long *fluid_nodes, int *s
  * scratch copies of the tiled boxes (their state does not advance), every variant of the even
  * and of the odd in-place step launch: one block per 256-node tile at 3..6 resident blocks per
  * SM, or a persistent work list (4..6 blocks per SM claiming 1, 2 or 4 tiles at a time from an
- * atomic ticket), and keeps the fastest; then the steps per CUDA graph (8, 32, 128 or 512: the
- * smallest within 1 % of the fastest); the first call with at least 64 shared-memory boxes picks
- * their block size. */
+ * atomic ticket), and keeps the fastest; then the steps per CUDA graph of the tiled boxes' launches
+ * (8, 32 or 128: the smallest within 1 % of the fastest; the shared-memory boxes step a whole call
+ * in one launch); the first call with at least 64 shared-memory boxes picks their block size. */
 typedef struct {
     int tuned;                    /* 1 once the tiled launches were tuned */
     int aa_work_list[2];          /* even, odd launch: 1 persistent work list, 0 block per tile */

@@ -453,13 +453,15 @@ int tune_aa(lbgpu_batch *b)
     }
     b->tuned_fluid = fluid;
     // steps per graph: a call's steps run as graphs of S steps (the last one holds the rest); S
-    // is the smallest of 8, 32, 128, 512 whose 512 steps (AA launches on the scratch copies) take
-    // no more than 1 % longer than the fastest S (graph launches cost a few microseconds, while
-    // a smaller S lets the host act sooner on a long call)
+    // is the smallest of 8, 32, 128 whose 128 steps (AA launches on the scratch copies) take no
+    // more than 1 % longer than the fastest S (graph launches cost a few microseconds, while a
+    // smaller S lets the host act sooner on a long call and keeps the graphs small).  The tuning
+    // runs inside the first call, so it is kept short: about 550 launches.
     {
-        float tS[4];
-        const int Ss[4] = {8, 32, 128, 512};
-        for (int q = 0; q < 4; ++q) {
+        constexpr int NS = 3, TS = 128;
+        float tS[NS];
+        const int Ss[NS] = {8, 32, 128};
+        for (int q = 0; q < NS; ++q) {
             cudaGraph_t g;
             cudaGraphExec_t ex;
             LBB_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -476,14 +478,14 @@ int tune_aa(lbgpu_batch *b)
             LBB_CK(ie);
             LBB_CK(cudaGraphLaunch(ex, s));   // warm-up
             LBB_CK(cudaEventRecord(b->ev0, s));
-            for (int k = 0; k < 512 / Ss[q]; ++k) LBB_CK(cudaGraphLaunch(ex, s));
+            for (int k = 0; k < TS / Ss[q]; ++k) LBB_CK(cudaGraphLaunch(ex, s));
             LBB_CK(cudaEventRecord(b->ev1, s));
             LBB_CK(cudaEventSynchronize(b->ev1));
             LBB_CK(cudaEventElapsedTime(&tS[q], b->ev0, b->ev1));
             cudaGraphExecDestroy(ex);
         }
-        const float fastest = *std::min_element(tS, tS + 4);
-        for (int q = 0; q < 4; ++q)
+        const float fastest = *std::min_element(tS, tS + NS);
+        for (int q = 0; q < NS; ++q)
             if (tS[q] <= 1.01f * fastest) {
                 b->steps_per_graph = Ss[q];
                 break;
