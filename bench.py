@@ -520,8 +520,9 @@ def bench_serving(a):
     p50/p99 latency (arrival to finish) and solves/s, over all requests, over those whose flow
     converged and over those that reached the step cap, and per family; the same stream served
     one request at a time (each alone, back to back) as the no-batching baseline of the highest
-    rate, with each family's share of that time (the large cavities and touching-sphere cells are
-    HBM-bound alone and in the mix, so they bound the gain of batching: the Amdahl bound below)."""
+    rate, with each family's share of that time; and each family's requests of that stream served
+    together on their own (all arrived), so that each family's gain from batching shows which
+    families bound the whole stream's."""
     from laboetie_gb300 import workloads as wl
     from laboetie_gb300.lbgpu import Batch
 
@@ -571,14 +572,21 @@ def bench_serving(a):
                     b.serve([dict(q, arrival=0.0)], du_tol=1e-8, check_every=100)
                 fam_time[f] = fam_time.get(f, 0.0) + time.perf_counter() - t1
             t_fifo = time.perf_counter() - t
-            # Amdahl bound of batching: the time the families that batching cannot speed up
-            # (their boxes keep the device busy alone) take one at a time, against the whole
-            big = sum(v for f, v in fam_time.items() if f in ("cc", "cavity"))
+            # each family batched on its own: its requests all arrived, served together
+            fam_batched = {}
+            for f in sorted(set(fams)):
+                group = [dict(q, arrival=0.0) for q, g in zip(reqs, fams) if g == f]
+                t1 = time.perf_counter()
+                with Batch() as b:
+                    b.serve(group, du_tol=1e-8, check_every=100)
+                fam_batched[f] = time.perf_counter() - t1
             fifo = {"solves_per_s": round(len(reqs) / t_fifo, 3), "seconds": round(t_fifo, 2),
                     "family_seconds": {f: round(v, 2) for f, v in sorted(fam_time.items())},
-                    "share_of_large_families": round(big / t_fifo, 3),
-                    "speedup_bound_if_large_families_gain_nothing": round(t_fifo / big, 2) if big > 0 else None,
-                    "what": "the highest-rate stream, each request served alone, back to back"}
+                    "family_share": {f: round(v / t_fifo, 3) for f, v in sorted(fam_time.items())},
+                    "family_seconds_batched_alone": {f: round(v, 2) for f, v in sorted(fam_batched.items())},
+                    "family_gain_batched_alone": {f: round(fam_time[f] / v, 2) for f, v in sorted(fam_batched.items())},
+                    "what": "the highest-rate stream, each request served alone, back to back; then "
+                            "each family's requests of it served together on their own"}
     return {"metric": "served solves/s, p50/p99 latency", "rates": out, "one_at_a_time": fifo,
             "config": {"workload": "Poisson arrivals; slit 4x4x(16..128), cylinder z (16..96)^2 x 32 "
                                    "r = lx/2-2, touching spheres cubic cell 32..96, spherical cavity "
