@@ -216,10 +216,9 @@ int lbgpu_host_unregister(void *ptr);
  * j_old on entry and j on exit; *l2err (host, optional) = max|j - j_old|.  Outputs and status
  * bits are those of lbgpu_moments, non-finite input included.  Boxes of more than
  * 16,777,216 nodes (256^3) are rejected (LBGPU_ERR_INVALID): the reduction scratch is a fixed
- * ~1 MiB device array per GPU, shared by all calls, so calls that overlap on the GPU race.  The
- * first call on each device looks up that array's address; make it before any stream capture.
- * stream: a cudaStream_t, or NULL for the default stream.  Every call ends by waiting for its
- * stream. */
+ * ~1 MiB device array per GPU, shared by all calls, so calls that overlap on the GPU race.
+ * stream: a cudaStream_t, or NULL for the default stream.  Every call waits for its stream
+ * before it returns, so it cannot be captured into a CUDA graph. */
 int lbgpu_moments_noalloc(int lx, int ly, int lz, const double *d_n, const double *d_fx,
                           const double *d_fy, const double *d_fz, double *d_density,
                           double *d_jx, double *d_jy, double *d_jz, double *l2err, void *stream);

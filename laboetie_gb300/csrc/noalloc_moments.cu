@@ -19,9 +19,8 @@
 // serialised by the caller.
 //
 // The host side needs the device address of the array.  The first call on each device looks
-// it up (cudaGetSymbolAddress, with that device current) and caches it; that first call should
-// therefore be made before any stream capture the caller might begin.  Every call ends by
-// copying l2err back and waiting for its stream.
+// it up (cudaGetSymbolAddress, with that device current) and caches it.  Every call ends by
+// copying l2err back and waiting for its stream, so no call can be captured into a CUDA graph.
 //
 // Results match lbgpu_moments bit for bit, including on non-finite input: l2err is a maximum
 // over IEEE bit patterns (a NaN difference gives a NaN l2err), and a NaN or infinite population
