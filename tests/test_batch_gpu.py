@@ -30,13 +30,19 @@ def _cells():
     ]
 
 
-def _run(cells, idx, flow_steps, mp_steps):
-    """Run the cells idx together; returns {i: (rho, j, mp_get, mp_fields)}."""
+def _run(cells, idx, flow_steps, mp_steps, du=None):
+    """Run the cells idx together; returns {i: (rho, j, mp_get, mp_fields)}.  With a dict du, the
+    flow steps end with a checked call whose max|u - u_prev| per box goes into du."""
     out = {}
     with Batch() as b:
         ids = {i: b.add(cells[i][0], relaxation_time=1.0, f_ext=cells[i][1],
                         tracer=dict(TR, f_ext=cells[i][1])) for i in idx}
-        b.steps(flow_steps)
+        if du is None:
+            b.steps(flow_steps)
+        else:
+            b.steps(flow_steps - 100)
+            d = b.steps(100, check=True)
+            du.update({i: d[ids[i]] for i in idx})
         mom = {i: b.moments(ids[i]) for i in idx}
         for i in idx:
             b.mp_start(ids[i])
@@ -94,11 +100,13 @@ def test_batch_work_list_launch_equals_one_block_per_tile(monkeypatch, variant):
     """The persistent work-list form of the tiled in-place step (blocks per SM, tiles claimed at a
     time, steps per graph forced through LBGPU_BATCH_AA_LIST) gives every box the same bits as one
     block per tile: the tiles are claimed in another order and by other blocks, but each node's
-    arithmetic is the same.  The call's steps also run as several graphs: the flow state, P, P_ads,
-    VACF(0) and the last step's VACF are bit-identical; the VACF sum of a box held in shared memory
-    is added up per launch, so its FP64 grouping follows the steps per graph (1e-12 relative)."""
+    arithmetic is the same.  The call's steps also run as several graphs of the tiled launches,
+    while the shared-memory boxes step the whole call in one launch of their own: the flow state,
+    the convergence measure of a checked call, P, P_ads and the VACF (sum included) are
+    bit-identical."""
     cells = _cells()
-    base = _run(cells, range(len(cells)), 300, 200)
+    du_base, du_listed = {}, {}
+    base = _run(cells, range(len(cells)), 300, 200, du_base)
     monkeypatch.setenv("LBGPU_BATCH_AA_LIST", variant)
     with Batch() as b:
         b.add(cells[3][0], f_ext=cells[3][1])
@@ -107,13 +115,10 @@ def test_batch_work_list_launch_equals_one_block_per_tile(monkeypatch, variant):
     minb, tpc, spg = (int(v) for v in variant.split(","))
     assert t["aa_work_list"] == [1, 1] and t["aa_min_blocks"] == [minb, minb]
     assert t["aa_tiles_per_claim"] == [tpc, tpc] and t["steps_per_graph"] == spg
-    listed = _run(cells, range(len(cells)), 300, 200)
+    listed = _run(cells, range(len(cells)), 300, 200, du_listed)
+    assert du_listed == du_base and all(v > 0 for v in du_base.values())
     for i in range(len(cells)):
-        (ra, ja, ma, fa), (rb, jb, mb, fb) = listed[i], base[i]
-        assert np.array_equal(ra, rb) and all(np.array_equal(ja[d], jb[d]) for d in range(3))
-        assert np.array_equal(fa[0], fb[0]) and np.array_equal(fa[1], fb[1])
-        assert np.array_equal(ma[0], mb[0]) and np.array_equal(ma[2], mb[2]) and ma[3] == mb[3]
-        assert np.allclose(ma[1], mb[1], rtol=1e-12, atol=1e-12 * np.abs(mb[0]).max())
+        _same(listed[i], base[i])
 
 
 def test_batch_flow_reaches_the_fp64_steady_state(oracle_mod):
