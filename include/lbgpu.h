@@ -264,8 +264,18 @@ int lbgpu_mp_init_charged(lbgpu_ctx *ctx, const lbgpu_tracer *tracer, const doub
 int lbgpu_mp_propagate(lbgpu_ctx *ctx, int nsteps, double *vacf, int *steps_done,
                        int *is_converged);
 
-/* Current P(3,lx,ly,lz) and adsorbed part (zeros when no adsorption); either may be NULL. */
+/* Current P(3,lx,ly,lz) and adsorbed part (zeros when no adsorption); either may be NULL.
+ * Together with lbgpu_mp_set: a checkpoint of the tracer phase. */
 int lbgpu_mp_get(lbgpu_ctx *ctx, double *P, double *P_ads);
+
+/* Resume a tracer phase from a checkpoint (no counterpart in the reference, which has none):
+ * after lbgpu_mp_init with the same tracer on the same flow moments, P and (with adsorption, else
+ * ignored and may be NULL) P_ads become the propagated quantity, as lbgpu_mp_get returned them,
+ * and it_next (>= 1) the reference's step counter it of the next lbgpu_mp_propagate (its
+ * convergence test starts at it > 2).  K steps, lbgpu_mp_get, then lbgpu_mp_init + lbgpu_mp_set
+ * in another context and K more steps give the bits of 2K steps in one run (FP32 values make the
+ * round trip through FP64 exactly). */
+int lbgpu_mp_set(lbgpu_ctx *ctx, const double *P, const double *P_ads, int it_next);
 
 /* deallocate_propagated_quantity (module_moment_propagation.f90:350-353). */
 int lbgpu_mp_release(lbgpu_ctx *ctx);

@@ -438,6 +438,45 @@ int lbgpu_mp_get(lbgpu_ctx *ctx, double *P, double *P_ads)
     return LBGPU_OK;
 }
 
+int lbgpu_mp_set(lbgpu_ctx *ctx, const double *P, const double *P_ads, int it_next)
+{
+    if (!ctx) return LBGPU_ERR_INVALID;
+    MpState *s = ctx->mp;
+    if (!s) return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_mp_set: call lbgpu_mp_init first");
+    if (!P || it_next < 1 || (s->ads && !P_ads))
+        return ctx_fail(ctx, LBGPU_ERR_INVALID, "lbgpu_mp_set: P (and P_ads with adsorption) and it_next >= 1");
+    const long long N = ctx->N;
+    cudaStream_t st = ctx->stream;
+    MpCtl c;
+    LBG_CK(ctx, cudaMemcpyAsync(&c, s->a64.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
+    LBG_CK(ctx, cudaStreamSynchronize(st));
+    const int par = c.parity;   // the buffers the next step reads
+    const double *ins[2] = {P, s->ads ? P_ads : nullptr};
+    for (int q = 0; q < 2; ++q) {
+        if (!ins[q]) continue;
+        if (s->prec == LBGPU_FP64) {
+            std::vector<double> comp((size_t)3 * N);
+            for (long long i = 0; i < N; ++i)
+                for (int d = 0; d < 3; ++d) comp[d * N + i] = ins[q][3 * i + d];
+            for (int d = 0; d < 3; ++d) {
+                double *dst = q == 0 ? s->a64.P[par][d] : s->a64.A[par][d];
+                LBG_CK(ctx, cudaMemcpyAsync(dst, comp.data() + d * N, sizeof(double) * N, cudaMemcpyHostToDevice, st));
+            }
+            LBG_CK(ctx, cudaStreamSynchronize(st));   // comp goes out of scope
+        } else {
+            std::vector<float4> f(N);
+            for (long long i = 0; i < N; ++i)
+                f[i] = make_float4((float)ins[q][3 * i], (float)ins[q][3 * i + 1], (float)ins[q][3 * i + 2], 0.0f);
+            float4 *dst = q == 0 ? s->a32.P[par] : s->a32.A[par];
+            LBG_CK(ctx, cudaMemcpyAsync(dst, f.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, st));
+            LBG_CK(ctx, cudaStreamSynchronize(st));
+        }
+    }
+    s->it_next = it_next;
+    s->converged = 0;
+    return LBGPU_OK;
+}
+
 int lbgpu_mp_release(lbgpu_ctx *ctx)
 {
     if (!ctx) return LBGPU_ERR_INVALID;

@@ -111,6 +111,7 @@ def library():
         ("lbgpu_mp_init_charged", [vp, C.POINTER(Tracer), vp, vp, vp, vp, vp]),
         ("lbgpu_mp_propagate", [vp, i, vp, pi, pi]),
         ("lbgpu_mp_get", [vp, vp, vp]),
+        ("lbgpu_mp_set", [vp, vp, vp, i]),
         ("lbgpu_mp_release", [vp]),
         ("lbgpu_time_mp_steps", [vp, i, C.POINTER(C.c_float)]),
         ("lbgpu_pnp_init", [vp, C.POINTER(PnpParams), C.POINTER(d)]),
@@ -351,6 +352,15 @@ def _mp_get(self):
     return P, A
 
 
+def _mp_set(self, P, P_ads=None, it_next=1):
+    """Resume the tracer phase from (P, P_ads) as mp_get returned them, the next step being the
+    reference's step it_next (after mp_init with the same tracer on the same flow)."""
+    P = np.ascontiguousarray(P, dtype=np.float64).reshape(self.shape + (3,))
+    A = None if P_ads is None else np.ascontiguousarray(P_ads, dtype=np.float64).reshape(self.shape + (3,))
+    self._chk(self.L.lbgpu_mp_set(self.ctx, _ptr(P), _ptr(A) if A is not None else None, int(it_next)),
+              "mp_set")
+
+
 def _time_mp_steps(self, nsteps):
     ms = C.c_float(0)
     self._chk(self.L.lbgpu_time_mp_steps(self.ctx, nsteps, C.byref(ms)), "time_mp_steps")
@@ -360,6 +370,7 @@ def _time_mp_steps(self, nsteps):
 Box.mp_init = _mp_init
 Box.mp_propagate = _mp_propagate
 Box.mp_get = _mp_get
+Box.mp_set = _mp_set
 Box.time_mp_steps = _time_mp_steps
 Box.mp_release = lambda self: self._chk(self.L.lbgpu_mp_release(self.ctx), "mp_release")
 
