@@ -73,7 +73,12 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if errs:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
-    if _stale(LIB, objs):
+    # objects of translation units that no longer exist: dropped, and the library relinked
+    gone = [os.path.join(OUT_DIR, f) for f in os.listdir(OUT_DIR) if f.endswith(".o")]
+    gone = [o for o in gone if o not in objs]
+    for o in gone:
+        os.remove(o)
+    if gone or _stale(LIB, objs):
         cmd = [cc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", LIB, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
