@@ -41,7 +41,7 @@ BYTES_F32 = 38 * 4   # 19 reads + 19 writes of one FP32 deviation per fluid node
 BYTES_F64 = 38 * 8
 WORKLOAD = "D3Q19 porous 192^3 spheres r=8 porosity 0.60 seed 20261203, tau 0.8, f_ext (1e-6,0,0)"
 METRIC = "D3Q19 MLUPS (fluid-node updates per microsecond)"
-E2E_REPS = 3          # end-to-end runs of the whole job; the median is reported
+E2E_REPS = 3          # end-to-end runs of the whole job after one untimed one; the median is reported
 
 
 def args_():
@@ -703,17 +703,19 @@ def main():
         rc = L.lbgpu_host_register(h.ctypes.data, h.nbytes)
         if rc:
             raise RuntimeError("cudaHostRegister failed")
-    # the whole job E2E_REPS times (the host side of a transfer varies from run to run on a shared
-    # host): the median is reported, every repetition in "runs"
+    # the whole job once untimed (the first transfers from newly registered host memory pay a
+    # one-time cost of some 25 ms), then E2E_REPS times: the median is reported, every timed
+    # repetition in "runs"
     reps = []
-    for _ in range(E2E_REPS):
+    for k in range(E2E_REPS + 1):
         barrier(dist)
         t0 = time.perf_counter()
         box.flow_set(n0, rho0, j0)
         box.flow_steps(K, force_on=True)
         rc = L.lbgpu_flow_get(box.ctx, None, rhos.ctypes.data, *(x.ctypes.data for x in js))
         box.sync()
-        reps.append(max_over_ranks(dist, time.perf_counter() - t0))
+        if k:
+            reps.append(max_over_ranks(dist, time.perf_counter() - t0))
         if rc:
             break
     clocks_out = clocks.stop()
@@ -728,14 +730,15 @@ def main():
         if L.lbgpu_host_register(h.ctypes.data, h.nbytes):
             raise RuntimeError("cudaHostRegister failed")
     reps64 = []
-    for _ in range(E2E_REPS):
+    for k in range(E2E_REPS + 1):
         barrier(dist)
         t0 = time.perf_counter()
         box64f.flow_set(n0, rho0, j0)
         box64f.flow_steps(K64, force_on=True)
         rc = L.lbgpu_flow_get(box64f.ctx, None, rhos.ctypes.data, *(x.ctypes.data for x in js))
         box64f.sync()
-        reps64.append(max_over_ranks(dist, time.perf_counter() - t0))
+        if k:
+            reps64.append(max_over_ranks(dist, time.perf_counter() - t0))
         if rc:
             break
     t_e2e64 = float(np.median(reps64))
@@ -796,7 +799,7 @@ def main():
                     "runs": [round(world * nfluid * K64 / t / 1e6, 2) for t in reps64],
                     "what": "FP64 fused context: lbgpu_flow_set (n, density, j from pinned host) + "
                             f"{K64} steps + lbgpu_flow_get (density, j to pinned host), wall clock, "
-                            f"median of {len(reps64)} runs"},
+                            f"median of {len(reps64)} runs after an untimed one"},
             "strict": {"value": round(mlups64, 2), "unit": "MLUPS", "steps": K64,
                        "ms_per_step": round(ms_step64, 4),
                        "hbm_frac": round(achieved64 / hbm, 4)},
@@ -819,7 +822,8 @@ def main():
                 "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
                 "runs": [round(world * nfluid * K / t / 1e6, 2) for t in reps],
                 "what": "lbgpu_flow_set (n, density, j from pinned host) + K fused steps + "
-                        f"lbgpu_flow_get (density, j to pinned host), wall clock, median of {len(reps)} runs"},
+                        f"lbgpu_flow_get (density, j to pinned host), wall clock, median of {len(reps)} runs "
+                        "after an untimed one"},
         "gpu_launches": K,   # the timed region: K k_aa32 launches (a graph of even + odd, K/2 times)
         "clocks": clocks_out,
         "cpu_baseline": cpu,
