@@ -112,8 +112,11 @@ size_t footprint_bound(long long N, int lx, int ly, int lz, bool tracer, bool ad
 
 struct lbgpu_batch {
     int device = 0;
-    cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr, join = nullptr;
+    // side: the shared-memory boxes in the flow phase, side2: those in the tracer phase, side3:
+    // the tiled boxes in the tracer phase while tiled boxes are also in the flow phase
+    cudaStream_t stream = nullptr, side = nullptr, side2 = nullptr, side3 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, fork = nullptr, join = nullptr, join2 = nullptr;
+    cudaEvent_t fork_mp = nullptr, join_mp = nullptr;
     size_t budget = 0, used = 0;
     int smem_max = BATCH_SMEM_BYTES_MAX;
     std::vector<Slot> slots;
@@ -282,15 +285,29 @@ int launch_aa(lbgpu_batch *b, const BatchInst *insts, int odd, cudaStream_t s)
     return LBGPU_OK;
 }
 
-// The shared-memory boxes' launch for nsteps steps on the side stream, forked from the main one
-// (the main stream waits on b->join for it).
+// The shared-memory boxes' launches for nsteps steps, forked from the main stream: the flow-phase
+// boxes on the side stream and the tracer-phase ones on the second side stream, concurrently (one
+// block per box, on disjoint boxes; in sequence a call of a batch in both phases cost the sum of
+// the two).  The main stream waits for both (join_smem).
 int enqueue_smem(lbgpu_batch *b, int nsteps, bool check)
 {
+    const int nflow = b->nsmem_flow, nmp = b->nsmem - b->nsmem_flow;
     LBB_CK(cudaEventRecord(b->fork, b->stream));
     LBB_CK(cudaStreamWaitEvent(b->side, b->fork, 0));
-    LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, b->nsmem_flow, b->nsmem - b->nsmem_flow, nsteps, check,
-                             b->d_du, b->smem_bytes_flow, b->smem_bytes_mp, b->smem_threads, b->side));
+    LBB_CK(cudaStreamWaitEvent(b->side2, b->fork, 0));
+    LBB_CK(launch_batch_smem(b->d_insts, b->d_smem, nflow, 0, nsteps, check, b->d_du, b->smem_bytes_flow,
+                             b->smem_bytes_mp, b->smem_threads, b->side));
+    LBB_CK(launch_batch_smem(b->d_insts, b->d_smem + nflow, 0, nmp, nsteps, check, b->d_du, b->smem_bytes_flow,
+                             b->smem_bytes_mp, b->smem_threads, b->side2));
     LBB_CK(cudaEventRecord(b->join, b->side));
+    LBB_CK(cudaEventRecord(b->join2, b->side2));
+    return LBGPU_OK;
+}
+
+int join_smem(lbgpu_batch *b)
+{
+    LBB_CK(cudaStreamWaitEvent(b->stream, b->join, 0));
+    LBB_CK(cudaStreamWaitEvent(b->stream, b->join2, 0));
     return LBGPU_OK;
 }
 
@@ -301,8 +318,10 @@ int clear_du(lbgpu_batch *b)
 }
 
 // The launches of one call (or, with smem = false, of a part of a call whose shared-memory boxes
-// run in a launch of their own): the shared-memory boxes on the side stream, concurrently with the
-// per-step launches of the tiled boxes on the main stream.
+// run in a launch of their own): the shared-memory boxes on the side streams, concurrently with the
+// per-step launches of the tiled boxes: those of the flow-phase boxes on the main stream and, when
+// both phases hold tiled boxes, those of the tracer-phase boxes as a second chain on the third
+// side stream (the two chains step disjoint boxes and meet at the end of the call).
 int enqueue_steps(lbgpu_batch *b, int nsteps, bool check, bool smem)
 {
     cudaStream_t s = b->stream;
@@ -310,13 +329,28 @@ int enqueue_steps(lbgpu_batch *b, int nsteps, bool check, bool smem)
         if (int rc = clear_du(b)) return rc;
     if (b->nsmem && smem)
         if (int rc = enqueue_smem(b, nsteps, check)) return rc;
+    const bool flow_tiles = b->nflow > 0, mp_tiles = b->nmp + b->nslab > 0;
+    cudaStream_t ms = s;
+    if (flow_tiles && mp_tiles) {
+        LBB_CK(cudaEventRecord(b->fork_mp, s));
+        LBB_CK(cudaStreamWaitEvent(b->side3, b->fork_mp, 0));
+        ms = b->side3;
+    }
     for (int t = 0; t < nsteps; ++t) {
-        if (int rc = launch_aa(b, b->d_insts, t & 1, s)) return rc;
-        LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, s));
-        LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, s));
+        if (flow_tiles)
+            if (int rc = launch_aa(b, b->d_insts, t & 1, s)) return rc;
+        if (mp_tiles) {
+            LBB_CK(launch_batch_mp(b->d_insts, b->d_tiles + b->nflow, b->nmp, t & 1, ms));
+            LBB_CK(launch_batch_mp_slab(b->d_insts, b->d_tiles + b->nflow + b->nmp, b->nslab, t & 1, ms));
+        }
+    }
+    if (ms != s) {
+        LBB_CK(cudaEventRecord(b->join_mp, ms));
+        LBB_CK(cudaStreamWaitEvent(s, b->join_mp, 0));
     }
     if (check) LBB_CK(launch_batch_check(b->d_insts, b->d_tiles, b->nflow, b->d_du, s));
-    if (b->nsmem && smem) LBB_CK(cudaStreamWaitEvent(s, b->join, 0));
+    if (b->nsmem && smem)
+        if (int rc = join_smem(b)) return rc;
     return LBGPU_OK;
 }
 
@@ -585,7 +619,8 @@ int call_graphs(lbgpu_batch *b, int nsteps, bool check, bool launch)
         if (int rc = graph_of(b, n, check && left == 0, !split, &exec)) return rc;
         if (launch) LBB_CK(cudaGraphLaunch(exec, b->stream));
     }
-    if (split && launch) LBB_CK(cudaStreamWaitEvent(b->stream, b->join, 0));
+    if (split && launch)
+        if (int rc = join_smem(b)) return rc;
     return LBGPU_OK;
 }
 
@@ -644,10 +679,15 @@ int lbgpu_batch_create(int device, size_t memory_budget, lbgpu_batch **out)
     e = cudaMemGetInfo(&fr, &tot);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side3, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_mp, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join_mp, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_counts, 4 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_ticket, sizeof(BatchTicket));
     if (e == cudaSuccess) e = cudaMemset(b->d_ticket, 0, sizeof(BatchTicket));
@@ -676,6 +716,8 @@ void lbgpu_batch_destroy(lbgpu_batch *b)
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->side) cudaStreamSynchronize(b->side);
+    if (b->side2) cudaStreamSynchronize(b->side2);
+    if (b->side3) cudaStreamSynchronize(b->side3);
     drop_graphs(b);
     for (auto &sl : b->slots)
         if (sl.active) cudaFree(sl.mem);
@@ -685,9 +727,11 @@ void lbgpu_batch_destroy(lbgpu_batch *b)
     cudaFree(b->d_du);
     cudaFree(b->d_counts);
     cudaFree(b->d_ticket);
-    for (cudaEvent_t ev : {b->ev0, b->ev1, b->fork, b->join})
+    for (cudaEvent_t ev : {b->ev0, b->ev1, b->fork, b->join, b->join2, b->fork_mp, b->join_mp})
         if (ev) cudaEventDestroy(ev);
     if (b->side) cudaStreamDestroy(b->side);
+    if (b->side2) cudaStreamDestroy(b->side2);
+    if (b->side3) cudaStreamDestroy(b->side3);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
