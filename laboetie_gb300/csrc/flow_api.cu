@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -72,6 +73,29 @@ int build_compact_layout(lbgpu_ctx *ctx, const int8_t *nature)
     LBG_CK(ctx, launch_compact_mask(a, ctx->d_cmask, s));
     LBG_CK(ctx, cudaStreamSynchronize(s));   // host tables go out of scope
     return LBGPU_OK;
+}
+
+// dst[i] = src[i], 16 bytes per thread: a device copy of a host array read in place through its
+// page-locked mapping
+__global__ void k_copy16(const double2 *__restrict__ src, double2 *__restrict__ dst, size_t n2)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// Host -> device copy of `count` doubles: read in place by a kernel when the host range lies in
+// one range registered by lbgpu_host_register (the copy runs at the link's read bandwidth and
+// with the kernel's many loads in flight), else by cudaMemcpyAsync.
+cudaError_t upload_f64(double *dst, const double *src, size_t count, cudaStream_t s)
+{
+    const void *view = pinned_device_view(src, sizeof(double) * count);
+    if (view && count % 2 == 0 && ((uintptr_t)view & 15u) == 0 && ((uintptr_t)dst & 15u) == 0) {
+        const size_t n2 = count / 2;
+        const unsigned grid = (unsigned)std::min<size_t>((n2 + 255) / 256, 152u * 16u);
+        k_copy16<<<grid, 256, 0, s>>>(static_cast<const double2 *>(view), reinterpret_cast<double2 *>(dst), n2);
+        return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyHostToDevice, s);
 }
 
 // LBGPU_ERR_OOM unless `need` bytes are free on the device
@@ -276,11 +300,10 @@ int lbgpu_flow_set(lbgpu_ctx *ctx, const double *n, const double *density, const
     if (ctx->p.precision == LBGPU_FP32_DEV) return f32_flow_set(ctx, n, density, jx, jy, jz);
     const long long N = ctx->N;
     cudaStream_t s = ctx->stream;
-    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_f[1], n, sizeof(double) * Q * N, cudaMemcpyHostToDevice, s));
-    LBG_CK(ctx, cudaMemcpyAsync(ctx->d_rho, density, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    LBG_CK(ctx, upload_f64(ctx->d_f[1], n, (size_t)Q * N, s));
+    LBG_CK(ctx, upload_f64(ctx->d_rho, density, (size_t)N, s));
     const double *j[3] = {jx, jy, jz};
-    for (int d = 0; d < 3; ++d)
-        LBG_CK(ctx, cudaMemcpyAsync(ctx->d_j[d], j[d], sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    for (int d = 0; d < 3; ++d) LBG_CK(ctx, upload_f64(ctx->d_j[d], j[d], (size_t)N, s));
     FlowArgs64 a;
     fill_args64(ctx, a);
     a.parity = 1;

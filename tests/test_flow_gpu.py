@@ -7,7 +7,7 @@ The FP32-deviation path is checked against FP64 with the tolerance stated in eac
 import numpy as np
 import pytest
 
-from laboetie_gb300 import FP32_DEV, FP64, Box, LbgpuError
+from laboetie_gb300 import FP32_DEV, FP64, FP64_FUSED, Box, LbgpuError
 from laboetie_gb300 import geometry as geo
 
 pytestmark = pytest.mark.gpu
@@ -252,10 +252,12 @@ def test_fp32_in_place_and_two_buffer_streaming_agree(monkeypatch):
             assert np.array_equal(ja[d], jb[d])
 
 
-def test_fp32_flow_set_from_registered_host_memory():
-    """lbgpu_flow_set on an FP32 context converts populations page-locked by lbgpu_host_register
-    straight from host memory; the state is bit-identical to the one staged from pageable memory,
-    after the upload and after steps."""
+@pytest.mark.parametrize("prec", [FP32_DEV, FP64, FP64_FUSED])
+def test_flow_set_from_registered_host_memory(prec):
+    """lbgpu_flow_set reads host arrays page-locked by lbgpu_host_register in place (an FP32
+    context converts the populations straight from host memory, an FP64 one copies them with a
+    kernel reading through the mapping); the state is bit-identical to the one staged from
+    pageable memory, after the upload and after steps."""
     from laboetie_gb300 import library
 
     L = library()
@@ -266,19 +268,21 @@ def test_fp32_flow_set_from_registered_host_memory():
         n0, rho0, j0 = b64.flow_get()
     out = {}
     for pinned in (False, True):
-        n = n0.copy()
+        host = [n0.copy(), rho0.copy()] + [x.copy() for x in j0]
         if pinned:
-            assert L.lbgpu_host_register(n.ctypes.data, n.nbytes) == 0
+            for h in host:
+                assert L.lbgpu_host_register(h.ctypes.data, h.nbytes) == 0
         try:
-            with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 0.0, 0.0), precision=FP32_DEV) as box:
+            with Box(nat, relaxation_time=0.8, f_ext=(1e-5, 0.0, 0.0), precision=prec) as box:
                 box.flow_init()
-                box.flow_set(n, rho0, j0)
+                box.flow_set(host[0], host[1], tuple(host[2:]))
                 first = box.flow_get()
                 box.flow_steps(7, force_on=True)
                 out[pinned] = (first, box.flow_get())
         finally:
             if pinned:
-                L.lbgpu_host_unregister(n.ctypes.data)
+                for h in host:
+                    L.lbgpu_host_unregister(h.ctypes.data)
     for (na, ra, ja), (nb, rb, jb) in zip(out[False], out[True]):
         assert np.array_equal(na, nb) and np.array_equal(ra, rb)
         assert all(np.array_equal(ja[d], jb[d]) for d in range(3))
