@@ -473,6 +473,7 @@ def bench_batched(a):
         tot_nf = sum(int((n == 0).sum()) for n, _, g in cells if g == f)
         rate = sum(x[1] for x in fam[f]) / sum(x[0] for x in fam[f])   # fluid nodes per second
         t_one += tot_nf / rate
+    smem_rate = smem_cells_rate(cells, tracer)
     n_solves = len(cells)
     one = None
     if t_one > 0:
@@ -497,8 +498,39 @@ def bench_batched(a):
         "speedup_vs_one_at_a_time": round(t_one / dt, 2) if one else None,
         "tuning": tuning,
         "roofline_tiled_flow": batch_roofline(tuning),
+        "shared_memory_cells": smem_rate,
         "d_eff_cell0": deff_cell0,
     }
+
+
+def smem_cells_rate(cells, tracer):
+    """The shared-memory kernels alone: the batch's chromatography cells (each held in one block's
+    shared memory for all the steps of a call), flow and tracer steps timed with CUDA events.  Such
+    a step touches HBM only at the ends of a call, so it is bound by the SM's issue, not by HBM:
+    the rate is set beside the HBM rate the same in-place step would need from HBM (152 B per
+    fluid node)."""
+    from laboetie_gb300.lbgpu import Batch
+
+    sub = [c for c in cells if c[2] == "cell"]
+    if not sub:
+        return None
+    hbm, kind = peaks()
+    with Batch() as b:
+        ids = [b.add(n, f_ext=fe, tracer=tracer(fe)) for n, fe, _ in sub]
+        fluid = b.info()["fluid_nodes"]
+        b.steps(100)
+        ms_f = b.time_steps(500)
+        for i in ids:
+            b.mp_start(i)
+        b.steps(100)
+        ms_m = b.time_steps(500)
+    flow = fluid * 500 / (ms_f * 1e-3)
+    return {"cells": len(sub), "fluid_nodes": fluid, "bound": "issue (one block per cell, state in shared memory)",
+            "flow_node_steps_per_s": round(flow / 1e9, 2), "tracer_node_steps_per_s": round(fluid * 500 / (ms_m * 1e-3) / 1e9, 2),
+            "unit": "G fluid-node steps/s",
+            "hbm_equivalent_gbs": round(BYTES_F32 * flow / 1e9, 1), "hbm_peak_gbs": hbm,
+            "hbm_equivalent_frac": round(BYTES_F32 * flow / 1e9 / hbm, 3),
+            "note": "flow rate x 152 B per fluid node: the HBM bandwidth the same step would need from HBM"}
 
 
 def batch_roofline(t):
