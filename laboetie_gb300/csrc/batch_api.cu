@@ -782,7 +782,10 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
         return bfail(LBGPU_ERR_INVALID, "lbgpu_batch_add: box shape beyond the packed-position limits");
     if (compact && pos.empty()) return bfail(LBGPU_ERR_INVALID, "All nodes are solid: no fluid, no fluid dynamics!");
     const long long units = compact ? (long long)pos.size() : N;
-    const int nslab = compact && tracer ? batch_slab_tiles(c->lx, c->ly, c->lz) : 0;
+    // LBGPU_BATCH_SLAB=0: tiled boxes take node tiles in the tracer phase too (same bits)
+    const char *slab_env = std::getenv("LBGPU_BATCH_SLAB");
+    const bool slab_ok = !(slab_env && std::string(slab_env) == "0");
+    const int nslab = compact && tracer && slab_ok ? batch_slab_tiles(c->lx, c->ly, c->lz) : 0;
     const int ntacc = std::max((int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK), nslab);
     const Layout L = layout(N, units, (long long)tab.size(), ntacc, compact, tracer, ads);
     if (b->used + L.total > b->budget)
