@@ -71,6 +71,41 @@ def test_batch_box_alone_equals_box_in_mix():
         _same(alone[i], mix[i])
 
 
+def test_batch_boxes_in_both_phases_at_once_equal_their_runs_alone():
+    """While some boxes are in the tracer phase and the others still in the flow phase, a call
+    runs the two phases' launches as concurrent chains (the shared-memory boxes of each phase on
+    their own stream, the tiled boxes' tracer steps on a third stream beside the flow steps): each
+    box's moments, VACF and tracer fields are bit-identical to its run alone with the same
+    schedule (a shared-memory cell and a tiled tube start their tracer after 100 steps, the rest
+    after 300)."""
+    cells = _cells()
+    early = {0, 3}
+
+    def run(idx):
+        out = {}
+        with Batch() as b:
+            ids = {i: b.add(cells[i][0], relaxation_time=1.0, f_ext=cells[i][1],
+                            tracer=dict(TR, f_ext=cells[i][1])) for i in idx}
+            b.steps(100)
+            mom = {i: b.moments(ids[i]) for i in idx if i in early}
+            for i in idx:
+                if i in early:
+                    b.mp_start(ids[i])
+            b.steps(200)                  # both phases in every call
+            mom.update({i: b.moments(ids[i]) for i in idx if i not in early})
+            for i in idx:
+                if i not in early:
+                    b.mp_start(ids[i])
+            b.steps(100)
+            for i in idx:
+                out[i] = mom[i] + (b.mp_get(ids[i]), b.mp_fields(ids[i]))
+        return out
+
+    mix = run(range(len(cells)))
+    for i in range(len(cells)):
+        _same(run([i])[i], mix[i])
+
+
 def test_batch_shared_memory_and_tiled_paths_agree(monkeypatch):
     """The shared-memory and the tiled kernels do the same per-node arithmetic: the flow state
     and the tracer's P and P_ads are bit-identical.  The VACF terms are summed per thread in FP32
