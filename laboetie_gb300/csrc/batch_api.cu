@@ -44,6 +44,9 @@ struct Slot {
     bool tracer = false;
     int ntile = 0;            // tiles with VACF accumulators (256-node tiles or slab tiles)
     int mp_steps = 0;
+    // slab tiles of the tracer phase that hold a fluid node (a tile of solid nodes only has
+    // nothing to step: it writes no P and adds nothing to the VACF, whose accumulators start at 0)
+    std::vector<int> slab_live;
 };
 
 struct GraphEntry {
@@ -237,8 +240,7 @@ int rebuild(lbgpu_batch *b)
                 bytes_mp = std::max(bytes_mp, batch_smem_mp(sl.d.N, sl.d.ads));
             }
         } else if (sl.d.phase == BATCH_MP && sl.d.zc > 0) {
-            const int n = batch_slab_tiles(sl.d.lx, sl.d.ly, sl.d.lz);
-            for (int k = 0; k < n; ++k) slab.push_back({id, k});
+            for (int k : sl.slab_live) slab.push_back({id, k});
         } else {
             auto &list = sl.d.phase == BATCH_FLOW ? flow : mp;
             const int units = (int)batch_units(sl.d);
@@ -787,6 +789,22 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
     const bool slab_ok = !(slab_env && std::string(slab_env) == "0");
     const int nslab = compact && tracer && slab_ok ? batch_slab_tiles(c->lx, c->ly, c->lz) : 0;
     const int ntacc = std::max((int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK), nslab);
+    sl.slab_live.clear();
+    if (nslab) {   // slab tile k: column tile k % nxy (32 x 8), planes [zc (k / nxy), + zc)
+        const int tx = (c->lx + 31) / 32, nxy = tx * ((c->ly + 7) / 8);
+        for (int k = 0; k < nslab; ++k) {
+            const int t = k % nxy, x0 = (t % tx) * 32, y0 = (t / tx) * 8, z0 = (k / nxy) * BATCH_SLAB_ZC;
+            bool fluid = false;
+            for (int z = z0; z < std::min(z0 + BATCH_SLAB_ZC, c->lz) && !fluid; ++z)
+                for (int y = y0; y < std::min(y0 + 8, c->ly) && !fluid; ++y)
+                    for (int x = x0; x < std::min(x0 + 32, c->lx); ++x)
+                        if (nature[(size_t)x + (size_t)c->lx * ((size_t)y + (size_t)c->ly * z)] == 0) {
+                            fluid = true;
+                            break;
+                        }
+            if (fluid) sl.slab_live.push_back(k);
+        }
+    }
     const Layout L = layout(N, units, (long long)tab.size(), ntacc, compact, tracer, ads);
     if (b->used + L.total > b->budget)
         return bfail(LBGPU_ERR_OOM, "lbgpu_batch_add: box needs " + std::to_string(L.total >> 20) +
