@@ -80,6 +80,11 @@ struct MpArgs32 {
     // and elec_slope for the per-link fermi factors (the grid-stride step is used)
     int charged;
     float lw[3], z, inv_pstat, E[3];
+    // the fluid nodes of an in-place (AA) FP32 context: their packed positions (compact.cuh), which
+    // the grid-stride step walks (one thread per fluid node), or null (every lattice node)
+    const uint32_t *cpos;
+    unsigned Nf;
+    int xbits, ybits;
     // bounded waits of the slab step's bulk copies: the limit (ns); skip_copies (set only by a
     // test, LBGPU_MP_TEST_SKIP_COPIES=1) arms each plane's barrier without issuing its copies, so
     // the wait runs out and the step reports LBGPU_ERR_TIMEOUT without any fault

@@ -248,6 +248,12 @@ int mp_init_impl(lbgpu_ctx *ctx, const lbgpu_tracer *tr, const double *density, 
         // LBGPU_MP_SLAB=0: the grid-stride step everywhere (same per-node arithmetic)
         const char *slab_env = std::getenv("LBGPU_MP_SLAB");
         b.slab = !(slab_env && std::string(slab_env) == "0");
+        if (ctx->aa && ctx->d_cpos) {   // in-place context: walk its fluid nodes
+            b.cpos = ctx->d_cpos;
+            b.Nf = ctx->Nf;
+            b.xbits = ctx->xbits;
+            b.ybits = ctx->ybits;
+        }
         b.slab_resident = resident;
         b.ka = (float)tr->ka;
         b.kd = (float)tr->kd;

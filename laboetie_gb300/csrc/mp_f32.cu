@@ -66,12 +66,27 @@ __global__ void __launch_bounds__(MP_BLOCK) k_mp32(const MpArgs32 a, float bw)
     float vt[3] = {0.0f, 0.0f, 0.0f};
     unsigned bad = 0;
     const unsigned N = (unsigned)a.N;
-    for (unsigned r = blockIdx.x * MP_BLOCK + threadIdx.x; r < N; r += gridDim.x * MP_BLOCK) {
+    // the fluid nodes through their packed positions (every lane of a warp works), else every
+    // lattice node
+    const unsigned n_it = a.cpos ? a.Nf : N;
+    for (unsigned i = blockIdx.x * MP_BLOCK + threadIdx.x; i < n_it; i += gridDim.x * MP_BLOCK) {
+        unsigned r;
+        int x, y, z;
+        if (a.cpos) {
+            const uint32_t c = __ldg(a.cpos + i);
+            x = (int)(c & ((1u << a.xbits) - 1u));
+            y = (int)((c >> a.xbits) & ((1u << a.ybits) - 1u));
+            z = (int)(c >> (a.xbits + a.ybits));
+            r = (unsigned)x + (unsigned)a.lx * ((unsigned)y + (unsigned)a.ly * (unsigned)z);
+        } else {
+            r = i;
+            x = (int)(r % (unsigned)a.lx);
+            const unsigned yz = r / (unsigned)a.lx;
+            y = (int)(yz % (unsigned)a.ly);
+            z = (int)(yz / (unsigned)a.ly);
+        }
         const uint32_t m = __ldg(a.mask + r);
         if (!(m & FLUID_BIT)) continue;
-        const int x = (int)(r % (unsigned)a.lx);
-        const unsigned yz = r / (unsigned)a.lx;
-        const int y = (int)(yz % (unsigned)a.ly), z = (int)(yz / (unsigned)a.ly);
         const int sy = a.lx, sz = a.lx * a.ly;
         // [c+1] = coordinate of (x + c), periodic
         const int X[3] = {wrap_minus(x, a.lx), x, wrap_plus(x, a.lx)};
