@@ -45,6 +45,7 @@ void pnp_release(lbgpu_ctx *ctx)
     for (cudaGraphExec_t g : ctx->pnp->sor_exec)
         if (g) cudaGraphExecDestroy(g);
     for (void *p : ctx->pnp->allocs) cudaFree(p);
+    if (ctx->pnp->phi_host) cudaFreeHost(ctx->pnp->phi_host);
     delete ctx->pnp;
     ctx->pnp = nullptr;
 }
@@ -452,12 +453,34 @@ int read4(lbgpu_ctx *ctx, unsigned nb, double out[4])
     return LBGPU_OK;
 }
 
-// anormf0 = sum(abs(phi)) in the reference's order (sor.f90:90), on the host
+// Two block-partial reductions (partials at s->partial and at s->partial + 4 nb) read back with
+// one synchronisation; each is summed exactly as read4 sums it.
+int read4x2(lbgpu_ctx *ctx, unsigned nb, double out0[4], double out1[4])
+{
+    PnpState *s = ctx->pnp;
+    LBG_CK(ctx, cudaGetLastError());
+    k_sum4<<<1, PB, 0, ctx->stream>>>(s->partial, nb, s->result);
+    k_sum4<<<1, PB, 0, ctx->stream>>>(s->partial + 4 * (size_t)nb, nb, s->result + 4);
+    LBG_CK(ctx, cudaGetLastError());
+    double h[8];
+    LBG_CK(ctx, cudaMemcpyAsync(h, s->result, 8 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < 4; ++q) {
+        out0[q] = h[q];
+        out1[q] = h[4 + q];
+    }
+    return LBGPU_OK;
+}
+
+// anormf0 = sum(abs(phi)) in the reference's order (sor.f90:90), on the host, from a page-locked
+// copy (the copy of every solve of the outer loop runs at the link's speed)
 int sum_abs_phi(lbgpu_ctx *ctx, double *out)
 {
     PnpState *s = ctx->pnp;
-    std::vector<double> h(ctx->N);
-    LBG_CK(ctx, cudaMemcpyAsync(h.data(), s->phi[s->par], sizeof(double) * ctx->N, cudaMemcpyDeviceToHost, ctx->stream));
+    if (!s->phi_host) LBG_CK(ctx, cudaMallocHost((void **)&s->phi_host, sizeof(double) * ctx->N));
+    const double *h = s->phi_host;
+    LBG_CK(ctx, cudaMemcpyAsync(s->phi_host, s->phi[s->par], sizeof(double) * ctx->N, cudaMemcpyDeviceToHost,
+                                ctx->stream));
     LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
     double a = 0.0;
     for (long long i = 0; i < ctx->N; ++i) a = a + std::fabs(h[i]);
@@ -508,7 +531,8 @@ int lbgpu_pnp_init(lbgpu_ctx *ctx, const lbgpu_pnp_params *p, double *anormf0)
         return rc;
     for (int q = 0; q < 3; ++q)
         if ((rc = alloc(&s->bak[q], N))) return rc;
-    if ((rc = alloc(&s->partial, 4 * (size_t)MP_MAX_BLOCKS)) || (rc = alloc(&s->result, 4))) return rc;
+    // partials: 4 per block, twice (two reductions read back together); results: 4, twice
+    if ((rc = alloc(&s->partial, 8 * (size_t)MP_MAX_BLOCKS)) || (rc = alloc(&s->result, 8))) return rc;
     LBG_CK(ctx, cudaMalloc((void **)&s->ctl, sizeof(PnpCtl)));
     s->allocs.push_back(s->ctl);
     LBG_CK(ctx, cudaMemsetAsync(s->ctl, 0, sizeof(PnpCtl), st));
@@ -789,9 +813,8 @@ int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *
         // check_charge_distribution_equilibrium.f90:24-44
         double r4[4], q4[4];
         k_rel_change<<<grid, PB, 0, st>>>(s->phi[s->par], s->bak[0], s->cp, s->bak[1], ctx->N, s->partial);
-        if ((rc = read4(ctx, grid, r4))) return rc;
-        k_rel_change<<<grid, PB, 0, st>>>(s->cm, s->bak[2], nullptr, nullptr, ctx->N, s->partial);
-        if ((rc = read4(ctx, grid, q4))) return rc;
+        k_rel_change<<<grid, PB, 0, st>>>(s->cm, s->bak[2], nullptr, nullptr, ctx->N, s->partial + 4 * (size_t)grid);
+        if ((rc = read4x2(ctx, grid, r4, q4))) return rc;
         const double eps = 1.0e-12;
         const double dphi = r4[1] != 0 ? r4[0] / r4[1] : 0.0;
         const double dcp = r4[3] != 0 ? r4[2] / r4[3] : 0.0;

@@ -41,6 +41,9 @@ struct PnpState {
     double *phi_tot = nullptr;
     double *solute_force = nullptr;
     double *adv_fp = nullptr, *adv_fm = nullptr;
+    // page-locked host copy of phi for anormf0 = SUM(ABS(phi)), summed on the host in the
+    // reference's order after every solve (allocated at its first use)
+    double *phi_host = nullptr;
 };
 
 }  // namespace lbg
