@@ -92,6 +92,9 @@ __device__ __forceinline__ long long nb(int x, int y, int z, int dx, int dy, int
 }
 
 // Final sum of the 4-value block partials of the last kernel, in block order.
+// The control block of a solve, set on the device (a kernel parameter, no staged host copy).
+__global__ void k_ctl_set(PnpCtl *ctl, const PnpCtl c) { *ctl = c; }
+
 __global__ void __launch_bounds__(PB) k_sum4(const double *partial, unsigned nb, double *out)
 {
     __shared__ double sh[4][PB / 32];
@@ -650,13 +653,15 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
         c.max_iter = s->p.max_iter > 0 ? s->p.max_iter : 500000;
     }
     a.one_minus_omega = 1.0 - a.omega;
-    LBG_CK(ctx, cudaMemcpyAsync(s->ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st));
+    k_ctl_set<<<1, 1, 0, st>>>(s->ctl, c);
+    LBG_CK(ctx, cudaGetLastError());
     const unsigned grid = grid_for(ctx->N);
-    // sweeps after the exit are no-ops (the control block is done): a graph of 8 sweeps first,
-    // then graphs of 64 until the solve converges or reaches its cap
+    // sweeps after the exit are no-ops (the control block is done): a graph of one sweep first
+    // (in the outer loop of the Poisson-Nernst-Planck solve most solves end at their first
+    // sweep), then graphs of 64 until the solve converges or reaches its cap
     for (int k = 0; k < 2; ++k) {
         if (s->sor_exec[k]) continue;
-        const int G = k == 0 ? 8 : 64;
+        const int G = k == 0 ? 1 : 64;
         cudaGraph_t g;
         LBG_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int q = 0; q < G; ++q) {
