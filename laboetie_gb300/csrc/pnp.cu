@@ -42,6 +42,16 @@ void pnp_release(lbgpu_ctx *ctx)
 {
     if (!ctx->pnp) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    PnpState *ps = ctx->pnp;
+    if (ps->anorm_thread.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(ps->anorm_m);
+            ps->anorm_quit = true;
+        }
+        ps->anorm_cv.notify_all();
+        ps->anorm_thread.join();
+    }
+    if (ps->anorm_ev) cudaEventDestroy(ps->anorm_ev);
     for (cudaGraphExec_t g : ctx->pnp->sor_exec)
         if (g) cudaGraphExecDestroy(g);
     for (void *p : ctx->pnp->allocs) cudaFree(p);
@@ -476,18 +486,61 @@ int read4x2(lbgpu_ctx *ctx, unsigned nb, double out0[4], double out1[4])
 }
 
 // anormf0 = sum(abs(phi)) in the reference's order (sor.f90:90), on the host, from a page-locked
-// copy (the copy of every solve of the outer loop runs at the link's speed)
-int sum_abs_phi(lbgpu_ctx *ctx, double *out)
+// copy of phi.  anorm_begin enqueues the copy and hands the sum to the state's worker thread,
+// which waits for the copy (an event) and adds the values up in element order; anorm_end waits
+// for it and stores anormf0.  Between the two the caller may go on (the outer loop runs its
+// Nernst-Planck update and convergence test, which do not read anormf0).
+void anorm_worker(PnpState *s, long long N, int device)
+{
+    cudaSetDevice(device);   // the context's device, current on this thread too
+    for (;;) {
+        std::unique_lock<std::mutex> lk(s->anorm_m);
+        s->anorm_cv.wait(lk, [s] { return s->anorm_job || s->anorm_quit; });
+        if (s->anorm_quit) return;
+        s->anorm_job = false;
+        lk.unlock();
+        const bool ok = cudaEventSynchronize(s->anorm_ev) == cudaSuccess;
+        double a = 0.0;
+        if (ok)
+            for (long long i = 0; i < N; ++i) a = a + std::fabs(s->phi_host[i]);
+        lk.lock();
+        s->anorm_sum = a;
+        s->anorm_failed = !ok;
+        s->anorm_ready = true;
+        lk.unlock();
+        s->anorm_cv.notify_all();
+    }
+}
+
+int anorm_begin(lbgpu_ctx *ctx)
 {
     PnpState *s = ctx->pnp;
     if (!s->phi_host) LBG_CK(ctx, cudaMallocHost((void **)&s->phi_host, sizeof(double) * ctx->N));
-    const double *h = s->phi_host;
+    if (!s->anorm_ev) LBG_CK(ctx, cudaEventCreateWithFlags(&s->anorm_ev, cudaEventDisableTiming));
+    if (!s->anorm_thread.joinable()) s->anorm_thread = std::thread(anorm_worker, s, ctx->N, ctx->p.device);
     LBG_CK(ctx, cudaMemcpyAsync(s->phi_host, s->phi[s->par], sizeof(double) * ctx->N, cudaMemcpyDeviceToHost,
                                 ctx->stream));
-    LBG_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    double a = 0.0;
-    for (long long i = 0; i < ctx->N; ++i) a = a + std::fabs(h[i]);
-    *out = a;
+    LBG_CK(ctx, cudaEventRecord(s->anorm_ev, ctx->stream));
+    {
+        std::lock_guard<std::mutex> lk(s->anorm_m);
+        s->anorm_job = true;
+        s->anorm_pending = true;
+        s->anorm_ready = false;
+    }
+    s->anorm_cv.notify_all();
+    return LBGPU_OK;
+}
+
+int anorm_end(lbgpu_ctx *ctx)
+{
+    PnpState *s = ctx->pnp;
+    std::unique_lock<std::mutex> lk(s->anorm_m);
+    if (!s->anorm_pending) return LBGPU_OK;
+    s->anorm_cv.wait(lk, [s] { return s->anorm_ready; });
+    s->anorm_pending = false;
+    s->anorm_ready = false;
+    if (s->anorm_failed) return ctx_fail(ctx, LBGPU_ERR_CUDA, "anormf0: copy of phi failed");
+    s->anormf0 = s->anorm_sum;
     return LBGPU_OK;
 }
 
@@ -617,11 +670,22 @@ int lbgpu_pnp_get(lbgpu_ctx *ctx, double *c_plus, double *c_minus, double *phi, 
     return lbgpu_sync(ctx);
 }
 
+static int sor_solve(lbgpu_ctx *ctx, int *iters, bool defer_anorm);
+
 int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
 {
     TraceRange trace_("lbgpu_sor");
     if (!ctx) return LBGPU_ERR_INVALID;
     int rc = need_pnp(ctx, "lbgpu_sor");
+    if (rc) return rc;
+    return sor_solve(ctx, iters, false);
+}
+
+// The solve of lbgpu_sor; with defer_anorm the new anormf0 is still being summed on return
+// (anorm_end, which the next solve calls first, completes it).
+static int sor_solve(lbgpu_ctx *ctx, int *iters, bool defer_anorm)
+{
+    int rc = anorm_end(ctx);   // the limit below uses the previous solve's anormf0
     if (rc) return rc;
     PnpState *s = ctx->pnp;
     cudaStream_t st = ctx->stream;
@@ -709,7 +773,8 @@ int lbgpu_sor(lbgpu_ctx *ctx, int *iters)
     }
     if (!multi) s->par = c.parity;
     if (iters) *iters = s->p.solver == LBGPU_POISSON_SOR4 ? c.iter : c.iter - 1;  // sor.f90:87
-    if ((rc = sum_abs_phi(ctx, &s->anormf0))) return rc;          // sor.f90:90
+    if ((rc = anorm_begin(ctx))) return rc;                       // sor.f90:90
+    if (!defer_anorm && (rc = anorm_end(ctx))) return rc;
     if (!c.converged)
         return ctx_fail(ctx, LBGPU_ERR_STEP_CAP, "maximum iterations 500 000 reached without convergence in sor");
     return LBGPU_OK;
@@ -801,6 +866,11 @@ int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *
     const unsigned grid = grid_for(ctx->N);
     int n = 0, total = 0;
     bool converged = false;
+    // every exit leaves anormf0 complete (no sum still running on the worker thread)
+    struct AnormDone {
+        lbgpu_ctx *ctx;
+        ~AnormDone() { anorm_end(ctx); }
+    } anorm_done_{ctx};
     while (!converged) {
         if (max_outer > 0 && n >= max_outer) {
             if (outer) *outer = n;
@@ -812,7 +882,7 @@ int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *
         LBG_CK(ctx, cudaMemcpyAsync(s->bak[1], s->cp, b, cudaMemcpyDeviceToDevice, st));
         LBG_CK(ctx, cudaMemcpyAsync(s->bak[2], s->cm, b, cudaMemcpyDeviceToDevice, st));
         int it = 0;
-        if ((rc = lbgpu_sor(ctx, &it))) return rc;
+        if ((rc = sor_solve(ctx, &it, true))) return rc;   // anormf0 summed meanwhile
         total += it;
         if ((rc = lbgpu_just_eq_smolu(ctx, nullptr))) return rc;
         // check_charge_distribution_equilibrium.f90:24-44
@@ -829,6 +899,7 @@ int lbgpu_poisson_nernst_planck(lbgpu_ctx *ctx, int max_outer, int *outer, int *
     }
     if (outer) *outer = n;
     if (sor_iters_total) *sor_iters_total = total;
+    if ((rc = anorm_end(ctx))) return rc;
     double sc, fc;
     return lbgpu_charge_test(ctx, &sc, &fc);   // poisson_nernst_planck.f90:50
 }

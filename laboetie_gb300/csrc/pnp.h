@@ -5,6 +5,9 @@
 
 #include <cuda_runtime.h>
 
+#include <condition_variable>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "lbgpu.h"
@@ -42,8 +45,19 @@ struct PnpState {
     double *solute_force = nullptr;
     double *adv_fp = nullptr, *adv_fm = nullptr;
     // page-locked host copy of phi for anormf0 = SUM(ABS(phi)), summed on the host in the
-    // reference's order after every solve (allocated at its first use)
+    // reference's order after every solve (allocated at its first use), by a worker thread of the
+    // state (pnp.cu: anorm_begin / anorm_end), so that the outer loop's Nernst-Planck update and
+    // convergence test run meanwhile
     double *phi_host = nullptr;
+    std::thread anorm_thread;
+    std::mutex anorm_m;
+    std::condition_variable anorm_cv;
+    // job: a sum to start (set by anorm_begin); pending: a sum begun and not yet consumed by
+    // anorm_end; ready: the worker finished it
+    bool anorm_job = false, anorm_pending = false, anorm_ready = false, anorm_quit = false;
+    bool anorm_failed = false;
+    double anorm_sum = 0.0;
+    cudaEvent_t anorm_ev = nullptr;
 };
 
 }  // namespace lbg
