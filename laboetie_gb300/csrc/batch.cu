@@ -674,7 +674,7 @@ cudaError_t batch_configure(int max_smem_bytes)
         const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_bytes);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return cudaFuncSetAttribute(k_batch_mp_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MPS_SMEM);
 }
 
 template <int MINB>

@@ -250,6 +250,7 @@ unsigned mp32_slab_resident()
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaFuncSetAttribute(k_mp32_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MPS_SMEM) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mp32_slab, MP_BLOCK, MPS_SMEM) != cudaSuccess) {
         cudaGetLastError();
         return 0u;

@@ -4,8 +4,9 @@
 // lz >= 3.  A ring of 4 planes of V and P with a one-node halo is filled by asynchronous copies
 // (or bulk tensor copies) ahead of use, so the neighbour reads are shared-memory reads and every
 // V and P value is fetched from L2/HBM about 1.3 times (halo) per step; the column's flag words
-// (and the node's fixed (u*, D)) are loaded into registers ahead of use.  One block barrier per
-// plane.  mp_slab_planes is the difference form of mp_f32.cu:k_mp32 (same operations in the same
+// (and the node's fixed (u*, D)) are loaded into registers ahead of use, and an interfacial
+// node's adsorbed part is copied into a slot of the thread's own two steps before it finishes.
+// One block barrier per plane.  mp_slab_planes is the difference form of mp_f32.cu:k_mp32 (same operations in the same
 // order, so P is bit-identical) visiting each plane once, for single boxes and batched ones alike.
 // The argument struct provides V (its w component: the node's fluid flag, 1 or 0), P[2], A[2],
 // aux, mask, lx, ly, lz, ads, ka, kd, one_minus_kd, a1[3], lwh[3], wait_ns, skip_copies.
@@ -26,8 +27,9 @@ constexpr int SHX = MPS_TX + 2, SHY = MPS_TY + 2, SPL = SHX * SHY;  // a plane w
 // 128-byte boundary)
 constexpr int SPLP = (SPL * 16 + 127) / 128 * 8;
 constexpr unsigned MPS_TMA_BYTES = SPL * 16;                        // one plane of V or of P
-// 4 planes of V and of P, 4 mbarriers, and slack to align the ring to 128 bytes
-constexpr size_t MPS_SMEM = 128 + sizeof(float4) * 8 * SPLP + 4 * sizeof(uint64_t);
+// 4 planes of V and of P, 4 mbarriers, two adsorbed-part slots per thread, and slack to align the
+// ring to 128 bytes
+constexpr size_t MPS_SMEM = 128 + sizeof(float4) * 8 * SPLP + 4 * sizeof(uint64_t) + 2 * MP_BLOCK * sizeof(float4);
 
 // Scattering probability of a link, a1 (c.V) + lambda w / 2 rounded once, or 0 across a
 // bounce-back link (blocked).  The reference multiplies by a 0/1 factor instead; the sums it
@@ -171,6 +173,8 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
     float4 *sm = sm_raw + ((128u - (smem_addr(sm_raw) & 127u)) & 127u) / 16u;
     float4 *sV = sm, *sP = sm + 4 * SPLP;
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 8 * SPLP);   // one per ring slot
+    // this thread's adsorbed-part slots (node z in slot z & 1), filled by its own cp.async
+    float4 *sA = sm + 8 * SPLP + 2 + threadIdx.x;
     const int lx = a.lx, ly = a.ly, lz = a.lz;
     const float4 *__restrict__ Vg = a.V;
     const float4 *__restrict__ Pg = a.P[par];
@@ -264,10 +268,6 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
         float4 axA = zero;
         if constexpr (da)
             if (A.m & FLUID_BIT) axA = __ldg(auxcol + plane * (unsigned)(zz - 1));
-        // the adsorbed part of node zz, read when it finishes at the end of the next step: asked
-        // into L1 now (no register held), so that read does not wait on L2/HBM
-        if constexpr (db)
-            if (a.ads && (B.m & INTERFACIAL_BIT)) prefetch_l1(a.A[par] + col0 + plane * (unsigned)zz);
         if (dc && ok) ok = wait_plane(zz + 1);
         // one verdict for the block: once a wait has run out, no thread uses the ring and no new
         // copy is issued (the per-thread path never fails)
@@ -330,10 +330,21 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
                 vt[1] += p.y * axA.y;
                 vt[2] += p.z * axA.z;
                 mp32_finish(p, axA.w, n0, n1, n2);
-                if (a.ads && (A.m & INTERFACIAL_BIT))
-                    a.A[par ^ 1][col0 + r] = mp32_adsorb(p, a.A[par][col0 + r], a.ka, a.kd, a.one_minus_kd, n0, n1, n2);
+                if (a.ads && (A.m & INTERFACIAL_BIT)) {
+                    cp_async_wait1();   // node zz-1's copy was committed a step ago
+                    a.A[par ^ 1][col0 + r] =
+                        mp32_adsorb(p, sA[((zz - 1) & 1) * MP_BLOCK], a.ka, a.kd, a.one_minus_kd, n0, n1, n2);
+                }
                 __stcs(Pout + r, make_float4(n0, n1, n2, 0.0f));
             }
+        }
+        // node zz+1's adsorbed part into the slot node zz-1 has just read: committed with the next
+        // plane's copies (or on its own where the planes are bulk-copied), it has landed by the
+        // time node zz+1 finishes, two steps on
+        if constexpr (dc) {
+            if (ok && a.ads && (C.m & INTERFACIAL_BIT))
+                cp_async16(sA + ((zz + 1) & 1) * MP_BLOCK, a.A[par] + col0 + plane * (unsigned)(zz + 1));
+            if (tma) cp_async_commit();
         }
     };
     using T = std::true_type;
@@ -354,6 +365,7 @@ __device__ __forceinline__ void mp_slab_planes(const Args &a, int par, int x0, i
         S1 = S2;
     }
     step(T{}, F{}, F{}, S0, S1, S2, z1);   // the last node's links from plane z1
+    cp_async_wait0();   // no copy of this thread still lands when the block leaves
     if (!ok) {
         // a wait ran out: let the copies already issued into this block's shared memory land
         // (each wait bounded again) before the block leaves, then report
