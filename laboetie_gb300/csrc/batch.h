@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "mp.h"
 
 namespace lbg {
 
@@ -92,8 +93,8 @@ constexpr int BATCH_SLAB_ZC = 16;   // planes per slab tile
 // slab tiles of a box (0: not eligible)
 __host__ __device__ inline int batch_slab_tiles(int lx, int ly, int lz)
 {
-    if (lx < 32 || ly < 8 || lz < 3) return 0;
-    return ((lx + 31) / 32) * ((ly + 7) / 8) * ((lz + BATCH_SLAB_ZC - 1) / BATCH_SLAB_ZC);
+    if (lx < MPS_TX || ly < MPS_TY || lz < 3) return 0;
+    return ((lx + MPS_TX - 1) / MPS_TX) * ((ly + MPS_TY - 1) / MPS_TY) * ((lz + BATCH_SLAB_ZC - 1) / BATCH_SLAB_ZC);
 }
 // Shared-memory boxes: list holds nflow boxes in the flow phase, then nmp in the tracer phase,
 // each group with its own dynamic shared memory size.  du: one word per descriptor, max

@@ -790,14 +790,14 @@ int lbgpu_batch_add(lbgpu_batch *b, const lbgpu_cell *c, const int8_t *nature, i
     const int nslab = compact && tracer && slab_ok ? batch_slab_tiles(c->lx, c->ly, c->lz) : 0;
     const int ntacc = std::max((int)((units + BATCH_BLOCK - 1) / BATCH_BLOCK), nslab);
     sl.slab_live.clear();
-    if (nslab) {   // slab tile k: column tile k % nxy (32 x 8), planes [zc (k / nxy), + zc)
-        const int tx = (c->lx + 31) / 32, nxy = tx * ((c->ly + 7) / 8);
+    if (nslab) {   // slab tile k: column tile k % nxy (MPS_TX x MPS_TY), planes [zc (k / nxy), + zc)
+        const int tx = (c->lx + MPS_TX - 1) / MPS_TX, nxy = tx * ((c->ly + MPS_TY - 1) / MPS_TY);
         for (int k = 0; k < nslab; ++k) {
-            const int t = k % nxy, x0 = (t % tx) * 32, y0 = (t / tx) * 8, z0 = (k / nxy) * BATCH_SLAB_ZC;
+            const int t = k % nxy, x0 = (t % tx) * MPS_TX, y0 = (t / tx) * MPS_TY, z0 = (k / nxy) * BATCH_SLAB_ZC;
             bool fluid = false;
             for (int z = z0; z < std::min(z0 + BATCH_SLAB_ZC, c->lz) && !fluid; ++z)
-                for (int y = y0; y < std::min(y0 + 8, c->ly) && !fluid; ++y)
-                    for (int x = x0; x < std::min(x0 + 32, c->lx); ++x)
+                for (int y = y0; y < std::min(y0 + MPS_TY, c->ly) && !fluid; ++y)
+                    for (int x = x0; x < std::min(x0 + MPS_TX, c->lx); ++x)
                         if (nature[(size_t)x + (size_t)c->lx * ((size_t)y + (size_t)c->ly * z)] == 0) {
                             fluid = true;
                             break;
