@@ -55,6 +55,8 @@ def args_():
     ap.add_argument("--mp-steps", type=int, default=0, help="default: min(steps, 400)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-seconds", type=float, default=120.0,
+                    help="--impl reference: the most its timed run may take (fewer steps than --steps then)")
     # batched cells (1024 chromatography cells + 64 modulated tubes, flow then tracer)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-cells", type=int, default=1024)
@@ -636,15 +638,24 @@ def run_reference(a):
 
     nature = geo.porous_spheres(a.size, RADIUS, POROSITY, SEED)
     threads = os.cpu_count() or 1
-    # --warmup untimed steps (a short run), then K timed samples of the same workload
+    nfluid = int((nature == 0).sum())
+    # --warmup untimed steps (one run), then one timed run of --steps steps of the full box, or of
+    # as many as fit in --reference-seconds when those would not (the line gives the count timed)
     import oracle
 
     oracle.build()
-    oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=1, nthreads=threads)
-    mlups, steps, dt, _ = cpu_oracle_mlups(nature, a.cpu_seconds, threads)
+    W = max(a.warmup, 1)
+    t = time.perf_counter()
+    oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=W, nthreads=threads)
+    per_step = (time.perf_counter() - t) / W
+    steps = max(1, min(a.steps, int(a.reference_seconds / per_step)))
+    t = time.perf_counter()
+    oracle.equilibration(nature, tau=TAU, f_ext=FEXT, fixed_steps=steps, nthreads=threads)
+    dt = time.perf_counter() - t
+    mlups = nfluid * steps / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(mlups, 4),
-        "unit": "MLUPS", "n_gpus": a.gpus, "steps": steps, "warmup": 1,
+        "unit": "MLUPS", "n_gpus": a.gpus, "steps": steps, "warmup": W,
         "ms_per_step": round(dt / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded porous medium)",
         "config": config_of(1, nature), "parallelism": "openmp",

@@ -62,11 +62,12 @@ def test_max_over_ranks_and_barriers_gloo():
 
 def test_reference_arm_runs_on_rank_zero_only():
     cmd = [sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--size", "16",
-           "--cpu-seconds", "0.2"]
+           "--steps", "4", "--warmup", "2"]
     outs = run_ranks(cmd, timeout=300)
     (rc0, o0, e0), (rc1, o1, e1) = outs
     assert rc0 == 0 and rc1 == 0, (e0, e1)
     line = json.loads(o0.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0 and line["n_gpus"] == 2
+    assert line["steps"] == 4 and line["warmup"] == 2   # the steps asked for, timed in full
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
     assert o1.strip() == ""
