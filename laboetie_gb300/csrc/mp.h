@@ -96,10 +96,11 @@ struct MpArgs32 {
 // of z planes.  Used when lx >= 32, ly >= 8 and lz >= 3.  Returns the grid (0: not eligible) and
 // the planes per block in *zc.  A chunk reads two planes beyond its own, so the chunks are as long
 // as filling the device once allows (resident: blocks resident at once), and at least 8 planes.
+// resident 0 (the step's shared memory could not be granted): not eligible.
 constexpr int MPS_TX = 32, MPS_TY = 8;
 inline unsigned mp32_slab_grid(int lx, int ly, int lz, unsigned resident, int *zc)
 {
-    if (lx < MPS_TX || ly < MPS_TY || lz < 3) return 0;
+    if (lx < MPS_TX || ly < MPS_TY || lz < 3 || resident == 0) return 0;
     const int nxy = ((lx + MPS_TX - 1) / MPS_TX) * ((ly + MPS_TY - 1) / MPS_TY);
     int nz = (int)(resident / (unsigned)nxy);
     if (nz > lz / 8) nz = lz / 8;
