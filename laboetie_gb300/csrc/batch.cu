@@ -598,7 +598,10 @@ __global__ void __launch_bounds__(MAXT, 1) k_batch_smem_mp(const BatchInst *__re
         msk[i] = I.mask[i];
     }
     __syncthreads();
-    double sum[3] = {0.0, 0.0, 0.0}, last[3] = {0.0, 0.0, 0.0};
+    // this thread's VACF terms: summed over the call's steps in FP64, and the last step's; the
+    // block adds them up once, after the last step
+    double sum[3] = {0.0, 0.0, 0.0};
+    float last32[3] = {0.0f, 0.0f, 0.0f};
     unsigned bad = 0;
     for (int s = 0; s < nsteps; ++s) {
         const bool odd = s & 1;
@@ -610,14 +613,15 @@ __global__ void __launch_bounds__(MAXT, 1) k_batch_smem_mp(const BatchInst *__re
             const uint32_t m = msk[node];
             if (m & FLUID_BIT) mp_node<false>(V, Pn, Px, An, Ax, I.aux, node, w.x, w.y, w.z, m, I, vt32, bad);
         }
-        double vt[3] = {(double)vt32[0], (double)vt32[1], (double)vt32[2]};
-        block_sum3(vt);  // its barriers also separate this step from the next
-        if (threadIdx.x == 0)
-            for (int d = 0; d < 3; ++d) {
-                sum[d] += vt[d];
-                last[d] = vt[d];
-            }
+        for (int d = 0; d < 3; ++d) {
+            sum[d] += (double)vt32[d];
+            last32[d] = vt32[d];
+        }
+        __syncthreads();   // this step's P before the next step reads it
     }
+    double last[3] = {(double)last32[0], (double)last32[1], (double)last32[2]};
+    block_sum3(sum);
+    block_sum3(last);
     __syncthreads();
     for (unsigned i = threadIdx.x; i < N; i += T) {
         I.P[0][i] = P0[i];
