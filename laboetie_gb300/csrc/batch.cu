@@ -151,9 +151,13 @@ __device__ __forceinline__ void mp_node(const float4 *V, const float4 *Pn, float
         constexpr int l = INIT ? decltype(L)::value : mp_link_order(decltype(L)::value);
         constexpr Vel c = vel(l);
         constexpr int w = wclass(l);
-        const bool blocked = (m >> inv(l)) & 1u;  // r + c_l is solid
         const unsigned rp = (unsigned)(X[c.x + 1] + Y[c.y + 1] + Z[c.z + 1]);
-        const float spp = mp32_scatter(blocked, I.a1[w], mp32_cdot<-c.x, -c.y, -c.z>(V[rp]), I.lwh[w]);
+        const bool blocked = INIT && ((m >> inv(l)) & 1u);  // r + c_l is solid
+        // a step takes the neighbour's fluid flag from V.w (V = 0 on a solid node): the bits of
+        // mp32_scatter with no test of the link's bit
+        const float4 vn = V[rp];
+        const float spp = INIT ? mp32_scatter(blocked, I.a1[w], mp32_cdot<-c.x, -c.y, -c.z>(vn), I.lwh[w])
+                               : mp32_scatter_flag(I.a1[w], mp32_cdot<-c.x, -c.y, -c.z>(vn), __fmul_rn(I.lwh[w], vn.w));
         if constexpr (INIT) {
             const float sp = mp32_scatter(blocked, I.a1[w], mp32_cdot<c.x, c.y, c.z>(vr), I.lwh[w]);
             frac -= sp;
