@@ -133,7 +133,44 @@ def test_tracer_bit_exact(oracle_mod, name, make, tau, f_ext, adsorb):
     mp.close()
 
 
+@pytest.mark.parametrize("adsorb", [False, True])
+@pytest.mark.parametrize("name,shape,frac,seed", [("random-7x5x6", (7, 5, 6), 0.3, 11),
+                                                  ("random-9x8x3", (9, 8, 3), 0.2, 12),
+                                                  ("random-2x3x5", (2, 3, 5), 0.25, 13)])
+def test_tracer_bit_exact_on_ragged_boxes(oracle_mod, name, shape, frac, seed, adsorb):
+    """The tracer restatements agree on ragged random boxes (thin axes, bounce-back links in
+    every direction) from synthetic moments: any flow state is a valid input to both."""
+    nat = _random_nature(shape, frac, seed)
+    rng = np.random.default_rng(seed + 100)
+    fl = nat == 0
+    rho = np.where(fl, 1.0 + 0.01 * rng.standard_normal(nat.shape), 0.0)
+    j = [np.where(fl, 2e-4 * rng.standard_normal(nat.shape), 0.0) for _ in range(3)]
+    f_ext = (1e-5, -2e-6, 3e-6)
+    ka, kd = (0.01 * math.e, 0.01) if adsorb else (0.0, 0.0)
+    nmp = oracle_mod.update_tracer_population(nat, rho, j, f_ext, 0.0, 0.01)
+    nmp2 = npo.update_tracer_population(nat, rho, j, f_ext)
+    assert np.array_equal(nmp2, nmp.reshape(nmp2.shape))
+    mp = oracle_mod.MomentPropagation(nat, oracle_mod.detect_interfacial(nat), rho, nmp,
+                                      ka=ka, kd=kd, Db=0.01)
+    mp2 = npo.MomentPropagation(nat, rho, nmp2, ka=ka, kd=kd, Db=0.01)
+    scale = np.abs(mp.vacf0).max()
+    assert np.max(np.abs(mp2.vacf0 - mp.vacf0)) <= 1e-12 * scale
+    for it in range(1, 121):
+        v, conv = mp.propagate(it)
+        v2, conv2 = mp2.propagate(it)
+        assert conv2 == conv
+        assert np.max(np.abs(v2 - v)) <= 1e-12 * scale
+        if conv:
+            break
+    assert np.array_equal(mp2.P, mp.P().reshape(mp2.P.shape)) and np.abs(mp2.P).max() > 0
+    if adsorb:
+        assert np.array_equal(mp2.A, mp.Pads().reshape(mp2.A.shape))
+    mp.close()
+
+
 @pytest.mark.parametrize("name,make", [("slit64", lambda: geo.slit(1, 1, 64)),
+                                       ("random-7x5x6", lambda: _random_nature((7, 5, 6), 0.3, 21)),
+                                       ("random-5x9x4", lambda: _random_nature((5, 9, 4), 0.35, 22)),
                                        ("cc8", lambda: geo.cc(8, 8, 8)),
                                        ("cyl", lambda: geo.cylinder(9, 9, 4))])
 def test_poisson_sweeps_bit_exact(oracle_mod, name, make):
