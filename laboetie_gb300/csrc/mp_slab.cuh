@@ -56,16 +56,6 @@ __device__ __forceinline__ void mp32_link(float spp, const float4 &pn, const flo
     n2 = __fmaf_rn(spp, __fsub_rn(pn.z, p.z), n2);
 }
 
-// The same with the x and y sums as one pair: packed FP32 operations (add.rn.f32x2 and
-// fma.rn.f32x2 round each element as the scalar operation does, and pn - p = pn + (-p) exactly),
-// so the bits are those of mp32_link with two instructions fewer per link.
-__device__ __forceinline__ void mp32_link2(float spp, const float4 &pn, const float4 &p, float2 &nxy, float &nz)
-{
-    const float2 d = __fadd2_rn(make_float2(pn.x, pn.y), make_float2(-p.x, -p.y));
-    nxy = __ffma2_rn(make_float2(spp, spp), d, nxy);
-    nz = __fmaf_rn(spp, __fsub_rn(pn.z, p.z), nz);
-}
-
 // End of an FP32 step: n = P(r) + (n + D P(r)), D = sum sp_in - sum sp_out of the node.
 __device__ __forceinline__ void mp32_finish(const float4 &p, float D, float &n0, float &n1, float &n2)
 {
