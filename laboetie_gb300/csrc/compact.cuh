@@ -37,7 +37,8 @@ __device__ __forceinline__ unsigned lattice_of(const A &a, unsigned c)
 
 // Element index of the slot read for each direction by the gather of an odd AA launch at the
 // compact node i (packed position c, flag word m): slot l of the node itself across a bounce-back
-// link, else slot inv(l) of the fluid node x - c_l.  f(l, o) is called for every l.
+// link, else slot inv(l) of the fluid node x - c_l (the reference's halfway bounce-back and
+// streaming, equilibration.f90:204-243, in pull form).  f(l, o) is called for every l.
 // Within a lattice row the fluid nodes are consecutive compact indices, so one table lookup per
 // neighbouring row gives cnt = the compact index the node x would have in that row (fluid nodes
 // before x); its neighbours x -+ 1 in the row are then cnt - 1 and cnt + fluid(x) (x - 1 and

@@ -1,6 +1,7 @@
 // pnp.h -- device state of the charged-solute operators of a context: the Poisson-Nernst-Planck
 // equilibration (pnp.cu) and the coupled electrokinetic operators (ek.cu) share the potential and
-// the ion densities.
+// the ion densities (the reference's module variables phi, c_plus, c_minus, phi_tot and their
+// previous values, module_system.f90:79-84).
 #pragma once
 
 #include <cuda_runtime.h>
