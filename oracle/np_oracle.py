@@ -285,6 +285,92 @@ class MomentPropagation:
 
 # ---------------------------------------------------------------------------------- Poisson
 
+def charges_init(nature, interfacial, bjl, sigma, lambda_D):
+    """charges_init.f90:3-130 with charge_distrib 'int' (the only distribution the reference
+    lets through, :96-100): the surface charge sigma on the interfacial solid nodes, its opposite
+    spread over the fluid nodes on top of the salt 0.5 rho_0, phi = 0, and
+    anormf0 = 4 pi bjl kBT / 2 * SUM(c+ + c-).  Returns (c+, c-, phi, anormf0, rho_ch)."""
+    zeros = np.zeros(nature.shape)
+    if bjl <= EPS_DP:
+        return zeros, zeros.copy(), zeros.copy(), 0.0, 0.0
+    four_pi_bjl = np.float64(4.0) * PI * bjl
+    rho_ch = np.float64(1.0) / (four_pi_bjl * (lambda_D * lambda_D))
+    rho_0 = 0.0 if abs(lambda_D) <= EPS_DP else float(rho_ch)
+    solid, fluid = nature == SOLID, nature == FLUID
+    inter = np.asarray(interfacial).astype(bool)
+    n_solid_int, n_fluid = int((solid & inter).sum()), int(fluid.sum())
+    if abs(sigma) <= EPS_DP:
+        return zeros, zeros.copy(), zeros.copy(), 0.0, float(rho_ch)
+    sigma_solid = sigma / n_solid_int if n_solid_int != 0 else 0.0
+    sigma_fluid = -1.0 * sigma / n_fluid if n_fluid != 0 else 0.0
+    p_solid, m_solid = 0.5 * sigma_solid, -0.5 * sigma_solid
+    if sigma_fluid > 0.0:
+        p_fluid, m_fluid = 0.5 * rho_0 + sigma_fluid, 0.5 * rho_0
+    else:
+        p_fluid, m_fluid = 0.5 * rho_0, 0.5 * rho_0 - sigma_fluid
+    cp = np.where(solid & inter, p_solid, np.where(fluid, p_fluid, 0.0))
+    cm = np.where(solid & inter, m_solid, np.where(fluid, m_fluid, 0.0))
+    anormf0 = 4.0 * PI * bjl * KBT / 2.0 * _seq_sum(cp + cm)
+    return cp, cm, zeros, anormf0, float(rho_ch)
+
+
+# delta of a link: 1 for a nearest neighbour, sqrt(2) for a next-nearest (module_lbmodel.f90:137,147)
+_DELTA = [0.0] + [1.0] * 6 + [math.sqrt(2.0)] * 12
+
+
+def just_eq_smolu(nature, phi, c_plus, c_minus, D_plus, D_minus, rho_ch, sigma, loop_bug=True):
+    """just_eq_smolu.f90:6-135 as poisson_nernst_planck calls it: time is 0 (init_simu.f90:57)
+    and D_equil is never set (0), so the first branch holds: eD = 0.1 D, at most 10 iterations.
+    Each iteration sums the link fluxes of every fluid-fluid link l = 2, 4, .., 18 (one of each
+    pair of opposite velocities) into both of its sites, in the reference's loop order (i outer,
+    j, k, l inner; with the reference's loop bounds j and k take only their last value,
+    loop_bug), checks that the fluxes add up to zero, adds them to the fluid nodes and forms the
+    relative residuals.  Returns (c+, c-, iterations)."""
+    lz, ly, lx = nature.shape
+    cp = np.array(c_plus, dtype=np.float64)
+    cm = np.array(c_minus, dtype=np.float64)
+    phi = np.asarray(phi, dtype=np.float64)
+    fluid = nature == FLUID
+    n_fluid = int(fluid.sum())
+    eDp, eDm = 0.1 * D_plus, 0.1 * D_minus
+    crit = float(np.float32(5.e-6))
+    tot_p = tot_m = float(np.finfo(np.float64).max)
+    links = range(1, 19, 2)
+    js = [ly - 1] if loop_bug else range(ly)
+    ks = [lz - 1] if loop_bug else range(lz)
+    it = 0
+    while tot_m + tot_p > crit and it < 10:
+        fp = np.zeros(nature.shape)
+        fm = np.zeros(nature.shape)
+        for i in range(lx):
+            for j in js:
+                for k in ks:
+                    for l in links:
+                        ip, jp, kp = (i + C[l][0]) % lx, (j + C[l][1]) % ly, (k + C[l][2]) % lz
+                        if not (fluid[k, j, i] and fluid[kp, jp, ip]):
+                            continue
+                        e = math.exp(phi[kp, jp, ip] - phi[k, j, i])
+                        em = 1.0 / e
+                        flp = 0.5 * (1.0 + em) * (cp[kp, jp, ip] * e - cp[k, j, i])
+                        flp = flp * eDp / _DELTA[l]
+                        flm = 0.5 * (1.0 + e) * (cm[kp, jp, ip] * em - cm[k, j, i])
+                        flm = flm * eDm / _DELTA[l]
+                        fp[k, j, i] = fp[k, j, i] + flp
+                        fm[k, j, i] = fm[k, j, i] + flm
+                        fp[kp, jp, ip] = fp[kp, jp, ip] - flp
+                        fm[kp, jp, ip] = fm[kp, jp, ip] - flm
+        lim = float(np.float32(1.e-12))
+        if abs(_seq_sum(fp)) > lim or abs(_seq_sum(fm)) > lim:
+            raise RuntimeError("the sum of all flux does not add up. problem in just_eq_smolu.f90")
+        cp = np.where(fluid, cp + fp, cp)
+        cm = np.where(fluid, cm + fm, cm)
+        if sigma != 0 and eDp != 0.0 and eDm != 0.0:
+            tot_p = math.sqrt(_seq_sum((fp * fp)[fluid])) / n_fluid / (0.5 * rho_ch * eDp) / sigma
+            tot_m = math.sqrt(_seq_sum((fm * fm)[fluid])) / n_fluid / (0.5 * rho_ch * eDm) / sigma
+        it = it + 1
+    return cp, cm, it
+
+
 def sor(nature, sigma, bjl, c_plus, c_minus, phi, anormf0, maxiter=500000):
     """sor.f90:7-91: over-relaxed Jacobi (omega 1.4) over every node, phi* = sum_l a0(l)
     phi(x - c_l) + 4 pi bjl kBT/2 (c+ - c-), stop when sum|phi* - phi| <= 1e-5 anormf0 (the

@@ -3,8 +3,9 @@
 oracle/lb_oracle.c (C) and oracle/np_oracle.py (numpy) were each written from the Fortran
 sources of the reference.  The reference cannot be compiled here (no Fortran compiler), so its
 own outputs are not available; two restatements that agree to the last bit on the collision,
-the bounce-back + streaming, the moments, the whole flow loop, the tracer init and propagation
-and the Poisson sweeps make a misreading of the Fortran by either one visible.  Sums that the
+the bounce-back + streaming, the moments, the whole flow loop, the tracer init and propagation,
+charges_init, the Poisson sweeps and the Nernst-Planck update make a misreading of the Fortran
+by either one visible.  Sums that the
 reference itself forms in an unspecified order (OpenMP reductions of the VACF) are compared to
 1e-12 of |VACF(0)|.
 """
@@ -183,6 +184,46 @@ def test_poisson_sweeps_bit_exact(oracle_mod, name, make):
     assert it_n == it_o
     assert np.array_equal(phi_n, phi_o)
     assert an_n == an_o
+
+
+PNP_BOXES = [("slit64", lambda: geo.slit(1, 1, 64)),
+             ("cc8", lambda: geo.cc(8, 8, 8)),
+             ("cyl", lambda: geo.cylinder(9, 9, 4)),
+             ("random-7x5x6", lambda: _random_nature((6, 5, 7), 0.3, 21))]
+
+
+def _charged(oracle_mod, nat):
+    inter = oracle_mod.detect_interfacial(nat)
+    return inter, -0.01 * int(((nat == 1) & (inter == 1)).sum())
+
+
+@pytest.mark.parametrize("name,make", PNP_BOXES)
+def test_charges_init_bit_exact(oracle_mod, name, make):
+    nat = make()
+    inter, sigma = _charged(oracle_mod, nat)
+    ref = oracle_mod.charges_init(nat, inter, 0.4, sigma, 4.0)
+    got = npo.charges_init(nat, inter, 0.4, sigma, 4.0)
+    for a, b in zip(got[:3], ref[:3]):
+        assert np.array_equal(a, b)
+    assert got[3] == ref[3] and got[4] == ref[4] and got[3] > 0
+
+
+@pytest.mark.parametrize("loop_bug", [True, False])
+@pytest.mark.parametrize("name,make", PNP_BOXES)
+def test_just_eq_smolu_bit_exact(oracle_mod, name, make, loop_bug):
+    """The Nernst-Planck update of the two restatements, from the charged state after the
+    reference Poisson solve, with the reference's loop bounds (only the line (i, ly, lz) starts
+    links) and with full ones: densities and iteration counts bit for bit."""
+    nat = make()
+    inter, sigma = _charged(oracle_mod, nat)
+    cp, cm, phi, an, rho_ch = oracle_mod.charges_init(nat, inter, 0.4, sigma, 4.0)
+    phi_o, _, _ = oracle_mod.sor(nat, sigma, 0.4, cp, cm, phi, an)
+    ref = oracle_mod.just_eq_smolu(nat, phi_o, cp, cm, 0.05, 0.05, rho_ch, sigma, loop_bug=loop_bug)
+    got = npo.just_eq_smolu(nat, phi_o, cp, cm, 0.05, 0.05, rho_ch, sigma, loop_bug=loop_bug)
+    assert got[2] == ref[2] >= 1
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    if not loop_bug:
+        assert not np.array_equal(got[0], cp)   # charge moved
 
 
 def _collide_regrouped(nature, tau, n, rho, jx, jy, jz, fx, fy, fz):
