@@ -397,6 +397,52 @@ def sor(nature, sigma, bjl, c_plus, c_minus, phi, anormf0, maxiter=500000):
     return phi, _seq_sum(np.abs(phi)), it - 1
 
 
+def check_charge_distribution_equilibrium(phi, phi_old, c_plus, c_plus_old, c_minus, c_minus_old):
+    """check_charge_distribution_equilibrium.f90:24-44: for phi, c+ and c-, the mean over the
+    nodes whose previous value exceeds 1e-12 in magnitude of |(new - old)/old| (a masked SUM in
+    element order over the count); converged when all three are below 1e-12.  Returns
+    (converged, (dphi, dcp, dcm))."""
+    eps = 1.0e-12
+    d = []
+    for new, old in ((phi, phi_old), (c_plus, c_plus_old), (c_minus, c_minus_old)):
+        mask = np.abs(old) > eps
+        n = int(mask.sum())
+        rel = np.abs((new[mask] - old[mask]) / old[mask])
+        d.append(_seq_sum(rel) / float(n) if n else 0.0)
+    return bool(d[0] < eps and d[1] < eps and d[2] < eps), tuple(d)
+
+
+def charge_test(nature, c_plus, c_minus, sigma):
+    """charge_test.f90:6-26: SUM(c+ - c-) over the solid and over the fluid nodes must stay sigma
+    and -sigma within the default-real tolerance 1.0e-10.  Returns (ok, solid, fluid)."""
+    q = c_plus - c_minus
+    solid = _seq_sum(q[nature == SOLID])
+    fluid = _seq_sum(q[nature == FLUID])
+    tol = float(np.float32(1.0e-10))
+    return not (abs(solid - sigma) > tol or abs(fluid + sigma) > tol), solid, fluid
+
+
+def pnp(nature, bjl, sigma, D_plus, D_minus, rho_ch, c_plus, c_minus, phi, anormf0, loop_bug=True,
+        max_outer=10000):
+    """poisson_nernst_planck.f90:38-48: until converged, back up phi, c+, c- (backup_phi_c_plus_
+    c_minus), solve Poisson (sor, which also refreshes anormf0), one Nernst-Planck update, and
+    test convergence (every outer iteration: time stays 0, so modulo(time, 10) is 0).  Stops
+    unconverged after max_outer iterations.  Returns the fields, anormf0, the outer count, the
+    total of the sweep counts sor reports and whether it converged."""
+    cp, cm, ph = (np.array(a, dtype=np.float64) for a in (c_plus, c_minus, phi))
+    outer = total = 0
+    converged = False
+    while not converged and outer < max_outer:
+        po, cpo, cmo = ph.copy(), cp.copy(), cm.copy()
+        ph, anormf0, it = sor(nature, sigma, bjl, cp, cm, ph, anormf0)
+        total += it
+        cp, cm, _ = just_eq_smolu(nature, ph, cp, cm, D_plus, D_minus, rho_ch, sigma, loop_bug)
+        converged, _ = check_charge_distribution_equilibrium(ph, po, cp, cpo, cm, cmo)
+        outer += 1
+    return dict(c_plus=cp, c_minus=cm, phi=ph, anormf0=anormf0, outer=outer, sor_iters=total,
+                converged=converged)
+
+
 # --------------------------------------------------------------- coupled electrokinetics
 
 _exp = np.vectorize(math.exp, otypes=[np.float64])   # the C library's exp, as the C oracle's

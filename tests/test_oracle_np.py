@@ -4,8 +4,9 @@ oracle/lb_oracle.c (C) and oracle/np_oracle.py (numpy) were each written from th
 sources of the reference.  The reference cannot be compiled here (no Fortran compiler), so its
 own outputs are not available; two restatements that agree to the last bit on the collision,
 the bounce-back + streaming, the moments, the whole flow loop, the tracer init and propagation,
-charges_init, the Poisson sweeps and the Nernst-Planck update make a misreading of the Fortran
-by either one visible.  Sums that the
+charges_init, the Poisson sweeps, the Nernst-Planck update and the outer Poisson-Nernst-Planck
+loop with its convergence and charge tests make a misreading of the Fortran by either one
+visible.  Sums that the
 reference itself forms in an unspecified order (OpenMP reductions of the VACF) are compared to
 1e-12 of |VACF(0)|.
 """
@@ -224,6 +225,29 @@ def test_just_eq_smolu_bit_exact(oracle_mod, name, make, loop_bug):
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     if not loop_bug:
         assert not np.array_equal(got[0], cp)   # charge moved
+
+
+@pytest.mark.parametrize("loop_bug", [True, False])
+@pytest.mark.parametrize("name,make", PNP_BOXES)
+def test_pnp_outer_loop_bit_exact(oracle_mod, name, make, loop_bug):
+    """Three outer iterations of the Poisson-Nernst-Planck loop (backup, Poisson solve, one
+    Nernst-Planck update, convergence test) in both restatements: fields, anormf0, the sweep
+    total bit for bit, and the charge-conservation test alike."""
+    nat = make()
+    inter, sigma = _charged(oracle_mod, nat)
+    cp, cm, phi, an, rho_ch = oracle_mod.charges_init(nat, inter, 0.4, sigma, 4.0)
+    ref = oracle_mod.pnp(nat, 0.4, sigma, 0.05, 0.05, rho_ch, cp, cm, phi, an, loop_bug=loop_bug,
+                         max_outer=3, check=False)
+    got = npo.pnp(nat, 0.4, sigma, 0.05, 0.05, rho_ch, cp, cm, phi, an, loop_bug=loop_bug,
+                  max_outer=3)
+    assert got["outer"] == ref["outer"] and got["sor_iters"] == ref["sor_iters"]
+    for k in ("c_plus", "c_minus", "phi"):
+        assert np.array_equal(got[k], ref[k])
+    assert got["anormf0"] == ref["anormf0"]
+    assert got["converged"] == (ref["status"] == 0)
+    rc, s_ref, f_ref = oracle_mod.charge_test(nat, ref["c_plus"], ref["c_minus"], sigma)
+    ok, s_got, f_got = npo.charge_test(nat, got["c_plus"], got["c_minus"], sigma)
+    assert (s_got, f_got) == (s_ref, f_ref) and ok == (rc == 0)
 
 
 def _collide_regrouped(nature, tau, n, rho, jx, jy, jz, fx, fy, fz):
