@@ -125,11 +125,67 @@ def moments(n, fx, fy, fz, jx_old, jy_old, jz_old):
     return negative, rho, (jx, jy, jz), float(l2err)
 
 
+def _norm2(v):
+    """gfortran's NORM2 of a short vector: scaled sum of squares, the scale starting at 1."""
+    result, scale = 0.0, 1.0
+    for x in v:
+        if x != 0.0:
+            ax = abs(x)
+            if scale < ax:
+                val = scale / ax
+                result = 1.0 + result * val * val
+                scale = ax
+            else:
+                val = ax / scale
+                result = result + val * val
+    return scale * math.sqrt(result)
+
+
+def compensated_force_field(nature, f_ext, particle_diameter=1, particle_coords=(0, 0, 0),
+                            geometry_label=0):
+    """equilibration.f90:388-487 (compensate_f_ext): f_ext on the fluid nodes of a ball of odd
+    diameter pd around the particle centre (1-based coordinates; 0 takes the reference's default
+    n/2+1), split evenly over its nodes; in a bulk box (geometryLabel -1) every fluid node also
+    carries -f_ext / (fluid nodes), so that the total force is zero; 0 on solid nodes."""
+    lz, ly, lx = nature.shape
+    pd = particle_diameter if particle_diameter > 0 else 1
+    if pd % 2 == 0 or lx % 2 == 0 or ly % 2 == 0 or lz % 2 == 0:
+        raise ValueError("compensate_f_ext needs an odd particle diameter and odd box sides")
+    pdr = pd // 2
+    c = [particle_coords[d] if particle_coords[d] > 0 else n // 2 + 1 for d, n in enumerate((lx, ly, lz))]
+    f = [np.zeros(nature.shape) for _ in range(3)]
+    cnt, err = 0, False
+    for i in range(c[0] - pdr, c[0] + pdr + 1):
+        for j in range(c[1] - pdr, c[1] + pdr + 1):
+            for k in range(c[2] - pdr, c[2] + pdr + 1):
+                if _norm2([float(i - c[0]), float(j - c[1]), float(k - c[2])]) > float(pd) / 2.0:
+                    continue
+                if not (1 <= i <= lx and 1 <= j <= ly and 1 <= k <= lz):
+                    raise ValueError("the particle reaches outside the box")
+                if nature[k - 1, j - 1, i - 1] != FLUID:
+                    err = True
+                for d in range(3):
+                    f[d][k - 1, j - 1, i - 1] = f_ext[d]
+                cnt += 1
+    if err:
+        raise ValueError("Dominika's particle at a solid node")
+    n_fluid = int((nature == FLUID).sum())
+    inside = (f[0] == f_ext[0]) & (f[1] == f_ext[1]) & (f[2] == f_ext[2])
+    if geometry_label == -1:
+        f = [np.where(inside, -f_ext[d] / n_fluid + f[d] / cnt, -f_ext[d] / n_fluid) for d in range(3)]
+        if any(abs(_seq_sum(f[d]) / n_fluid) > EPS_DP for d in range(3)):
+            raise ValueError("The compensation is not well-implemented")
+    else:
+        f = [np.where(inside, f[d] / cnt, 0.0) for d in range(3)]
+    return tuple(np.where(nature != FLUID, 0.0, f[d]) for d in range(3))
+
+
 def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), svden=1.0,
-                  max_steps=100000):
-    """The time loop of equilibration.f90:143-491 with the uniform force (no compensate_f_ext):
-    collide, bounce-back, streaming, moments, l2err, and the two-phase force machine (f_ext on
-    fluid nodes from the step after the first convergence, exit at the second)."""
+                  max_steps=100000, compensate_f_ext=False, particle_diameter=1,
+                  particle_coords=(0, 0, 0), geometry_label=0):
+    """The time loop of equilibration.f90:143-491: collide, bounce-back, streaming, moments,
+    l2err, and the two-phase force machine (from the step after the first convergence the force:
+    f_ext on fluid nodes, or the compensated field of compensate_f_ext; exit at the second)."""
     n, rho = init_populations(nature, svden)
     z = np.zeros(nature.shape)
     jx, jy, jz = z.copy(), z.copy(), z.copy()
@@ -151,12 +207,18 @@ def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), sv
             else:
                 with_ = True
             if without and with_ and t > 2:
-                return dict(n=n, rho=rho, j=(jx, jy, jz), steps=t, l2err=np.array(hist))
-            fl = nature == FLUID
-            fx = np.where(fl, f_ext[0], fx)
-            fy = np.where(fl, f_ext[1], fy)
-            fz = np.where(fl, f_ext[2], fz)
-    return dict(n=n, rho=rho, j=(jx, jy, jz), steps=max_steps, l2err=np.array(hist), capped=True)
+                return dict(n=n, rho=rho, j=(jx, jy, jz), steps=t, l2err=np.array(hist),
+                            f=(fx, fy, fz))
+            if compensate_f_ext:
+                fx, fy, fz = compensated_force_field(nature, f_ext, particle_diameter,
+                                                     particle_coords, geometry_label)
+            else:
+                fl = nature == FLUID
+                fx = np.where(fl, f_ext[0], fx)
+                fy = np.where(fl, f_ext[1], fy)
+                fz = np.where(fl, f_ext[2], fz)
+    return dict(n=n, rho=rho, j=(jx, jy, jz), steps=max_steps, l2err=np.array(hist), capped=True,
+                f=(fx, fy, fz))
 
 
 # ------------------------------------------------------------------------ moment propagation

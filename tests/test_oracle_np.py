@@ -3,7 +3,8 @@
 oracle/lb_oracle.c (C) and oracle/np_oracle.py (numpy) were each written from the Fortran
 sources of the reference.  The reference cannot be compiled here (no Fortran compiler), so its
 own outputs are not available; two restatements that agree to the last bit on the collision,
-the bounce-back + streaming, the moments, the whole flow loop, the tracer init and propagation,
+the bounce-back + streaming, the moments, the whole flow loop (with the uniform and with the
+compensated force), the tracer init and propagation,
 charges_init, the Poisson sweeps, the Nernst-Planck update and the outer Poisson-Nernst-Planck
 loop with its convergence and charge tests make a misreading of the Fortran by either one
 visible.  Sums that the
@@ -101,6 +102,27 @@ def test_flow_loop_bit_exact(oracle_mod, name, make, tau, f_ext, target):
     assert np.array_equal(got["l2err"], ref["l2err"])
     assert np.array_equal(got["n"], ref["n"]) and np.array_equal(got["rho"], ref["rho"])
     assert all(np.array_equal(a, b) for a, b in zip(got["j"], ref["j"]))
+
+
+@pytest.mark.parametrize("label,make", [(-1, lambda: geo.bulk(9, 9, 9)),
+                                        (1, lambda: geo.slit(9, 7, 11))])
+def test_flow_loop_with_compensated_force_bit_exact(oracle_mod, label, make):
+    """compensate_f_ext (equilibration.f90:388-487): the force on a particle of diameter 3 at the
+    box centre, with the compensating background in the solid-free box (label -1) and without it
+    between walls: the force field and the whole flow loop bit for bit."""
+    nat = make()
+    fe = (1e-4, 2e-5, 0.0)
+    ref = oracle_mod.equilibration(nat, tau=1.0, target_error=1e-10, f_ext=fe, max_steps=20000,
+                                   compensate_f_ext=True, particle_diameter=3, geometry_label=label)
+    f = npo.compensated_force_field(nat, fe, 3, (0, 0, 0), label)
+    assert all(np.array_equal(f[d], ref["f"][d]) for d in range(3))
+    got = npo.equilibration(nat, tau=1.0, target_error=1e-10, f_ext=fe, max_steps=20000,
+                            compensate_f_ext=True, particle_diameter=3, geometry_label=label)
+    assert got["steps"] == ref["steps"]
+    assert np.array_equal(got["l2err"], ref["l2err"])
+    assert np.array_equal(got["n"], ref["n"]) and np.array_equal(got["rho"], ref["rho"])
+    assert all(np.array_equal(a, b) for a, b in zip(got["j"], ref["j"]))
+    assert all(np.array_equal(a, b) for a, b in zip(got["f"], ref["f"]))
 
 
 @pytest.mark.parametrize("adsorb", [False, True])
