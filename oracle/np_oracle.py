@@ -221,6 +221,26 @@ def equilibration(nature, tau=1.0, target_error=1e-10, f_ext=(0.0, 0.0, 0.0), sv
                 f=(fx, fy, fz))
 
 
+def profiles(rho, j, axis):
+    """equilibration.f90:153-176 (and :504-516 at the loop's exit): per plane k normal to axis
+    (0 = x, 1 = y, 2 = z), SUM(jx), SUM(jy), SUM(jz) and SUM(density) / MAX(COUNT(density > eps),
+    1) over the plane's section, each SUM one accumulator in the section's element order (its
+    first remaining index fastest).  Returns (flux (L, 3), mean density (L,))."""
+    def section(a, k):   # (lz, ly, lx) arrays: x fastest
+        if axis == 0:
+            return a[:, :, k]
+        return a[:, k, :] if axis == 1 else a[k]
+    L = rho.shape[2 - axis]
+    flux = np.zeros((L, 3))
+    dens = np.zeros(L)
+    for k in range(L):
+        for d in range(3):
+            flux[k, d] = _seq_sum(section(j[d], k))
+        sd = section(rho, k)
+        dens[k] = _seq_sum(sd) / max(int((sd > EPS_DP).sum()), 1)
+    return flux, dens
+
+
 # ------------------------------------------------------------------------ moment propagation
 
 def detect_interfacial(nature):

@@ -5,9 +5,9 @@ sources of the reference.  The reference cannot be compiled here (no Fortran com
 own outputs are not available; two restatements that agree to the last bit on the collision,
 the bounce-back + streaming, the moments, the whole flow loop (with the uniform and with the
 compensated force), the tracer init and propagation,
-charges_init, the Poisson sweeps, the Nernst-Planck update and the outer Poisson-Nernst-Planck
-loop with its convergence and charge tests make a misreading of the Fortran by either one
-visible.  Sums that the
+charges_init, the Poisson sweeps, the Nernst-Planck update, the outer Poisson-Nernst-Planck
+loop with its convergence and charge tests and the per-plane profiles make a misreading of the
+Fortran by either one visible.  Sums that the
 reference itself forms in an unspecified order (OpenMP reductions of the VACF) are compared to
 1e-12 of |VACF(0)|.
 """
@@ -123,6 +123,19 @@ def test_flow_loop_with_compensated_force_bit_exact(oracle_mod, label, make):
     assert np.array_equal(got["n"], ref["n"]) and np.array_equal(got["rho"], ref["rho"])
     assert all(np.array_equal(a, b) for a, b in zip(got["j"], ref["j"]))
     assert all(np.array_equal(a, b) for a, b in zip(got["f"], ref["f"]))
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("name,make", BOXES)
+def test_profiles_bit_exact(oracle_mod, name, make, axis):
+    """The per-plane flux and mean-density profiles the reference writes, from a random state:
+    each plane's sums in the reference's element order, bit for bit."""
+    nat = make()
+    n, rho, j, f = _random_state(nat, 7)
+    rho = np.where(nat == 0, rho, 0.0)
+    ref = oracle_mod.profiles(nat, rho, j, axis)
+    got = npo.profiles(rho, j, axis)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
 
 
 @pytest.mark.parametrize("adsorb", [False, True])
